@@ -1,0 +1,386 @@
+"""Benchmark of the P3DFFT 3D r2c + c2r transform path on GB300.
+
+One step = one forward r2c ('fft') plus one backward c2r ('tff') of one
+synthetic grid (the reference sample drivers' timed loop,
+sample/FORTRAN/driver_rand.F90:209-243).  The headline workload is the
+1024^3 FP64 round trip; the line also carries the FP32 form on the same grid.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config large|noncubic|small|cheby]
+  python bench.py --impl reference ...   # the CPU reference arm (oracle port, all host cores)
+
+Under torchrun (N > 1) every rank runs an independent replica of the
+workload on its own GPU (the path does not shard on one GPU per rank):
+value = points of all ranks / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "3D r2c+c2r Gpts/s & %HBM roofline, FP32 vs FP64 at stated error; serve p50/p99"
+UNIT = "Gpts/s"
+
+CONFIGS = {
+    "large": dict(grid=(1024, 1024, 1024), ops=("fft", "tff"),
+                  workload="1024^3 FP64 r2c+c2r round trip (32 seeded Fourier modes + N(0,1e-3) noise)"),
+    "noncubic": dict(grid=(768, 1024, 540), ops=("fft", "tff"),
+                     workload="768x1024x540 FP64 r2c+c2r round trip (32 seeded Fourier modes + N(0,1e-3) noise)"),
+    "small": dict(grid=(128, 128, 128), ops=("fft", "tff"), workload="128^3 FP64 r2c+c2r round trip, U[-1,1)"),
+    "cheby": dict(grid=(512, 512, 257), ops=("ffc", "cff"),
+                  workload="512x512x257 FP64 FFT(x,y) + DCT-I(z) round trip"),
+}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------- inputs
+def make_input(torch, grid, seed, device, kind):
+    """Seeded synthetic field on the device, (nz, ny, nx) float64."""
+    nx, ny, nz = grid
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    if kind == "uniform":
+        return torch.rand((nz, ny, nx), generator=g, device=device, dtype=torch.float64) * 2 - 1
+    rng = np.random.default_rng(seed)
+    x = torch.arange(nx, device=device, dtype=torch.float64) / nx
+    y = torch.arange(ny, device=device, dtype=torch.float64) / ny
+    z = torch.arange(nz, device=device, dtype=torch.float64) / nz
+    f = torch.randn((nz, ny, nx), generator=g, device=device, dtype=torch.float64) * 1e-3
+    kmax = nx / 4
+    for _ in range(32):
+        while True:
+            k = rng.integers(-int(kmax), int(kmax) + 1, size=3)
+            if 0 < np.sqrt((k ** 2).sum()) <= kmax:
+                break
+        amp = rng.uniform(0.5, 1.5)
+        ph = rng.uniform(0, 2 * np.pi)
+        # cos(2 pi (kx x + ky y + kz z) + ph), built separably
+        ax = torch.exp(1j * (2 * np.pi * k[0] * x + ph))
+        ay = torch.exp(1j * 2 * np.pi * k[1] * y)
+        az = torch.exp(1j * 2 * np.pi * k[2] * z)
+        for zi in range(0, nz, 64):  # chunk to bound temporaries
+            blk = az[zi:zi + 64, None, None] * ay[None, :, None] * ax[None, None, :]
+            f[zi:zi + 64] += amp * blk.real
+    return f
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                           "--format=csv,noheader,nounits", "-lms", "100"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+        return False
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# ------------------------------------------------------------ our arm
+def bytes_model(grid, esize_real):
+    """3-pass model per direction: X pass R + C, Y pass 2C, Z pass 2C."""
+    nx, ny, nz = grid
+    r = nx * ny * nz * esize_real
+    c = (nx // 2 + 1) * ny * nz * 2 * esize_real
+    return {"x": r + c, "y": 2 * c, "z": 2 * c, "dir": r + 5 * c, "rt": 2 * (r + 5 * c), "R": r, "C": c}
+
+
+def time_device(torch, plan, x, b, r, ops, steps, warmup, stream):
+    """Device-resident round trips, CUDA events on the plan's stream."""
+    for _ in range(warmup):
+        plan.ftran_r2c(x, b, op=ops[0], stream=stream)
+        plan.btran_c2r(b, r, op=ops[1], stream=stream)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    plan.reset_timers()
+    launches0 = plan.launches
+    ev0.record(stream)
+    for _ in range(steps):
+        plan.ftran_r2c(x, b, op=ops[0], stream=stream)
+        plan.btran_c2r(b, r, op=ops[1], stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    return ms, plan.launches - launches0
+
+
+def run_ours(args):
+    import torch
+    import p3dfft_gb300 as pg
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist = dist_mod
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    cfg = CONFIGS[args.config]
+    grid = cfg["grid"]
+    nx, ny, nz = grid
+    ops = cfg["ops"]
+    npts = nx * ny * nz
+    stream = torch.cuda.Stream(device=dev)
+    peak, peak_kind = load_peaks()
+
+    # ---- FP64 (headline)
+    plan = pg.Plan(nx, ny, nz, precision=pg.F64, timers=True)
+    kind = "uniform" if args.config == "small" else "modes"
+    x = make_input(torch, grid, 1234 + rank, dev, kind)
+    b = torch.empty(plan.complex_shape, dtype=torch.complex128, device=dev)
+    r = torch.empty_like(x)
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        ms64, launches = time_device(torch, plan, x, b, r, ops, args.steps, args.warmup, stream)
+    if dist:
+        t = torch.tensor([ms64], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms64 = float(t.item())
+    timers = plan.timers()
+    # per-pass kernel times over the timed steps (plan timers: slots 5,7,8,9,10,12)
+    bm = bytes_model(grid, 8)
+    scale = 1.0 / nx / ny / nz
+    # accuracy on the full grid: round trip, and F32 vs F64 forward below
+    plan.ftran_r2c(x, b, op=ops[0], stream=stream)
+    fwd64 = b.clone()
+    b.mul_(scale)
+    plan.btran_c2r(b, r, op=ops[1], stream=stream)
+    torch.cuda.synchronize()
+    rt_err = float((r - x).abs().max() / x.abs().max())
+    pass_ms = {
+        "x_r2c": timers[4] * 1e3 / args.steps, "y_fwd": timers[6] * 1e3 / args.steps,
+        "z_fwd": timers[7] * 1e3 / args.steps, "z_bwd": timers[8] * 1e3 / args.steps,
+        "y_bwd": timers[9] * 1e3 / args.steps, "x_c2r": timers[11] * 1e3 / args.steps,
+    }
+    pass_bytes = {"x_r2c": bm["x"], "y_fwd": bm["y"], "z_fwd": bm["z"], "z_bwd": bm["z"], "y_bwd": bm["y"],
+                  "x_c2r": bm["x"]}
+    dom = max(pass_ms, key=lambda k: pass_ms[k])
+    achieved = pass_bytes[dom] / (pass_ms[dom] * 1e-3) / 1e9 if pass_ms[dom] > 0 else None
+    del r
+    plan.close()
+
+    # ---- FP32 form on the same grid
+    plan32 = pg.Plan(nx, ny, nz, precision=pg.F32)
+    x32 = x.float()
+    b32 = torch.empty(plan32.complex_shape, dtype=torch.complex64, device=dev)
+    r32 = torch.empty_like(x32)
+    ms32, _ = time_device(torch, plan32, x32, b32, r32, ops, args.steps, args.warmup, stream)
+    plan32.ftran_r2c(x32, b32, op=ops[0], stream=stream)
+    torch.cuda.synchronize()
+    diff = (b32.to(torch.complex128) - fwd64)
+    err32 = float(torch.linalg.vector_norm(diff) / torch.linalg.vector_norm(fwd64))
+    del b32, r32, x32, diff, fwd64
+    plan32.close()
+    if dist:
+        t = torch.tensor([ms32], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms32 = float(t.item())
+
+    # ---- end to end through the drop-in C-ABI with pinned host buffers
+    e2e = None
+    if not args.skip_e2e:
+        e2e = run_e2e(torch, pg, grid, ops, x, max(1, args.steps // 2), dev)
+    del x, b
+    torch.cuda.empty_cache()
+
+    value = world * npts / (ms64 * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms64, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": cfg["workload"], "grid": list(grid), "ops": list(ops), "precision": "f64",
+                   "arithmetic": "binary64 I/O, double-float (2 x binary32) butterflies",
+                   "l2": "inputs larger than L2 (8 GB per field), no flush needed",
+                   "parallelism": f"replicas x{world}"},
+        "error": {"f64_roundtrip_normalised_linf": rt_err,
+                  "f32_forward_rel_l2_vs_f64": err32},
+        "f32": {"value": round(world * npts / (ms32 * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_step": round(ms32, 4),
+                "rel_l2_vs_f64": err32, "speedup_vs_f64": round(ms64 / ms32, 3)},
+        "passes_ms": {k: round(v, 4) for k, v in pass_ms.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1) if achieved else None,
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
+                     "peak_kind": peak_kind, "traffic": None,
+                     "step_bytes_model": bm["rt"],
+                     "step_frac": round(bm["rt"] / (ms64 * 1e-3) / 1e9 / peak, 4)},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0 and not args.skip_cpu:
+        line["cpu_baseline"] = cpu_baseline(args)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_e2e(torch, pg, grid, ops, x_dev, steps, dev):
+    """Same metric through the reference-facing C-ABI (p3dfft_ftran_r2c /
+    p3dfft_btran_c2r) with pinned host buffers: H2D and D2H inside the timing."""
+    nx, ny, nz = grid
+    host_in = torch.empty((nz, ny, nx), dtype=torch.float64, pin_memory=True)
+    host_in.copy_(x_dev.cpu())
+    host_c = torch.empty((nz, ny, nx // 2 + 1), dtype=torch.complex128, pin_memory=True)
+    host_out = torch.empty((nz, ny, nx), dtype=torch.float64, pin_memory=True)
+    pg.p3dfft_setup((1, 1), nx, ny, nz, 0, nx, ny, nz, True)
+    try:
+        pg.p3dfft_ftran_r2c(host_in, host_c, ops[0])
+        pg.p3dfft_btran_c2r(host_c, host_out, ops[1])
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            pg.p3dfft_ftran_r2c(host_in, host_c, ops[0])
+            pg.p3dfft_btran_c2r(host_c, host_out, ops[1])
+        dt = (time.perf_counter() - t0) / steps
+    finally:
+        pg.p3dfft_clean()
+    r_bytes = nx * ny * nz * 8
+    c_bytes = (nx // 2 + 1) * ny * nz * 16
+    return {"value": round(nx * ny * nz / dt / 1e9, 3), "unit": UNIT, "ms_per_step": round(dt * 1e3, 3),
+            "h2d_bytes_per_step": r_bytes + c_bytes, "d2h_bytes_per_step": c_bytes + r_bytes,
+            "path": "libp3dfft.so p3dfft_ftran_r2c + p3dfft_btran_c2r, pinned host arrays"}
+
+
+# ------------------------------------------------------------ CPU arms
+def cpu_sample_grid(args):
+    return (256, 256, 256) if args.config in ("large", "noncubic") else CONFIGS[args.config]["grid"]
+
+
+def cpu_round_trips(grid, ops, seconds, max_steps=None):
+    from oracle import p3dfft_oracle as orc
+    orc.WORKERS = os.cpu_count() or 1
+    nx, ny, nz = grid
+    a = np.random.default_rng(7).uniform(-1, 1, size=(nz, ny, nx))
+    p = orc.OraclePlan(nx, ny, nz)
+    b = p.ftran_r2c(a, ops[0])  # warm-up (plans, page faults)
+    p.btran_c2r(b, ops[1])
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        b = p.ftran_r2c(a, ops[0])
+        p.btran_c2r(b, ops[1])
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or (max_steps and n >= max_steps):
+            break
+    return n, el, orc.WORKERS
+
+
+def cpu_baseline(args):
+    grid = cpu_sample_grid(args)
+    ops = CONFIGS[args.config]["ops"]
+    n, el, cores = cpu_round_trips(grid, ops, seconds=args.cpu_seconds)
+    pts = grid[0] * grid[1] * grid[2]
+    return {"value": round(pts * n / el / 1e9, 4), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} FP64 r2c+c2r round trips of {grid[0]}x{grid[1]}x{grid[2]} (oracle: numpy/scipy "
+                      f"pocketfft restatement of the reference path, scipy.fft workers={cores}); the FFTW+MPI "
+                      f"reference does not build here (no Fortran/MPI/FFTW)"}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    grid = cpu_sample_grid(args)
+    ops = CONFIGS[args.config]["ops"]
+    for _ in range(args.warmup):
+        cpu_round_trips(grid, ops, seconds=0, max_steps=1)
+    n, el, cores = cpu_round_trips(grid, ops, seconds=0, max_steps=args.steps)
+    pts = grid[0] * grid[1] * grid[2]
+    value = pts * n / el / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / n * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": CONFIGS[args.config]["workload"], "sample_grid": list(grid),
+                   "ops": list(ops)},
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"each step one FP64 round trip of {grid[0]}x{grid[1]}x{grid[2]} through the "
+                                   f"oracle port (scipy.fft, {cores} threads); the FFTW+MPI reference does not "
+                                   f"build here"},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="large", choices=sorted(CONFIGS))
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

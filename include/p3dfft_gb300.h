@@ -1,0 +1,95 @@
+/*
+ * p3dfft_gb300.h -- explicit device API of the GB300 P3DFFT transform library.
+ *
+ * Plain C ABI (no CUDA or torch types in the signatures).  Arrays passed to
+ * the transform calls are DEVICE pointers; the stream argument is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream).  Every
+ * call returns 0 on success or a negative P3G_E* code; p3g_last_error()
+ * returns the message of the last failure on the calling thread.
+ *
+ * The drop-in reference interface (p3dfft_setup, p3dfft_ftran_r2c, ...) is
+ * declared in p3dfft.h and implemented on top of this API by libp3dfft.so.
+ *
+ * Array layouts follow the reference (column-major, X fastest):
+ *   real field     (nx, ny, nz)
+ *   complex field  (nxc/2+1, nyc, nzc), interleaved (re, im), or
+ *                  (nzc, nyc, nxc/2+1) with P3G_LAYOUT_STRIDE1.
+ */
+#ifndef P3DFFT_GB300_H
+#define P3DFFT_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct p3g_plan_s* p3g_plan;
+
+enum {
+  P3G_OK = 0,
+  P3G_E_ARG = -1,       /* invalid argument (sizes, op letters, geometry) */
+  P3G_E_CUDA = -2,      /* a CUDA runtime call failed */
+  P3G_E_NOMEM = -3,     /* device allocation failed */
+  P3G_E_UNSUPPORTED = -4, /* a size or option outside this build's limits */
+  P3G_E_STATE = -5      /* call out of order (no plan / plan already set up) */
+};
+
+enum { P3G_F64 = 0, P3G_F32 = 1 };               /* precision of data and arithmetic path */
+enum { P3G_LAYOUT_XYZ = 0, P3G_LAYOUT_STRIDE1 = 1 }; /* complex output layout */
+enum { P3G_FLAG_TIMERS = 1 };                     /* record per-pass CUDA-event timers */
+
+/* Create a plan for an nx*ny*nz real grid keeping nxc*nyc*nzc modes
+ * (pruned transform when smaller than the grid).  Replaces the planning and
+ * buffer set-up of p3dfft_setup (reference build/setup.F90:107-605,
+ * build/init_plan.F90:29-489): twiddle tables are generated once in FP64 on
+ * the host and kept on the device with the stage plans.  The workspace is
+ * allocated on the first transform call and grown for larger nv. */
+int p3g_plan_create(p3g_plan* plan, int nx, int ny, int nz, int nxc, int nyc, int nzc, int precision, int layout,
+                    int flags);
+int p3g_plan_destroy(p3g_plan plan);
+
+/* Bounds of the local arrays, as p3dfft_get_dims (reference
+ * build/module.F90:225-273): conf 1 real space, 2 wavenumber space,
+ * 3 padded in-place size (memsize).  1-based start/end, size. */
+int p3g_get_dims(p3g_plan plan, int conf, int start[3], int end[3], int size[3]);
+
+/* Forward real-to-complex transform of nv fields (reference
+ * build/ftran.F90:489-780 and :104-317).  op is 3 letters; op[2] selects the
+ * Z transform: 't'/'f' FFT, 'c' DCT-I (REDFT00), 's' DST-I (RODFT00), 'n'/'0'
+ * none.  dim_in/dim_out are the element spacings between fields (reals /
+ * complexes); <= 0 selects the dense size.  in and out may alias. */
+int p3g_ftran_r2c(p3g_plan plan, const void* in, void* out, const char* op, int nv, long long dim_in,
+                  long long dim_out, void* stream);
+
+/* Backward complex-to-real transform (reference build/btran.F90:396-679 and
+ * :104-304); op[0] selects the Z transform.  Unnormalised.  The input is not
+ * modified. */
+int p3g_btran_c2r(p3g_plan plan, const void* in, void* out, const char* op, int nv, long long dim_in,
+                  long long dim_out, void* stream);
+
+/* p3dfft_cheby (reference build/ftran.F90:321-464): 'ffc' transform, scaling
+ * by 1/(nx*ny*(nzc-1)) and the Chebyshev-derivative recurrence along z with
+ * factor 4/lz. */
+int p3g_cheby(p3g_plan plan, const void* in, void* out, double lz, int nv, long long dim_in, long long dim_out,
+              void* stream);
+
+/* The reference's 12 accumulating stage timers (build/module.F90:106,709-744),
+ * in seconds: slot 5 X r2c, 7 Y forward, 8 Z forward, 9 Z backward,
+ * 10 Y backward, 12 X c2r (1-based; communication slots stay 0).  Needs
+ * P3G_FLAG_TIMERS; get synchronises with the recorded events. */
+int p3g_get_timers(p3g_plan plan, double timers[12]);
+int p3g_set_timers(p3g_plan plan);
+
+/* Device bytes held by the plan (tables + workspace). */
+long long p3g_plan_device_bytes(p3g_plan plan);
+/* Kernel launches issued by this plan since creation. */
+long long p3g_plan_launches(p3g_plan plan);
+
+const char* p3g_last_error(void);
+int p3g_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* P3DFFT_GB300_H */

@@ -1,0 +1,282 @@
+"""GB300-native P3DFFT 3D transform path.
+
+Two interfaces over the same sm_103a kernels:
+
+* ``Plan`` -- the explicit device API (include/p3dfft_gb300.h): device
+  tensors, CUDA streams, F64 or F32 path, many fields per call.
+* ``p3dfft_setup`` / ``p3dfft_get_dims`` / ``p3dfft_ftran_r2c`` /
+  ``p3dfft_btran_c2r`` / ``p3dfft_*_many`` / ``p3dfft_cheby`` /
+  ``p3dfft_clean`` / ``get_timers`` / ``set_timers`` -- the reference's module
+  interface (build/module.F90:178-186, include/p3dfft.h) through the drop-in
+  library, with the same argument meaning: arrays are column-major
+  (X fastest), i.e. numpy C-order arrays shaped (nz, ny, nx) for real fields
+  and (nzc, nyc, nxc/2+1) for complex ones; host numpy arrays or CUDA
+  tensors are accepted.  Errors raise ``P3DFFTError`` where the reference
+  prints and aborts.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+__all__ = [
+    "P3DFFTError", "Plan", "F64", "F32", "p3dfft_setup", "p3dfft_get_dims", "p3dfft_get_mpi_info",
+    "p3dfft_ftran_r2c", "p3dfft_btran_c2r", "p3dfft_ftran_r2c_many", "p3dfft_btran_c2r_many",
+    "p3dfft_cheby", "p3dfft_cheby_many", "p3dfft_clean", "get_timers", "set_timers",
+]
+
+F64 = 0
+F32 = 1
+LAYOUT_XYZ = 0
+LAYOUT_STRIDE1 = 1
+FLAG_TIMERS = 1
+
+
+class P3DFFTError(RuntimeError):
+    pass
+
+
+def _core():
+    return _lib.load().core
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise P3DFFTError(f"p3g error {rc}: {_core().p3g_last_error().decode()}")
+
+
+def _ptr(t) -> int:
+    """Data pointer of a torch tensor (device) or numpy array (host)."""
+    if hasattr(t, "data_ptr"):
+        return t.data_ptr()
+    return t.ctypes.data
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                return torch.cuda.current_stream().cuda_stream
+        except ImportError:
+            pass
+        return None
+    return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+
+class Plan:
+    """Device plan for an nx*ny*nz grid (optionally pruned to nxc*nyc*nzc).
+
+    ``precision`` is F64 (binary64 data, double-float arithmetic) or F32.
+    Arrays are CUDA tensors in the reference's layouts: real (nz, ny, nx),
+    complex (nzc, nyc, nxc//2+1) complex128/complex64 (or float views).
+    """
+
+    def __init__(self, nx, ny, nz, nxc=None, nyc=None, nzc=None, precision=F64, layout=LAYOUT_XYZ, timers=False):
+        self._h = ctypes.c_void_p()
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.nxc = nxc or nx
+        self.nyc = nyc or ny
+        self.nzc = nzc or nz
+        self.precision = precision
+        self.layout = layout
+        _check(_core().p3g_plan_create(ctypes.byref(self._h), nx, ny, nz, self.nxc, self.nyc, self.nzc,
+                                       precision, layout, FLAG_TIMERS if timers else 0))
+
+    @property
+    def real_shape(self):
+        return (self.nz, self.ny, self.nx)
+
+    @property
+    def complex_shape(self):
+        if self.layout == LAYOUT_STRIDE1:
+            return (self.nxc // 2 + 1, self.nyc, self.nzc)
+        return (self.nzc, self.nyc, self.nxc // 2 + 1)
+
+    def get_dims(self, conf: int):
+        s, e, z = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
+        _check(_core().p3g_get_dims(self._h, conf, s, e, z))
+        return tuple(s), tuple(e), tuple(z)
+
+    def _dtypes(self):
+        import torch
+        return (torch.float64, torch.complex128) if self.precision == F64 else (torch.float32, torch.complex64)
+
+    def ftran_r2c(self, x, out=None, op="fft", nv=1, dim_in=0, dim_out=0, stream=None):
+        if out is None:
+            import torch
+            shape = ((nv,) if nv > 1 else ()) + self.complex_shape
+            out = torch.empty(shape, dtype=self._dtypes()[1], device=x.device)
+        _check(_core().p3g_ftran_r2c(self._h, _ptr(x), _ptr(out), op.encode(), nv, dim_in, dim_out,
+                                     _stream_ptr(stream)))
+        return out
+
+    def btran_c2r(self, c, out=None, op="tff", nv=1, dim_in=0, dim_out=0, stream=None):
+        if out is None:
+            import torch
+            shape = ((nv,) if nv > 1 else ()) + self.real_shape
+            out = torch.empty(shape, dtype=self._dtypes()[0], device=c.device)
+        _check(_core().p3g_btran_c2r(self._h, _ptr(c), _ptr(out), op.encode(), nv, dim_in, dim_out,
+                                     _stream_ptr(stream)))
+        return out
+
+    def cheby(self, x, lz, out=None, nv=1, dim_in=0, dim_out=0, stream=None):
+        if out is None:
+            import torch
+            shape = ((nv,) if nv > 1 else ()) + self.complex_shape
+            out = torch.empty(shape, dtype=self._dtypes()[1], device=x.device)
+        _check(_core().p3g_cheby(self._h, _ptr(x), _ptr(out), float(lz), nv, dim_in, dim_out, _stream_ptr(stream)))
+        return out
+
+    def timers(self):
+        t = (ctypes.c_double * 12)()
+        _check(_core().p3g_get_timers(self._h, t))
+        return list(t)
+
+    def reset_timers(self):
+        _check(_core().p3g_set_timers(self._h))
+
+    @property
+    def device_bytes(self) -> int:
+        return _core().p3g_plan_device_bytes(self._h)
+
+    @property
+    def launches(self) -> int:
+        return _core().p3g_plan_launches(self._h)
+
+    def close(self):
+        if self._h:
+            _core().p3g_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ----------------------------------------------------------------------------
+# reference module interface through the drop-in library
+# ----------------------------------------------------------------------------
+_single = False
+
+
+def _legacy():
+    libs = _lib.load()
+    return libs.legacy_single if _single else libs.legacy
+
+
+def _ci(v) -> ctypes.c_int:
+    return ctypes.c_int(int(v))
+
+
+def _legacy_check():
+    lib = _legacy()
+    st = lib.p3dfft_gb_status()
+    if st != 0:
+        raise P3DFFTError(lib.p3dfft_gb_last_error().decode())
+
+
+def p3dfft_setup(dims, nx, ny, nz, comm=0, nxc=None, nyc=None, nzc=None, overwrite=True, single=False):
+    """setup.F90:107: returns memsize (the padded in-place size)."""
+    global _single
+    _single = bool(single)
+    d = (ctypes.c_int * 2)(*dims)
+    mem = (ctypes.c_int * 3)()
+    _legacy().p3dfft_setup(d, ctypes.byref(_ci(nx)), ctypes.byref(_ci(ny)), ctypes.byref(_ci(nz)),
+                           ctypes.byref(_ci(comm)), ctypes.byref(_ci(nxc or nx)), ctypes.byref(_ci(nyc or ny)),
+                           ctypes.byref(_ci(nzc or nz)), ctypes.byref(_ci(1 if overwrite else 0)), mem)
+    _legacy_check()
+    return tuple(mem)
+
+
+def p3dfft_get_dims(conf: int):
+    """module.F90:225: (start, end, size), 1-based, Fortran dimension order."""
+    s, e, z = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
+    _legacy().p3dfft_get_dims(s, e, z, ctypes.byref(_ci(conf)))
+    _legacy_check()
+    return tuple(s), tuple(e), tuple(z)
+
+
+def p3dfft_get_mpi_info():
+    t, n, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _legacy().p3dfft_get_mpi_info(ctypes.byref(t), ctypes.byref(n), ctypes.byref(c))
+    _legacy_check()
+    return t.value, n.value, c.value
+
+
+def _real_dtype():
+    return np.float32 if _single else np.float64
+
+
+def _check_host(a, complex_=False):
+    if hasattr(a, "data_ptr"):
+        return
+    want = (np.complex64 if _single else np.complex128) if complex_ else _real_dtype()
+    if a.dtype != want or not a.flags.c_contiguous:
+        raise P3DFFTError(f"array must be C-contiguous {np.dtype(want).name}")
+
+
+def p3dfft_ftran_r2c(XgYZ, XYZg, op="fft"):
+    _check_host(XgYZ)
+    _check_host(XYZg, True)
+    _legacy().p3dfft_ftran_r2c(_ptr(XgYZ), _ptr(XYZg), op.encode())
+    _legacy_check()
+    return XYZg
+
+
+def p3dfft_btran_c2r(XYZg, XgYZ, op="tff"):
+    _check_host(XYZg, True)
+    _check_host(XgYZ)
+    _legacy().p3dfft_btran_c2r(_ptr(XYZg), _ptr(XgYZ), op.encode())
+    _legacy_check()
+    return XgYZ
+
+
+def p3dfft_ftran_r2c_many(XgYZ, dim_in, XYZg, dim_out, nv, op="fft"):
+    _legacy().p3dfft_ftran_r2c_many(_ptr(XgYZ), ctypes.byref(_ci(dim_in)), _ptr(XYZg), ctypes.byref(_ci(dim_out)),
+                                    ctypes.byref(_ci(nv)), op.encode())
+    _legacy_check()
+    return XYZg
+
+
+def p3dfft_btran_c2r_many(XYZg, dim_in, XgYZ, dim_out, nv, op="tff"):
+    _legacy().p3dfft_btran_c2r_many(_ptr(XYZg), ctypes.byref(_ci(dim_in)), _ptr(XgYZ), ctypes.byref(_ci(dim_out)),
+                                    ctypes.byref(_ci(nv)), op.encode())
+    _legacy_check()
+    return XgYZ
+
+
+def _lz_arg(lz):
+    return ctypes.byref(ctypes.c_float(lz) if _single else ctypes.c_double(lz))
+
+
+def p3dfft_cheby(XgYZ, XYZg, Lz):
+    _legacy().p3dfft_cheby(_ptr(XgYZ), _ptr(XYZg), _lz_arg(Lz))
+    _legacy_check()
+    return XYZg
+
+
+def p3dfft_cheby_many(XgYZ, dim_in, XYZg, dim_out, nv, Lz):
+    _legacy().p3dfft_cheby_many(_ptr(XgYZ), ctypes.byref(_ci(dim_in)), _ptr(XYZg), ctypes.byref(_ci(dim_out)),
+                                ctypes.byref(_ci(nv)), _lz_arg(Lz))
+    _legacy_check()
+    return XYZg
+
+
+def p3dfft_clean():
+    _legacy().p3dfft_clean()
+
+
+def get_timers():
+    t = (ctypes.c_double * 12)()
+    _legacy().get_timers(t)
+    return list(t)
+
+
+def set_timers():
+    _legacy().set_timers()

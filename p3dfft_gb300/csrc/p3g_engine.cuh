@@ -1,0 +1,184 @@
+// CTA-level mixed-radix Stockham FFT over a tile of M lines in shared memory.
+//
+// A tile holds M independent lines of N complex points.  Element (line, j)
+// lives at sm[line * LS + j * JS]; the X passes use line-major tiles
+// (LS = N, JS = 1), the strided Y/Z passes point-major tiles (LS = 1, JS = M)
+// so that consecutive threads touch consecutive x columns.
+//
+// Each stage of radix R runs the Stockham autosort step (Govindaraju et al.,
+// SC'08): butterfly j of a line reads points j + q N/R (q < R), multiplies them
+// by w_{Ns R}^{q (j mod Ns)}, runs a register DFT of size R and writes points
+// (j / Ns) Ns R + (j mod Ns) + q Ns.  All reads of a stage finish before any
+// write (one barrier), so a stage works in place: every thread keeps all of its
+// butterflies of the stage in registers (at most ceil(E/R), E = elements per
+// thread, which the launch guarantees by using ceil(M N / E) threads).
+//
+// Radices 2, 3, 4, 5, 8, 16 are register codelets.  Any other prime p runs a
+// generic direct-DFT stage through a second shared-memory buffer (O(N p) work).
+#pragma once
+
+#include "p3g_codelets.cuh"
+
+namespace p3g {
+
+constexpr int kMaxStages = 20;
+constexpr int kElemsPerThread = 16;  // E
+
+struct StagePlan {
+  int n;                   // transform length (1 allowed: no stages)
+  int nstages;
+  int has_generic;         // a stage with a radix outside {2,3,4,5,8,16}
+  int cnt[6];              // number of stages of radix 16, 8, 4, 2, 3, 5 (stored in this order, then generic)
+  int radix[kMaxStages];
+  int ns[kMaxStages];      // sub-transform length before the stage
+  int tw_off[kMaxStages];  // float4 offset of this stage's twiddles [k < ns][q-1 < radix-1]
+  int root_off[kMaxStages];  // generic stages: float4 offset of the radix-th roots of unity
+};
+
+// Twiddles are stored for the forward sign (exp(-2 pi i ...)) as double-float
+// complex float4 (re.hi, im.hi, re.lo, im.lo); the backward direction
+// multiplies by the conjugate.
+P3G_D cdf load_tw(const float4* __restrict__ tw, int idx) {
+  const float4 v = __ldg(tw + idx);
+  return cdf{df{v.x, v.z}, df{v.y, v.w}};
+}
+
+template <class P>
+struct Tile {
+  typename P::W* sm;       // M lines x N points
+  typename P::W* scratch;  // same size, generic stages only
+  int M, log2m, LS, JS;
+  P3G_D int addr(int line, int j) const { return line * LS + j * JS; }
+  // butterfly b -> (line, j) over M lines x (N / R) butterflies per line
+  P3G_D void decode(int b, int per_line, int& line, int& j) const {
+    if (LS == 1) {  // point-major: line fastest
+      line = b & (M - 1);
+      j = b >> log2m;
+    } else {
+      line = b / per_line;
+      j = b - line * per_line;
+    }
+  }
+};
+
+// Hardware barrier with a compile-time id.  Each radix uses its own id: with a
+// plain __syncthreads() the compiler merges the identical barriers of all
+// switch cases in cta_fft, which keeps every case's registers live at once.
+template <int ID>
+P3G_D void cta_barrier() {
+  asm volatile("bar.sync %0;" ::"n"(ID) : "memory");
+}
+
+template <class P, int DIR, int R>
+__device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const float4* __restrict__ tw) {
+  using C = typename P::C;
+  constexpr int MAXB = (kElemsPerThread + R - 1) / R;
+  const int per_line = N / R;
+  const int nb = t.M * per_line;
+  const int T = blockDim.x;
+  C v[MAXB][R];
+  int oline[MAXB], obase[MAXB];
+#pragma unroll
+  for (int i = 0; i < MAXB; ++i) {
+    const int b = threadIdx.x + i * T;
+    oline[i] = -1;
+    if (b < nb) {
+      int line, j;
+      t.decode(b, per_line, line, j);
+#pragma unroll
+      for (int q = 0; q < R; ++q) v[i][q] = P::from_w(t.sm[t.addr(line, j + q * per_line)]);
+      const int k = j % ns;
+      if (ns > 1) {
+        const float4* twp = tw + k * (R - 1) - 1;
+#pragma unroll
+        for (int q = 1; q < R; ++q) v[i][q] = cmul<(DIR > 0)>(v[i][q], load_tw(twp, q));
+      }
+      dft<R, DIR>(v[i]);
+      oline[i] = line;
+      obase[i] = (j - k) * R + k;
+    }
+  }
+  cta_barrier<(R == 16 ? 1 : R)>();
+#pragma unroll
+  for (int i = 0; i < MAXB; ++i) {
+    if (oline[i] >= 0) {
+#pragma unroll
+      for (int q = 0; q < R; ++q) t.sm[t.addr(oline[i], obase[i] + q * ns)] = P::to_w(v[i][q]);
+    }
+  }
+  cta_barrier<(R == 16 ? 1 : R)>();
+}
+
+// Generic prime radix p: twiddle the inputs into scratch, then each output is
+// a direct p-term sum with the p-th roots of unity.
+template <class P, int DIR>
+__device__ __noinline__ void stage_generic(const Tile<P>& t, int N, int p, int ns, const float4* __restrict__ tw,
+                                           const float4* __restrict__ roots) {
+  using C = typename P::C;
+  const int per_line = N / p;
+  const int total = t.M * N;
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    int line, idx;
+    t.decode(e, N, line, idx);
+    const int q = idx / per_line;
+    const int j = idx - q * per_line;
+    C v = P::from_w(t.sm[t.addr(line, idx)]);
+    const int k = j % ns;
+    if (q > 0 && ns > 1) v = cmul<(DIR > 0)>(v, load_tw(tw, k * (p - 1) + q - 1));
+    t.scratch[t.addr(line, idx)] = P::to_w(v);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    int line, idx;
+    t.decode(e, N, line, idx);
+    const int kout = idx / per_line;  // output index within the butterfly
+    const int j = idx - kout * per_line;
+    C acc = P::from_w(t.scratch[t.addr(line, j)]);
+    int m = 0;
+    for (int q = 1; q < p; ++q) {
+      m += kout;
+      if (m >= p) m -= p;
+      const C x = P::from_w(t.scratch[t.addr(line, j + q * per_line)]);
+      acc = acc + (m == 0 ? x : cmul<(DIR > 0)>(x, load_tw(roots, m)));
+    }
+    const int k = j % ns;
+    t.sm[t.addr(line, (j - k) * p + k + kout * ns)] = P::to_w(acc);
+  }
+  __syncthreads();
+}
+
+template <class P, int DIR, int R>
+__device__ __forceinline__ int run_family(const Tile<P>& t, const StagePlan* __restrict__ sp,
+                                          const float4* __restrict__ tw, int N, int s, int cnt) {
+#pragma unroll 1
+  for (int c = 0; c < cnt; ++c, ++s) stage_reg<P, DIR, R>(t, N, __ldg(&sp->ns[s]), tw + __ldg(&sp->tw_off[s]));
+  return s;
+}
+
+// Runs all stages of the plan on the tile (sm must be filled and
+// synchronised).  The plan orders its stages by radix family (16, 8, 4, 2, 3,
+// 5, then generic primes) and each family runs in its own loop: a single loop
+// with a switch over the radix makes the register allocator keep the live
+// ranges of every codelet at once and spill.  The stage plan lives in device
+// memory, read with uniform cached loads.  Radix 16 is compiled only for the
+// F32 path (the F64 codelet needs ~200 registers; radix 8 has the same
+// double-float operation count per point for the sizes used here).
+template <class P, int DIR>
+__device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __restrict__ sp,
+                                        const float4* __restrict__ tw) {
+  const int N = __ldg(&sp->n);
+  int s = 0;
+  if constexpr (!P::kF64) s = run_family<P, DIR, 16>(t, sp, tw, N, s, __ldg(&sp->cnt[0]));
+  s = run_family<P, DIR, 8>(t, sp, tw, N, s, __ldg(&sp->cnt[1]));
+  s = run_family<P, DIR, 4>(t, sp, tw, N, s, __ldg(&sp->cnt[2]));
+  s = run_family<P, DIR, 2>(t, sp, tw, N, s, __ldg(&sp->cnt[3]));
+  s = run_family<P, DIR, 3>(t, sp, tw, N, s, __ldg(&sp->cnt[4]));
+  s = run_family<P, DIR, 5>(t, sp, tw, N, s, __ldg(&sp->cnt[5]));
+  const int nst = __ldg(&sp->nstages);
+#pragma unroll 1
+  for (; s < nst; ++s)
+    stage_generic<P, DIR>(t, N, __ldg(&sp->radix[s]), __ldg(&sp->ns[s]), tw + __ldg(&sp->tw_off[s]),
+                          tw + __ldg(&sp->root_off[s]));
+}
+
+}  // namespace p3g

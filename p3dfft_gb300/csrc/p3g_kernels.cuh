@@ -1,0 +1,70 @@
+// Kernel parameter blocks and launch entry points shared by the host plan.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "p3g_engine.cuh"
+
+namespace p3g {
+
+// X passes: lines along x (contiguous).  Two real lines travel as the real and
+// imaginary parts of one complex line of length nx.
+struct XParams {
+  const void* in;
+  void* out;
+  long long in_field, out_field;  // element stride between fields (nv)
+  long long in_line, out_line;    // element stride between lines
+  int nlines;                     // lines per field (ny * nz)
+  int nx;                         // real line length = complex FFT length
+  int nkeep;                      // complex modes per line stored (r2c) / read (c2r)
+  int M, log2m;                   // line pairs per tile
+  int tiles;                      // tiles per field
+};
+
+// Strided Y/Z passes: a tile is M consecutive x columns of one (o1, o2) row
+// set, transformed along the axis.  Element (x, j) of the input sits at
+// in + x + j*in_axis + o1*in_o1 + o2*in_o2 (elements of 16 B on the F64 path,
+// 8 B on the F32 path, for both the workspace and the user format).
+struct SParams {
+  const void* in;
+  void* out;
+  int in_user, out_user;  // 1: user complex format, 0: workspace format
+  long long in_axis, in_o1, in_o2;
+  long long out_axis, out_o1, out_o2;
+  int X;            // valid x columns
+  int M, log2m;     // tile width (power of two)
+  int xtiles, O1;   // tiles per row, number of o1 rows (o2 = fields from the grid)
+  int L;            // logical transform length along the axis
+  int N;            // FFT length (L, 2(L-1) or 2(L+1))
+  int Lout;         // rows stored
+  int pre;          // 0: rows as is, 1: DCT-I even extension (N = 2(L-1)), 2: DST-I odd extension (N = 2(L+1))
+  int post;         // 0: result row k = buffer[k], 1: DST-I, result k = i*buffer[k+1]
+  int lmap_a0, lmap_a1, lmap_d;  // load: row j <- input row j - d if j >= a1, j if j < a0, else 0
+  int smap_s0, smap_d;           // store: output row jo <- result row jo (jo < s0) or jo + d
+};
+
+struct ChebyParams {
+  void* data;          // user complex output of the 'ffc' transform
+  long long field;     // element stride between fields
+  long long pstride;   // element stride between pencils
+  long long zstride;   // element stride along z
+  int npencil;         // nxhpc * nyc
+  int nzc;
+  float sc_hi, sc_lo;  // 1/(nx*ny*(nzc-1)) as double-float
+  float l_hi, l_lo;    // 4/Lz as double-float
+};
+
+// Launchers (one per path).  Return the cudaError_t of the launch.
+template <class P>
+cudaError_t launch_x_r2c(const XParams& p, const StagePlan* sp, const float4* tw, int threads, size_t smem,
+                         int nfields, cudaStream_t st);
+template <class P>
+cudaError_t launch_x_c2r(const XParams& p, const StagePlan* sp, const float4* tw, int threads, size_t smem,
+                         int nfields, cudaStream_t st);
+template <class P>
+cudaError_t launch_strided(const SParams& p, const StagePlan* sp, const float4* tw, bool forward_sign, int threads,
+                           size_t smem, int nfields, cudaStream_t st);
+template <class P>
+cudaError_t launch_cheby(const ChebyParams& p, int nfields, cudaStream_t st);
+
+}  // namespace p3g

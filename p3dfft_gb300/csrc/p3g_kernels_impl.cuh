@@ -1,0 +1,275 @@
+// Pass kernels, instantiated once per path by p3g_kernels_f64.cu / _f32.cu.
+#pragma once
+
+#include "p3g_kernels.cuh"
+
+namespace p3g {
+
+extern __shared__ __align__(16) unsigned char p3g_smem[];
+
+template <class P>
+struct PathLimits;
+template <>
+struct PathLimits<PathF64> {  // 2 CTAs of 256 threads per SM, 128 registers
+  static constexpr int kMaxThreads = 256;
+  static constexpr int kMinBlocks = 2;
+};
+template <>
+struct PathLimits<PathF32> {
+  static constexpr int kMaxThreads = 512;
+  static constexpr int kMinBlocks = 1;
+};
+
+// ---------------------------------------------------------------- X r2c
+// Real lines 2p and 2p+1 form z = x1 + i x2; Z = FFT(z);
+// X1[k] = (Z[k] + conj Z[N-k]) / 2, X2[k] = -i (Z[k] - conj Z[N-k]) / 2.
+template <class P>
+__global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
+    k_x_r2c(const XParams prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw) {
+  using W = typename P::W;
+  using C = typename P::C;
+  W* sm = reinterpret_cast<W*>(p3g_smem);
+  const int N = prm.nx;
+  const int M = prm.M;
+  const int field = blockIdx.y;
+  const int p0 = blockIdx.x * M;  // first pair of the tile
+  const auto* in = static_cast<const typename P::UR*>(prm.in) + field * prm.in_field;
+  W* out = static_cast<W*>(prm.out) + field * prm.out_field;
+
+  float* smf = reinterpret_cast<float*>(sm);
+  constexpr int kW = sizeof(W) / sizeof(float);  // floats per element: 4 (F64) or 2 (F32)
+  for (int e = threadIdx.x; e < 2 * M * N; e += blockDim.x) {
+    const int lt = e / N;
+    const int x = e - lt * N;
+    const int line = 2 * p0 + lt;
+    const int c = lt & 1;
+    float* f = smf + ((lt >> 1) * N + x) * kW;
+    if constexpr (P::kF64) {
+      const df v = line < prm.nlines ? P::from_ur(in[(long long)line * prm.in_line + x]) : df{0.f, 0.f};
+      f[c] = v.hi;
+      f[2 + c] = v.lo;
+    } else {
+      f[c] = line < prm.nlines ? in[(long long)line * prm.in_line + x] : 0.0f;
+    }
+  }
+  __syncthreads();
+  Tile<P> t{sm, sm + M * N, M, prm.log2m, N, 1};
+  cta_fft<P, -1>(t, sp, tw);
+  const int nk = prm.nkeep;
+  for (int e = threadIdx.x; e < M * nk; e += blockDim.x) {
+    const int pr = e / nk;
+    const int k = e - pr * nk;
+    const int line = 2 * (p0 + pr);
+    if (line >= prm.nlines) continue;
+    const C a = P::from_w(sm[pr * N + k]);
+    const C b = cconj(P::from_w(sm[pr * N + (k == 0 ? 0 : N - k)]));
+    out[(long long)line * prm.out_line + k] = P::to_w(cscale2(a + b, 0.5f));
+    if (line + 1 < prm.nlines) out[(long long)(line + 1) * prm.out_line + k] = P::to_w(cscale2(rot<-1>(a - b), 0.5f));
+  }
+}
+
+// ---------------------------------------------------------------- X c2r
+// Z[k] = X1[k] + i X2[k] (k <= N/2, imaginary parts of DC and Nyquist
+// dropped as FFTW's c2r does), Z[N-k] = conj X1[k] + i conj X2[k];
+// z = IFFT(Z) (unnormalised) gives x1 = Re z, x2 = Im z.
+template <class P>
+__global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
+    k_x_c2r(const XParams prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw) {
+  using W = typename P::W;
+  using C = typename P::C;
+  W* sm = reinterpret_cast<W*>(p3g_smem);
+  const int N = prm.nx;
+  const int M = prm.M;
+  const int field = blockIdx.y;
+  const int p0 = blockIdx.x * M;
+  const W* in = static_cast<const W*>(prm.in) + field * prm.in_field;
+  auto* out = static_cast<typename P::UR*>(prm.out) + field * prm.out_field;
+  const int nh = N / 2 + 1;
+  for (int e = threadIdx.x; e < M * nh; e += blockDim.x) {
+    const int pr = e / nh;
+    const int k = e - pr * nh;
+    const int line = 2 * (p0 + pr);
+    C x1 = P::zero(), x2 = P::zero();
+    if (k < prm.nkeep) {
+      if (line < prm.nlines) x1 = P::from_w(in[(long long)line * prm.in_line + k]);
+      if (line + 1 < prm.nlines) x2 = P::from_w(in[(long long)(line + 1) * prm.in_line + k]);
+    }
+    if (k == 0 || 2 * k == N) {
+      x1 = P::make(P::re(x1), P::re(P::zero()));
+      x2 = P::make(P::re(x2), P::re(P::zero()));
+    }
+    sm[pr * N + k] = P::to_w(x1 + rot<1>(x2));
+    if (k > 0 && 2 * k < N) sm[pr * N + N - k] = P::to_w(cconj(x1) + rot<1>(cconj(x2)));
+  }
+  __syncthreads();
+  Tile<P> t{sm, sm + M * N, M, prm.log2m, N, 1};
+  cta_fft<P, 1>(t, sp, tw);
+  const float* smf = reinterpret_cast<const float*>(sm);
+  constexpr int kW = sizeof(W) / sizeof(float);
+  for (int e = threadIdx.x; e < 2 * M * N; e += blockDim.x) {
+    const int lt = e / N;
+    const int n = e - lt * N;
+    const int line = 2 * p0 + lt;
+    if (line >= prm.nlines) continue;
+    const int c = lt & 1;
+    const float* f = smf + ((lt >> 1) * N + n) * kW;
+    if constexpr (P::kF64) {
+      out[(long long)line * prm.out_line + n] = P::to_ur(df{f[c], f[2 + c]});
+    } else {
+      out[(long long)line * prm.out_line + n] = f[c];
+    }
+  }
+}
+
+// ------------------------------------------------------------- strided Y/Z
+template <class P>
+P3G_D typename P::C load_elem(const void* base, int user, long long idx) {
+  if (user) return P::from_uc(static_cast<const typename P::UC*>(base)[idx]);
+  return P::from_w(static_cast<const typename P::W*>(base)[idx]);
+}
+template <class P>
+P3G_D void store_elem(void* base, int user, long long idx, typename P::C v) {
+  if (user) static_cast<typename P::UC*>(base)[idx] = P::to_uc(v);
+  else static_cast<typename P::W*>(base)[idx] = P::to_w(v);
+}
+
+template <class P, int DIR>
+__global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
+    k_strided(const SParams prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw) {
+  using W = typename P::W;
+  using C = typename P::C;
+  W* sm = reinterpret_cast<W*>(p3g_smem);
+  const int M = prm.M;
+  const int N = prm.N;
+  const int L = prm.L;
+  long long bid = blockIdx.x;
+  const int xt = (int)(bid % prm.xtiles);
+  bid /= prm.xtiles;
+  const int o1 = (int)(bid % prm.O1);
+  const int o2 = (int)(bid / prm.O1);
+  const int x0 = xt * M;
+  const long long ibase = (long long)o1 * prm.in_o1 + (long long)o2 * prm.in_o2 + x0;
+  const long long obase = (long long)o1 * prm.out_o1 + (long long)o2 * prm.out_o2 + x0;
+
+  if (prm.pre == 2 && threadIdx.x < M) {  // DST-I odd extension: zero rows 0 and L+1
+    sm[threadIdx.x] = P::to_w(P::zero());
+    sm[(L + 1) * M + threadIdx.x] = P::to_w(P::zero());
+  }
+  for (int e = threadIdx.x; e < M * L; e += blockDim.x) {
+    const int m = e & (M - 1);
+    const int j = e >> prm.log2m;
+    const int src = j >= prm.lmap_a1 ? j - prm.lmap_d : (j < prm.lmap_a0 ? j : -1);
+    C v = P::zero();
+    if (x0 + m < prm.X && src >= 0) v = load_elem<P>(prm.in, prm.in_user, ibase + m + src * prm.in_axis);
+    if (prm.pre == 0) {
+      sm[j * M + m] = P::to_w(v);
+    } else if (prm.pre == 1) {
+      sm[j * M + m] = P::to_w(v);
+      if (j >= 1 && j <= L - 2) sm[(2 * (L - 1) - j) * M + m] = P::to_w(v);
+    } else {
+      sm[(j + 1) * M + m] = P::to_w(v);
+      sm[(2 * (L + 1) - (j + 1)) * M + m] = P::to_w(cneg(v));
+    }
+  }
+  __syncthreads();
+  Tile<P> t{sm, sm + M * N, M, prm.log2m, 1, M};
+  cta_fft<P, DIR>(t, sp, tw);
+  for (int e = threadIdx.x; e < M * prm.Lout; e += blockDim.x) {
+    const int m = e & (M - 1);
+    const int jo = e >> prm.log2m;
+    if (x0 + m >= prm.X) continue;
+    const int k = jo < prm.smap_s0 ? jo : jo + prm.smap_d;
+    C v;
+    if (prm.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
+    else v = P::from_w(sm[k * M + m]);
+    store_elem<P>(prm.out, prm.out_user, obase + m + jo * prm.out_axis, v);
+  }
+}
+
+// ------------------------------------------------------------- Chebyshev
+// out(k) = L k old + out(k+2), ftran.F90:412-451, one thread per (x, y) pencil.
+template <class P>
+__global__ void k_cheby(const ChebyParams prm) {
+  using C = typename P::C;
+  using UC = typename P::UC;
+  const int pcl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pcl >= prm.npencil) return;
+  UC* d = static_cast<UC*>(prm.data) + blockIdx.y * prm.field + pcl * prm.pstride;
+  const int n = prm.nzc;
+  const long long zs = prm.zstride;
+  auto scaled = [&](int k) { return mulr(P::from_uc(d[k * zs]), prm.sc_hi, prm.sc_lo); };
+  auto lk = [&](int k, C v) {  // (4/Lz) * k * v
+    const df f = dmulc(df{(float)k, 0.0f}, prm.l_hi, prm.l_lo);
+    return mulr(v, f.hi, f.lo);
+  };
+  C old = scaled(n - 2);
+  C o1 = cscale2(lk(n - 1, scaled(n - 1)), 0.5f);  // out(nzc-1)
+  C o2 = P::zero();                                // out(nzc)
+  d[(n - 2) * zs] = P::to_uc(o1);
+  d[(n - 1) * zs] = P::to_uc(o2);
+  for (int k = n - 3; k >= 0; --k) {
+    const C nw = scaled(k);
+    const C val = lk(k + 1, old) + o2;
+    d[k * zs] = P::to_uc(val);
+    o2 = o1;
+    o1 = val;
+    old = nw;
+  }
+  d[0] = P::to_uc(cscale2(P::from_uc(d[0]), 0.5f));
+}
+
+// ---------------------------------------------------------------- launchers
+template <class P>
+cudaError_t launch_x_r2c(const XParams& p, const StagePlan* sp, const float4* tw, int threads, size_t smem,
+                         int nfields, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_x_r2c<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr = true;
+  }
+  k_x_r2c<P><<<dim3(p.tiles, nfields), threads, smem, st>>>(p, sp, tw);
+  return cudaGetLastError();
+}
+template <class P>
+cudaError_t launch_x_c2r(const XParams& p, const StagePlan* sp, const float4* tw, int threads, size_t smem,
+                         int nfields, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_x_c2r<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr = true;
+  }
+  k_x_c2r<P><<<dim3(p.tiles, nfields), threads, smem, st>>>(p, sp, tw);
+  return cudaGetLastError();
+}
+template <class P>
+cudaError_t launch_strided(const SParams& p, const StagePlan* sp, const float4* tw, bool forward_sign, int threads,
+                           size_t smem, int nfields, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_strided<P, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_strided<P, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr = true;
+  }
+  const long long blocks = (long long)p.xtiles * p.O1 * nfields;
+  if (blocks <= 0 || blocks > 0x7FFFFFFFLL) return cudaErrorInvalidConfiguration;
+  if (forward_sign) k_strided<P, -1><<<(unsigned)blocks, threads, smem, st>>>(p, sp, tw);
+  else k_strided<P, 1><<<(unsigned)blocks, threads, smem, st>>>(p, sp, tw);
+  return cudaGetLastError();
+}
+template <class P>
+cudaError_t launch_cheby(const ChebyParams& p, int nfields, cudaStream_t st) {
+  const int threads = 128;
+  k_cheby<P><<<dim3((p.npencil + threads - 1) / threads, nfields), threads, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
+#define P3G_INSTANTIATE(P)                                                                                          \
+  template cudaError_t launch_x_r2c<P>(const XParams&, const StagePlan*, const float4*, int, size_t, int,          \
+                                       cudaStream_t);                                                              \
+  template cudaError_t launch_x_c2r<P>(const XParams&, const StagePlan*, const float4*, int, size_t, int,          \
+                                       cudaStream_t);                                                              \
+  template cudaError_t launch_strided<P>(const SParams&, const StagePlan*, const float4*, bool, int, size_t, int,  \
+                                         cudaStream_t);                                                            \
+  template cudaError_t launch_cheby<P>(const ChebyParams&, int, cudaStream_t);
+
+}  // namespace p3g

@@ -1,0 +1,743 @@
+// Host plan and C-ABI of the explicit device API (include/p3dfft_gb300.h).
+//
+// A plan replaces the reference's p3dfft_setup + init_plan (build/setup.F90,
+// build/init_plan.F90) for one rank on a 1x1 processor grid: it factors each
+// axis length into radix stages, generates the twiddle tables once in FP64
+// (long double on the host), uploads them with the stage plans, and sizes the
+// per-pass tiles.  Transforms run three passes per direction:
+//   forward:  X r2c (user real -> workspace), Y c2c (workspace -> workspace,
+//             y pruning on store), Z op (workspace -> user complex, z pruning)
+//   backward: Z op (user complex -> workspace, z zero-fill on load), Y c2c
+//             (y zero-fill on load), X c2r (workspace -> user real)
+// replacing ftran.F90:489-780 / btran.F90:396-679, whose 1x1 path runs the
+// same FFTs with seg_copy/seg_zero passes (module.F90:502-706) in between.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/p3dfft_gb300.h"
+#include "p3g_kernels.cuh"
+
+namespace p3g {
+
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+#define P3G_CUDA_TRY(call)                                                                 \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return fail(P3G_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// ------------------------------------------------------------ factorisation
+// Stage radices for length n, ordered by family (16, 8, 4, 2, 3, 5, other
+// primes) as cta_fft expects.  Powers of two use radix 8 (and 16 on the F32
+// path) with a 4 or 2 remainder.
+static bool factor(int n, bool allow16, std::vector<int>& radices) {
+  radices.clear();
+  int a = 0;
+  while (n % 2 == 0) {
+    n /= 2;
+    ++a;
+  }
+  std::vector<int> pow2;
+  if (allow16) {
+    while (a >= 4 && a != 5) {  // 2^5 = 8*4 beats 16*2
+      pow2.push_back(16);
+      a -= 4;
+    }
+  }
+  while (a >= 3 && a != 4) {
+    pow2.push_back(8);
+    a -= 3;
+  }
+  if (a == 4) {
+    pow2.push_back(4);
+    pow2.push_back(4);
+  } else if (a == 2) {
+    pow2.push_back(4);
+  } else if (a == 1) {
+    pow2.push_back(2);
+  } else if (a == 3) {
+    pow2.push_back(8);
+  }
+  for (int r : {16, 8, 4, 2})
+    for (int x : pow2)
+      if (x == r) radices.push_back(r);
+  for (int p : {3, 5}) {
+    while (n % p == 0) {
+      radices.push_back(p);
+      n /= p;
+    }
+  }
+  for (int p = 7; n > 1; p += 2) {
+    while (n % p == 0) {
+      radices.push_back(p);
+      n /= p;
+    }
+    if ((long long)p * p > n && n > 1) {
+      radices.push_back(n);
+      n = 1;
+    }
+  }
+  return (int)radices.size() <= kMaxStages;
+}
+
+struct HostTw {
+  std::vector<float4> v;
+  int push_root(long long num, long long den) {  // exp(-2 pi i num/den), split into hi/lo
+    const long double two_pi = 6.283185307179586476925286766559L;
+    long long t = num % den;
+    const long double ang = -two_pi * (long double)t / (long double)den;
+    const long double c = cosl(ang), s = sinl(ang);
+    const float ch = (float)c, sh = (float)s;
+    const float cl = (float)(c - (long double)ch), sl = (float)(s - (long double)sh);
+    v.push_back(make_float4(ch, sh, cl, sl));
+    return (int)v.size() - 1;
+  }
+};
+
+struct AxisPlan {
+  StagePlan sp{};
+  int n = 0;
+  int M = 1, log2m = 0, threads = 32;
+  size_t smem = 0;
+  int sp_index = 0;  // index into the device StagePlan array
+};
+
+static bool build_stages(int n, bool allow16, HostTw& tw, StagePlan& sp) {
+  std::memset(&sp, 0, sizeof(sp));
+  sp.n = n;
+  std::vector<int> rad;
+  if (n > 1 && !factor(n, allow16, rad)) return false;
+  sp.nstages = (int)rad.size();
+  int ns = 1;
+  for (int s = 0; s < sp.nstages; ++s) {
+    const int r = rad[s];
+    sp.radix[s] = r;
+    sp.ns[s] = ns;
+    switch (r) {
+      case 16: sp.cnt[0]++; break;
+      case 8: sp.cnt[1]++; break;
+      case 4: sp.cnt[2]++; break;
+      case 2: sp.cnt[3]++; break;
+      case 3: sp.cnt[4]++; break;
+      case 5: sp.cnt[5]++; break;
+      default: sp.has_generic = 1; break;
+    }
+    sp.tw_off[s] = (int)tw.v.size();
+    if (ns > 1) {
+      for (int k = 0; k < ns; ++k)
+        for (int q = 1; q < r; ++q) tw.push_root((long long)q * k, (long long)ns * r);
+    } else {
+      tw.push_root(0, 1);  // keep offsets valid
+    }
+    sp.root_off[s] = (int)tw.v.size();
+    if (r != 2 && r != 3 && r != 4 && r != 5 && r != 8 && r != 16)
+      for (int m = 0; m < r; ++m) tw.push_root(m, r);
+    ns *= r;
+  }
+  return true;
+}
+
+static int ilog2(int v) {
+  int l = 0;
+  while ((1 << l) < v) ++l;
+  return l;
+}
+
+// Tile sizing: M lines of n points so that one tile holds about `budget`
+// elements (64 KB), M a power of two not larger than needed, threads =
+// ceil(M n / E) rounded up to a warp.
+static bool size_tile(AxisPlan& ap, int n, int lines_avail, bool f64) {
+  const int budget = f64 ? 4096 : 8192;
+  const int max_threads = f64 ? 256 : 512;
+  const size_t esize = f64 ? 16 : 8;
+  int M = 1;
+  while (M * 2 * n <= budget && M * 2 <= (1 << ilog2(lines_avail > 0 ? lines_avail : 1))) M *= 2;
+  auto threads_for = [&](int m) {
+    int t = (m * n + kElemsPerThread - 1) / kElemsPerThread;
+    t = (t + 31) / 32 * 32;
+    return t < 32 ? 32 : t;
+  };
+  while (M > 1 && threads_for(M) > max_threads) M /= 2;
+  if (threads_for(M) > max_threads) return false;
+  ap.n = n;
+  ap.M = M;
+  ap.log2m = ilog2(M);
+  ap.threads = threads_for(M);
+  ap.smem = (size_t)M * n * esize * (ap.sp.has_generic ? 2 : 1);
+  return ap.smem <= 227 * 1024;
+}
+
+struct TimerRec {
+  int slot;
+  cudaEvent_t a, b;
+};
+
+}  // namespace p3g
+
+using namespace p3g;
+
+struct p3g_plan_s {
+  int nx, ny, nz, nxc, nyc, nzc, prec, layout, flags;
+  int nxh, nxhp, nxhc, nxhpc, nycph, nzcph;
+  long long pitch;
+  AxisPlan ax_x, ax_y, ax_z[4];  // z: 0 fft, 1 dct (2(nz-1)), 2 dst (2(nz+1)), 3 none
+  bool z_ok[4];
+  float4* d_tw = nullptr;
+  StagePlan* d_sp = nullptr;
+  size_t tw_bytes = 0;
+  void* wa = nullptr;  // nz*ny*pitch*nv elements
+  void* wb = nullptr;  // nz*nyc*pitch*nv elements (only if nyc < ny)
+  size_t w_fields = 0;
+  double timers[12];
+  std::vector<TimerRec> pending;
+  std::vector<cudaEvent_t> free_events;
+  long long launches = 0;
+  std::mutex mu;
+
+  size_t esize() const { return prec == P3G_F64 ? 16 : 8; }
+};
+
+namespace {
+
+int ensure_workspace(p3g_plan p, int nv) {
+  if ((size_t)nv <= p->w_fields) return P3G_OK;
+  if (p->wa) cudaFree(p->wa);
+  if (p->wb) cudaFree(p->wb);
+  p->wa = p->wb = nullptr;
+  p->w_fields = 0;
+  const size_t na = (size_t)p->nz * p->ny * p->pitch * nv * p->esize();
+  if (cudaMalloc(&p->wa, na) != cudaSuccess) {
+    cudaGetLastError();
+    p->wa = nullptr;
+    return fail(P3G_E_NOMEM, "workspace allocation failed (" + std::to_string(na) + " bytes)");
+  }
+  if (p->nyc < p->ny) {
+    const size_t nb = (size_t)p->nz * p->nyc * p->pitch * nv * p->esize();
+    if (cudaMalloc(&p->wb, nb) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(p->wa);
+      p->wa = p->wb = nullptr;
+      return fail(P3G_E_NOMEM, "workspace allocation failed (" + std::to_string(nb) + " bytes)");
+    }
+  }
+  p->w_fields = nv;
+  return P3G_OK;
+}
+
+cudaEvent_t get_event(p3g_plan p) {
+  if (!p->free_events.empty()) {
+    cudaEvent_t e = p->free_events.back();
+    p->free_events.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+struct PassTimer {
+  p3g_plan p;
+  int slot;
+  cudaStream_t st;
+  cudaEvent_t a = nullptr;
+  PassTimer(p3g_plan p_, int slot_, cudaStream_t st_) : p(p_), slot(slot_), st(st_) {
+    if (p->flags & P3G_FLAG_TIMERS) {
+      a = get_event(p);
+      cudaEventRecord(a, st);
+    }
+  }
+  void done() {
+    if (!a) return;
+    cudaEvent_t b = get_event(p);
+    cudaEventRecord(b, st);
+    p->pending.push_back(TimerRec{slot, a, b});
+    a = nullptr;
+  }
+};
+
+int op_index(char c, bool& forward_sign, bool natural_forward) {
+  switch (c) {
+    case 't':
+    case 'f':
+      forward_sign = natural_forward;
+      return 0;
+    case 'c':
+      forward_sign = true;
+      return 1;
+    case 's':
+      forward_sign = true;  // RODFT00 is the same transform in both directions
+      return 2;
+    case 'n':
+    case '0':
+      forward_sign = true;
+      return 3;
+    default:
+      return -1;
+  }
+}
+
+template <class P>
+int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int nv, cudaStream_t st) {
+  s.M = ap.M;
+  s.log2m = ap.log2m;
+  s.N = ap.n;
+  s.xtiles = (s.X + ap.M - 1) / ap.M;
+  cudaError_t e = launch_strided<P>(s, p->d_sp + ap.sp_index, p->d_tw, fwd_sign, ap.threads, ap.smem, nv, st);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("strided pass launch: ") + cudaGetErrorString(e));
+  p->launches++;
+  return P3G_OK;
+}
+
+template <class P>
+int do_ftran(p3g_plan p, const void* in, void* out, const char* op, int nv, long long dim_in, long long dim_out,
+             cudaStream_t st) {
+  bool fsign = true;
+  const int zi = op_index(op[2], fsign, true);
+  if (zi < 0) return fail(P3G_E_ARG, std::string("Unknown transform type: ") + op[2]);
+  if (!p->z_ok[zi]) return fail(P3G_E_UNSUPPORTED, std::string("Z transform '") + op[2] + "' unsupported for nz");
+  if (p->layout == P3G_LAYOUT_STRIDE1) return fail(P3G_E_UNSUPPORTED, "STRIDE1 layout is not built yet");
+  int rc = ensure_workspace(p, nv);
+  if (rc) return rc;
+  const long long P_ = p->pitch;
+  const long long wa_field = (long long)p->nz * p->ny * P_;
+  const long long wb_field = (long long)p->nz * p->nyc * P_;
+  void* ybuf = p->nyc < p->ny ? p->wb : p->wa;
+  const long long y_field = p->nyc < p->ny ? wb_field : wa_field;
+  // X r2c: user real -> wa
+  {
+    PassTimer tm(p, 4, st);
+    XParams x{};
+    x.in = in;
+    x.out = p->wa;
+    x.in_field = dim_in;
+    x.out_field = wa_field;
+    x.in_line = p->nx;
+    x.out_line = P_;
+    x.nlines = p->ny * p->nz;
+    x.nx = p->nx;
+    x.nkeep = p->nxhpc;
+    x.M = p->ax_x.M;
+    x.log2m = p->ax_x.log2m;
+    x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
+    cudaError_t e = launch_x_r2c<P>(x, p->d_sp + p->ax_x.sp_index, p->d_tw, p->ax_x.threads, p->ax_x.smem, nv, st);
+    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X r2c launch: ") + cudaGetErrorString(e));
+    p->launches++;
+    tm.done();
+  }
+  // Y c2c: wa -> ybuf, keeping y modes 0..nycph-1 and the top nyc-nycph (seg_copy_y, ftran.F90:736-738)
+  {
+    PassTimer tm(p, 6, st);
+    SParams s{};
+    s.in = p->wa;
+    s.out = ybuf;
+    s.in_user = 0;
+    s.out_user = 0;
+    s.in_axis = P_;
+    s.in_o1 = (long long)p->ny * P_;
+    s.in_o2 = wa_field;
+    s.out_axis = P_;
+    s.out_o1 = (long long)p->nyc * P_;
+    s.out_o2 = y_field;
+    s.X = p->nxhpc;
+    s.O1 = p->nz;
+    s.L = p->ny;
+    s.Lout = p->nyc;
+    s.pre = 0;
+    s.post = 0;
+    s.lmap_a0 = p->ny;
+    s.lmap_a1 = p->ny;
+    s.lmap_d = 0;
+    s.smap_s0 = p->nycph;
+    s.smap_d = p->ny - p->nyc;
+    rc = run_strided<P>(p, s, p->ax_y, true, nv, st);
+    if (rc) return rc;
+    tm.done();
+  }
+  // Z op: ybuf -> user complex, keeping z modes 0..nzcph-1 and the top nzc-nzcph (seg_copy_z, ftran.F90:705-706)
+  {
+    PassTimer tm(p, 7, st);
+    SParams s{};
+    s.in = ybuf;
+    s.out = out;
+    s.in_user = 0;
+    s.out_user = 1;
+    s.in_axis = (long long)p->nyc * P_;
+    s.in_o1 = P_;
+    s.in_o2 = y_field;
+    s.out_axis = (long long)p->nxhpc * p->nyc;
+    s.out_o1 = p->nxhpc;
+    s.out_o2 = dim_out;
+    s.X = p->nxhpc;
+    s.O1 = p->nyc;
+    s.L = p->nz;
+    s.Lout = p->nzc;
+    s.pre = zi == 1 ? 1 : (zi == 2 ? 2 : 0);
+    s.post = zi == 2 ? 1 : 0;
+    s.lmap_a0 = p->nz;
+    s.lmap_a1 = p->nz;
+    s.lmap_d = 0;
+    s.smap_s0 = p->nzcph;
+    s.smap_d = p->nz - p->nzc;
+    rc = run_strided<P>(p, s, p->ax_z[zi], fsign, nv, st);
+    if (rc) return rc;
+    tm.done();
+  }
+  return P3G_OK;
+}
+
+template <class P>
+int do_btran(p3g_plan p, const void* in, void* out, const char* op, int nv, long long dim_in, long long dim_out,
+             cudaStream_t st) {
+  bool fsign = false;
+  const int zi = op_index(op[0], fsign, false);
+  if (zi < 0) return fail(P3G_E_ARG, std::string("Unknown transform type: ") + op[0]);
+  if (!p->z_ok[zi]) return fail(P3G_E_UNSUPPORTED, std::string("Z transform '") + op[0] + "' unsupported for nz");
+  int rc = ensure_workspace(p, nv);
+  if (rc) return rc;
+  if (p->layout == P3G_LAYOUT_STRIDE1) return fail(P3G_E_UNSUPPORTED, "STRIDE1 layout is not built yet");
+  const long long P_ = p->pitch;
+  const long long wa_field = (long long)p->nz * p->ny * P_;
+  const long long wb_field = (long long)p->nz * p->nyc * P_;
+  void* zbuf = p->nyc < p->ny ? p->wb : p->wa;
+  const long long z_field = p->nyc < p->ny ? wb_field : wa_field;
+  // Z op: user complex -> zbuf with z zero-fill (seg_copy_z + seg_zero_z, btran.F90:553-555)
+  {
+    PassTimer tm(p, 8, st);
+    SParams s{};
+    s.in = in;
+    s.out = zbuf;
+    s.in_user = 1;
+    s.out_user = 0;
+    s.in_axis = (long long)p->nxhpc * p->nyc;
+    s.in_o1 = p->nxhpc;
+    s.in_o2 = dim_in;
+    s.out_axis = (long long)p->nyc * P_;
+    s.out_o1 = P_;
+    s.out_o2 = z_field;
+    s.X = p->nxhpc;
+    s.O1 = p->nyc;
+    s.L = p->nz;
+    s.Lout = p->nz;
+    s.pre = zi == 1 ? 1 : (zi == 2 ? 2 : 0);
+    s.post = zi == 2 ? 1 : 0;
+    s.lmap_a0 = p->nzcph;
+    s.lmap_a1 = p->nz - p->nzcph;
+    s.lmap_d = p->nz - p->nzc;
+    s.smap_s0 = p->nz;
+    s.smap_d = 0;
+    rc = run_strided<P>(p, s, p->ax_z[zi], fsign, nv, st);
+    if (rc) return rc;
+    tm.done();
+  }
+  // Y c2c backward: zbuf -> wa with y zero-fill (seg_copy_y + seg_zero_y, btran.F90:585-588)
+  {
+    PassTimer tm(p, 9, st);
+    SParams s{};
+    s.in = zbuf;
+    s.out = p->wa;
+    s.in_user = 0;
+    s.out_user = 0;
+    s.in_axis = P_;
+    s.in_o1 = (long long)p->nyc * P_;
+    s.in_o2 = z_field;
+    s.out_axis = P_;
+    s.out_o1 = (long long)p->ny * P_;
+    s.out_o2 = wa_field;
+    s.X = p->nxhpc;
+    s.O1 = p->nz;
+    s.L = p->ny;
+    s.Lout = p->ny;
+    s.lmap_a0 = p->nycph;
+    s.lmap_a1 = p->ny - p->nycph;
+    s.lmap_d = p->ny - p->nyc;
+    s.smap_s0 = p->ny;
+    s.smap_d = 0;
+    rc = run_strided<P>(p, s, p->ax_y, false, nv, st);
+    if (rc) return rc;
+    tm.done();
+  }
+  // X c2r: wa -> user real, x modes beyond nxhpc read as zero (seg_zero_x, btran.F90:662-663)
+  {
+    PassTimer tm(p, 11, st);
+    XParams x{};
+    x.in = p->wa;
+    x.out = out;
+    x.in_field = wa_field;
+    x.out_field = dim_out;
+    x.in_line = P_;
+    x.out_line = p->nx;
+    x.nlines = p->ny * p->nz;
+    x.nx = p->nx;
+    x.nkeep = p->nxhpc;
+    x.M = p->ax_x.M;
+    x.log2m = p->ax_x.log2m;
+    x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
+    cudaError_t e = launch_x_c2r<P>(x, p->d_sp + p->ax_x.sp_index, p->d_tw, p->ax_x.threads, p->ax_x.smem, nv, st);
+    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X c2r launch: ") + cudaGetErrorString(e));
+    p->launches++;
+    tm.done();
+  }
+  return P3G_OK;
+}
+
+bool valid_op(const char* op) { return op && op[0] && op[1] && op[2]; }
+
+void split_df(long double v, float& hi, float& lo) {
+  hi = (float)v;
+  lo = (float)(v - (long double)hi);
+}
+
+}  // namespace
+
+extern "C" {
+
+int p3g_version(void) { return 100; }
+
+const char* p3g_last_error(void) { return g_last_error.c_str(); }
+
+int p3g_plan_create(p3g_plan* out, int nx, int ny, int nz, int nxc, int nyc, int nzc, int precision, int layout,
+                    int flags) {
+  if (!out) return fail(P3G_E_ARG, "plan pointer is NULL");
+  *out = nullptr;
+  if (nx <= 0 || ny <= 0 || nz <= 0)
+    return fail(P3G_E_ARG, "Invalid dimensions : " + std::to_string(nx) + " " + std::to_string(ny) + " " +
+                               std::to_string(nz));
+  if (nxc <= 0) nxc = nx;
+  if (nyc <= 0) nyc = ny;
+  if (nzc <= 0) nzc = nz;
+  if (nxc > nx || nyc > ny || nzc > nz) return fail(P3G_E_ARG, "pruned sizes must not exceed the grid");
+  if (precision != P3G_F64 && precision != P3G_F32) return fail(P3G_E_ARG, "unknown precision");
+  if (layout != P3G_LAYOUT_XYZ && layout != P3G_LAYOUT_STRIDE1) return fail(P3G_E_ARG, "unknown layout");
+  auto* p = new p3g_plan_s();
+  p->nx = nx;
+  p->ny = ny;
+  p->nz = nz;
+  p->nxc = nxc;
+  p->nyc = nyc;
+  p->nzc = nzc;
+  p->prec = precision;
+  p->layout = layout;
+  p->flags = flags;
+  p->nxh = nx / 2;
+  p->nxhp = p->nxh + 1;
+  p->nxhc = nxc / 2;
+  p->nxhpc = p->nxhc + 1;
+  p->nycph = (nyc + 1) / 2;
+  p->nzcph = (nzc + 1) / 2;
+  std::memset(p->timers, 0, sizeof(p->timers));
+  const bool f64 = precision == P3G_F64;
+  const long long align = f64 ? 8 : 16;  // 128-byte workspace rows
+  p->pitch = (p->nxhpc + align - 1) / align * align;
+
+  HostTw tw;
+  std::vector<StagePlan> sps;
+  auto add_axis = [&](AxisPlan& ap, int n, int lines) -> bool {
+    if (!build_stages(n, !f64, tw, ap.sp)) return false;
+    if (!size_tile(ap, n, lines, f64)) return false;
+    ap.sp_index = (int)sps.size();
+    sps.push_back(ap.sp);
+    return true;
+  };
+  auto bad = [&](const std::string& m) {
+    delete p;
+    return fail(P3G_E_UNSUPPORTED, m);
+  };
+  if (!add_axis(p->ax_x, nx, (ny * nz + 1) / 2)) return bad("x length " + std::to_string(nx) + " is too long");
+  if (!add_axis(p->ax_y, ny, p->nxhpc)) return bad("y length " + std::to_string(ny) + " is too long");
+  p->z_ok[0] = add_axis(p->ax_z[0], nz, p->nxhpc);
+  p->z_ok[1] = nz >= 2 && add_axis(p->ax_z[1], 2 * (nz - 1), p->nxhpc);
+  p->z_ok[2] = add_axis(p->ax_z[2], 2 * (nz + 1), p->nxhpc);
+  p->z_ok[3] = add_axis(p->ax_z[3], 1, p->nxhpc);
+  if (p->z_ok[3]) {  // 'none': a copy pass of nz rows, no stages
+    p->ax_z[3].n = nz;
+    sps[p->ax_z[3].sp_index].n = nz;
+    p->ax_z[3].sp.n = nz;
+    if (!size_tile(p->ax_z[3], nz, p->nxhpc, f64)) p->z_ok[3] = false;
+  }
+  if (!p->z_ok[0] && !p->z_ok[1] && !p->z_ok[3]) return bad("z length " + std::to_string(nz) + " is too long");
+
+  p->tw_bytes = tw.v.size() * sizeof(float4);
+  if (cudaMalloc(&p->d_tw, p->tw_bytes) != cudaSuccess ||
+      cudaMalloc(&p->d_sp, sps.size() * sizeof(StagePlan)) != cudaSuccess) {
+    cudaGetLastError();
+    if (p->d_tw) cudaFree(p->d_tw);
+    delete p;
+    return fail(P3G_E_NOMEM, "plan table allocation failed");
+  }
+  if (cudaMemcpy(p->d_tw, tw.v.data(), p->tw_bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(p->d_sp, sps.data(), sps.size() * sizeof(StagePlan), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(p->d_tw);
+    cudaFree(p->d_sp);
+    delete p;
+    return fail(P3G_E_CUDA, "plan table upload failed");
+  }
+  *out = p;
+  return P3G_OK;
+}
+
+int p3g_plan_destroy(p3g_plan p) {
+  if (!p) return P3G_OK;
+  for (auto& r : p->pending) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (auto e : p->free_events) cudaEventDestroy(e);
+  if (p->wa) cudaFree(p->wa);
+  if (p->wb) cudaFree(p->wb);
+  if (p->d_tw) cudaFree(p->d_tw);
+  if (p->d_sp) cudaFree(p->d_sp);
+  delete p;
+  return P3G_OK;
+}
+
+int p3g_get_dims(p3g_plan p, int conf, int start[3], int end[3], int size[3]) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  if (conf == 1) {
+    const int s[3] = {p->nx, p->ny, p->nz};
+    for (int i = 0; i < 3; ++i) {
+      start[i] = 1;
+      end[i] = size[i] = s[i];
+    }
+  } else if (conf == 2) {
+    int s[3] = {p->nxhpc, p->nyc, p->nzc};
+    if (p->layout == P3G_LAYOUT_STRIDE1) {
+      s[0] = p->nzc;
+      s[2] = p->nxhpc;
+    }
+    for (int i = 0; i < 3; ++i) {
+      start[i] = 1;
+      end[i] = size[i] = s[i];
+    }
+  } else if (conf == 3) {
+    // setup.F90:580-603 at 1x1: pad1 = 2*max(nz*nyc*nxhpc, ny*nz*nxhpc) - nx*ny*nz
+    long long pad1 = 2LL * std::max((long long)p->nz * p->nyc * p->nxhpc, (long long)p->ny * p->nz * p->nxhpc) -
+                     (long long)p->nx * p->ny * p->nz;
+    if (pad1 < 0) pad1 = 0;
+    const long long den = (long long)p->nx * p->ny;
+    const long long padi = pad1 / den + (pad1 % den ? 1 : 0);
+    const int s[3] = {p->nx, p->ny, (int)(p->nz + padi)};
+    for (int i = 0; i < 3; ++i) {
+      start[i] = 0;
+      end[i] = size[i] = s[i];
+    }
+  } else {
+    return fail(P3G_E_ARG, "conf must be 1, 2 or 3");
+  }
+  return P3G_OK;
+}
+
+int p3g_ftran_r2c(p3g_plan p, const void* in, void* out, const char* op, int nv, long long dim_in, long long dim_out,
+                  void* stream) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  if (!valid_op(op)) return fail(P3G_E_ARG, "op must have 3 letters");
+  if (nv <= 0 || nv > 65535) return fail(P3G_E_ARG, "nv out of range");
+  if (!in || !out) return fail(P3G_E_ARG, "NULL array");
+  const long long rsize = (long long)p->nx * p->ny * p->nz;
+  const long long csize = (long long)p->nxhpc * p->nyc * p->nzc;
+  if (dim_in <= 0) dim_in = rsize;
+  if (dim_out <= 0) dim_out = csize;
+  if (dim_in < rsize) return fail(P3G_E_ARG, "ftran error: input array dimensions are too low");
+  if (dim_out < csize) return fail(P3G_E_ARG, "ftran error: output array dimensions are too low");
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  return p->prec == P3G_F64 ? do_ftran<PathF64>(p, in, out, op, nv, dim_in, dim_out, st)
+                            : do_ftran<PathF32>(p, in, out, op, nv, dim_in, dim_out, st);
+}
+
+int p3g_btran_c2r(p3g_plan p, const void* in, void* out, const char* op, int nv, long long dim_in, long long dim_out,
+                  void* stream) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  if (!valid_op(op)) return fail(P3G_E_ARG, "op must have 3 letters");
+  if (nv <= 0 || nv > 65535) return fail(P3G_E_ARG, "nv out of range");
+  if (!in || !out) return fail(P3G_E_ARG, "NULL array");
+  const long long rsize = (long long)p->nx * p->ny * p->nz;
+  const long long csize = (long long)p->nxhpc * p->nyc * p->nzc;
+  if (dim_in <= 0) dim_in = csize;
+  if (dim_out <= 0) dim_out = rsize;
+  if (dim_in < csize) return fail(P3G_E_ARG, "btran error: input array dimensions are too low");
+  if (dim_out < rsize) return fail(P3G_E_ARG, "btran error: output array dimensions are too low");
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  return p->prec == P3G_F64 ? do_btran<PathF64>(p, in, out, op, nv, dim_in, dim_out, st)
+                            : do_btran<PathF32>(p, in, out, op, nv, dim_in, dim_out, st);
+}
+
+int p3g_cheby(p3g_plan p, const void* in, void* out, double lz, int nv, long long dim_in, long long dim_out,
+              void* stream) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  if (p->nzc < 2) return fail(P3G_E_ARG, "Chebyshev transform needs nzc >= 2");
+  if (!(lz != 0.0)) return fail(P3G_E_ARG, "Lz must be non-zero");
+  int rc = p3g_ftran_r2c(p, in, out, "ffc", nv, dim_in, dim_out, stream);
+  if (rc) return rc;
+  const long long csize = (long long)p->nxhpc * p->nyc * p->nzc;
+  if (dim_out <= 0) dim_out = csize;
+  std::lock_guard<std::mutex> lk(p->mu);
+  ChebyParams c{};
+  c.data = out;
+  c.field = dim_out;
+  c.npencil = p->nxhpc * p->nyc;
+  c.nzc = p->nzc;
+  if (p->layout == P3G_LAYOUT_STRIDE1) {
+    c.pstride = p->nzc;
+    c.zstride = 1;
+  } else {
+    c.pstride = 1;
+    c.zstride = (long long)p->nxhpc * p->nyc;
+  }
+  split_df(1.0L / ((long double)p->nx * (long double)p->ny * (long double)(p->nzc - 1)), c.sc_hi, c.sc_lo);
+  split_df(4.0L / (long double)lz, c.l_hi, c.l_lo);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  PassTimer tm(p, 7, st);
+  cudaError_t e = p->prec == P3G_F64 ? launch_cheby<PathF64>(c, nv, st) : launch_cheby<PathF32>(c, nv, st);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("cheby launch: ") + cudaGetErrorString(e));
+  p->launches++;
+  tm.done();
+  return P3G_OK;
+}
+
+int p3g_get_timers(p3g_plan p, double timers[12]) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  std::lock_guard<std::mutex> lk(p->mu);
+  for (auto& r : p->pending) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess)
+      p->timers[r.slot] += ms * 1e-3;
+    p->free_events.push_back(r.a);
+    p->free_events.push_back(r.b);
+  }
+  p->pending.clear();
+  std::memcpy(timers, p->timers, sizeof(p->timers));
+  return P3G_OK;
+}
+
+int p3g_set_timers(p3g_plan p) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  double tmp[12];
+  p3g_get_timers(p, tmp);
+  std::lock_guard<std::mutex> lk(p->mu);
+  std::memset(p->timers, 0, sizeof(p->timers));
+  return P3G_OK;
+}
+
+long long p3g_plan_device_bytes(p3g_plan p) {
+  if (!p) return 0;
+  long long b = (long long)p->tw_bytes + 6LL * sizeof(StagePlan);
+  if (p->wa) b += (long long)p->nz * p->ny * p->pitch * p->w_fields * p->esize();
+  if (p->wb) b += (long long)p->nz * p->nyc * p->pitch * p->w_fields * p->esize();
+  return b;
+}
+
+long long p3g_plan_launches(p3g_plan p) { return p ? p->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,256 @@
+"""GPU parity of the sm_103a transforms against the CPU oracle (through the C-ABI).
+
+Tolerances: F64 path, normalised L-inf (max|gpu - oracle| / max|oracle|)
+<= 1e-12 for forward and backward outputs; F32 path, relative L2 <= 1e-6
+against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from oracle import p3dfft_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+F64_TOL = 1e-12
+F32_TOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import p3dfft_gb300  # noqa: F401  (loads the native libraries; no fallback)
+    return torch
+
+
+def _rand(shape, seed):
+    return np.random.default_rng(seed).uniform(-1.0, 1.0, size=shape)
+
+
+def _spectrum(shape, seed):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+def _run_pair(torch, plan_args, a, op_f, op_b, precision, seed=0):
+    import p3dfft_gb300 as pg
+    nx, ny, nz = plan_args[:3]
+    pruned = plan_args[3:] if len(plan_args) > 3 else (nx, ny, nz)
+    plan = pg.Plan(nx, ny, nz, *pruned, precision=precision)
+    ref = orc.OraclePlan(nx, ny, nz, *pruned)
+    rdt = torch.float64 if precision == pg.F64 else torch.float32
+    x = torch.from_numpy(a).to("cuda", rdt)
+    b = plan.ftran_r2c(x, op=op_f)
+    want_b = ref.ftran_r2c(a, op_f)
+    c_in = _spectrum(want_b.shape, seed + 1)
+    cdt = torch.complex128 if precision == pg.F64 else torch.complex64
+    r = plan.btran_c2r(torch.from_numpy(c_in).to("cuda", cdt), op=op_b)
+    want_r = ref.btran_c2r(c_in, op_b)
+    torch.cuda.synchronize()
+    got_b = b.cpu().numpy().astype(np.complex128)
+    got_r = r.cpu().numpy().astype(np.float64)
+    plan.close()
+    return got_b, want_b, got_r, want_r
+
+
+SIZES = [
+    (32, 32, 32),
+    (16, 8, 4),
+    (14, 26, 38),    # 7, 13, 19: generic prime stages (the reference's uneven-grid test)
+    (15, 9, 7),      # odd lengths everywhere
+    (48, 64, 96),
+    (120, 160, 192),
+    (60, 36, 45),
+    (2, 3, 5),
+    (1, 4, 6),
+    (128, 128, 128),
+]
+
+
+@pytest.mark.parametrize("shape", SIZES)
+def test_f64_fft_parity(torch_cuda, shape):
+    import p3dfft_gb300 as pg
+    a = _rand(shape[::-1], 11)
+    gb, wb, gr, wr = _run_pair(torch_cuda, shape, a, "fft", "tff", pg.F64)
+    assert orc.normalised_linf(gb, wb) <= F64_TOL
+    assert orc.normalised_linf(gr, wr) <= F64_TOL
+
+
+@pytest.mark.parametrize("shape", [(32, 32, 33), (16, 12, 9), (24, 20, 17), (8, 8, 2)])
+@pytest.mark.parametrize("ops", [("ffc", "cff"), ("ffs", "sff"), ("ffn", "nff"), ("fff", "fff")])
+def test_f64_z_ops_parity(torch_cuda, shape, ops):
+    import p3dfft_gb300 as pg
+    a = _rand(shape[::-1], 5)
+    gb, wb, gr, wr = _run_pair(torch_cuda, shape, a, ops[0], ops[1], pg.F64)
+    assert orc.normalised_linf(gb, wb) <= F64_TOL
+    assert orc.normalised_linf(gr, wr) <= F64_TOL
+
+
+@pytest.mark.parametrize("args", [(64, 64, 64, 32, 32, 32), (16, 12, 10, 8, 6, 4), (16, 16, 16, 10, 9, 7),
+                                  (20, 18, 16, 20, 7, 16), (24, 24, 24, 24, 24, 9)])
+def test_f64_pruned_parity(torch_cuda, args):
+    import p3dfft_gb300 as pg
+    a = _rand(args[:3][::-1], 3)
+    gb, wb, gr, wr = _run_pair(torch_cuda, args, a, "fft", "tff", pg.F64)
+    assert orc.normalised_linf(gb, wb) <= F64_TOL
+    assert orc.normalised_linf(gr, wr) <= F64_TOL
+
+
+@pytest.mark.parametrize("shape", [(32, 32, 32), (14, 26, 38), (120, 160, 192), (128, 128, 128)])
+def test_f32_parity(torch_cuda, shape):
+    import p3dfft_gb300 as pg
+    a = _rand(shape[::-1], 21)
+    gb, wb, gr, wr = _run_pair(torch_cuda, shape, a, "fft", "tff", pg.F32)
+    assert orc.relative_l2(gb, wb) <= F32_TOL
+    assert orc.relative_l2(gr, wr) <= F32_TOL
+
+
+def test_f64_roundtrip_sample_rule(torch_cuda):
+    # driver_rand.F90: ftran 'fft', multiply by 1/N, btran 'tff', max |diff| <= 1e-14 N/4
+    import p3dfft_gb300 as pg
+    nx = ny = nz = 128
+    a = np.random.default_rng(99).random((nz, ny, nx))
+    plan = pg.Plan(nx, ny, nz)
+    x = torch_cuda.from_numpy(a).cuda()
+    b = plan.ftran_r2c(x, op="fft")
+    b *= 1.0 / a.size
+    r = plan.btran_c2r(b, op="tff")
+    err = float((r - x).abs().max())
+    assert err <= orc.roundtrip_tolerance(a.size)
+    assert err < 1e-13
+
+
+def test_many_fields(torch_cuda):
+    import p3dfft_gb300 as pg
+    nx, ny, nz, nv = 16, 12, 10, 3
+    plan = pg.Plan(nx, ny, nz)
+    ref = orc.OraclePlan(nx, ny, nz)
+    rsize = nx * ny * nz
+    csize = (nx // 2 + 1) * ny * nz
+    dim_in, dim_out = rsize + 5, csize + 3
+    a = _rand((nv, dim_in), 8)
+    x = torch_cuda.from_numpy(a).cuda()
+    out = torch_cuda.zeros((nv, dim_out), dtype=torch_cuda.complex128, device="cuda")
+    plan.ftran_r2c(x, out, op="fft", nv=nv, dim_in=dim_in, dim_out=dim_out)
+    back = torch_cuda.zeros((nv, dim_in), dtype=torch_cuda.float64, device="cuda")
+    plan.btran_c2r(out, back, op="tff", nv=nv, dim_in=dim_out, dim_out=dim_in)
+    got = out.cpu().numpy()
+    gback = back.cpu().numpy()
+    for v in range(nv):
+        want = ref.ftran_r2c(a[v, :rsize].reshape(nz, ny, nx), "fft")
+        assert orc.normalised_linf(got[v, :csize].reshape(want.shape), want) <= F64_TOL
+        assert np.all(got[v, csize:] == 0)  # padding untouched
+        wr = ref.btran_c2r(want, "tff")
+        assert orc.normalised_linf(gback[v, :rsize].reshape(nz, ny, nx), wr) <= F64_TOL
+        assert np.array_equal(gback[v, rsize:], a[v, rsize:] * 0)  # zero-initialised padding untouched
+
+
+def test_in_place_transform(torch_cuda):
+    # ftran_r2c(B, B) / btran_c2r(B, B) on one buffer sized by memsize (driver_sine_inplace)
+    import p3dfft_gb300 as pg
+    nx, ny, nz = 16, 16, 16
+    plan = pg.Plan(nx, ny, nz)
+    _, _, mem = plan.get_dims(3)
+    buf = torch_cuda.zeros(mem[0] * mem[1] * mem[2], dtype=torch_cuda.float64, device="cuda")
+    a = _rand((nz, ny, nx), 4)
+    buf[: a.size] = torch_cuda.from_numpy(a.ravel()).cuda()
+    plan.ftran_r2c(buf, buf, op="fft")
+    want = orc.OraclePlan(nx, ny, nz).ftran_r2c(a, "fft")
+    got = buf.view(torch_cuda.complex128)[: want.size].cpu().numpy().reshape(want.shape)
+    assert orc.normalised_linf(got, want) <= F64_TOL
+    buf.view(torch_cuda.complex128)[: want.size] *= 1.0 / a.size
+    plan.btran_c2r(buf, buf, op="tff")
+    back = buf[: a.size].cpu().numpy().reshape(a.shape)
+    assert np.abs(back - a).max() <= orc.roundtrip_tolerance(a.size)
+
+
+def test_cheby_known_answer(torch_cuda):
+    # driver_cheby.F90 on the device path: d/dz sin(z) on Gauss-Lobatto points
+    import p3dfft_gb300 as pg
+    nx, ny, nz, lz = 32, 32, 33, 2.0
+    coord_z = np.cos(np.pi * np.arange(nz) / (nz - 1)) * 2.0 / lz
+    a = np.broadcast_to(np.sin(coord_z)[:, None, None], (nz, ny, nx)).copy()
+    plan = pg.Plan(nx, ny, nz)
+    c = plan.cheby(torch_cuda.from_numpy(a).cuda(), lz)
+    want = orc.OraclePlan(nx, ny, nz).cheby(a, lz)
+    assert orc.normalised_linf(c.cpu().numpy(), want) <= F64_TOL
+    c[0] *= 2.0
+    c[nz - 1] *= 2.0
+    c *= 0.5
+    r = plan.btran_c2r(c, op="cff").cpu().numpy()
+    assert np.abs(r - np.cos(coord_z)[:, None, None]).max() < 1e-12
+
+
+def test_dropin_host_api(torch_cuda):
+    # the reference's module interface with host arrays, as driver_rand.c uses it
+    import p3dfft_gb300 as pg
+    nx, ny, nz = 32, 16, 8
+    mem = pg.p3dfft_setup((1, 1), nx, ny, nz, 0, nx, ny, nz, False)
+    try:
+        assert pg.p3dfft_get_dims(1) == ((1, 1, 1), (nx, ny, nz), (nx, ny, nz))
+        s, e, fsize = pg.p3dfft_get_dims(2)
+        assert fsize == (nx // 2 + 1, ny, nz)
+        assert pg.p3dfft_get_dims(3)[2] == mem
+        a = np.random.default_rng(5).random((nz, ny, nx))
+        b = np.zeros((nz, ny, nx // 2 + 1), np.complex128)
+        pg.p3dfft_ftran_r2c(a, b, "fft")
+        want = orc.OraclePlan(nx, ny, nz).ftran_r2c(a, "fft")
+        assert orc.normalised_linf(b, want) <= F64_TOL
+        b *= 1.0 / a.size
+        c = np.zeros_like(a)
+        pg.p3dfft_btran_c2r(b, c, "tff")
+        assert np.abs(c - a).max() <= orc.roundtrip_tolerance(a.size)
+        t = pg.get_timers()
+        assert t[4] > 0 and t[6] > 0 and t[7] > 0 and t[8] > 0 and t[9] > 0 and t[11] > 0
+        assert t[0] == t[1] == t[2] == t[3] == 0
+        with pytest.raises(pg.P3DFFTError):
+            pg.p3dfft_ftran_r2c(a, b, "ffq")
+    finally:
+        pg.p3dfft_clean()
+    # timers survive clean (driver_rand.c reads them after Cp3dfft_clean)
+    assert pg.get_timers()[4] > 0
+    with pytest.raises(pg.P3DFFTError):
+        pg.p3dfft_get_dims(1)
+
+
+def test_dropin_single_precision(torch_cuda):
+    import p3dfft_gb300 as pg
+    nx, ny, nz = 16, 16, 16
+    pg.p3dfft_setup((1, 1), nx, ny, nz, single=True)
+    try:
+        a = np.random.default_rng(6).random((nz, ny, nx)).astype(np.float32)
+        b = np.zeros((nz, ny, nx // 2 + 1), np.complex64)
+        pg.p3dfft_ftran_r2c(a, b, "fft")
+        want = orc.OraclePlan(nx, ny, nz).ftran_r2c(a.astype(np.float64), "fft")
+        assert orc.relative_l2(b, want) <= F32_TOL
+        b *= 1.0 / a.size
+        c = np.zeros_like(a)
+        pg.p3dfft_btran_c2r(b, c, "tff")
+        assert np.abs(c - a).max() <= orc.roundtrip_tolerance(a.size, single=True)
+    finally:
+        pg.p3dfft_clean()
+
+
+def test_device_pointer_dropin(torch_cuda):
+    # device arrays go straight to the kernels (no staging)
+    import p3dfft_gb300 as pg
+    nx, ny, nz = 16, 12, 10
+    pg.p3dfft_setup((1, 1), nx, ny, nz)
+    try:
+        a = _rand((nz, ny, nx), 12)
+        x = torch_cuda.from_numpy(a).cuda()
+        b = torch_cuda.zeros((nz, ny, nx // 2 + 1), dtype=torch_cuda.complex128, device="cuda")
+        pg.p3dfft_ftran_r2c(x, b, "fft")
+        want = orc.OraclePlan(nx, ny, nz).ftran_r2c(a, "fft")
+        assert orc.normalised_linf(b.cpu().numpy(), want) <= F64_TOL
+    finally:
+        pg.p3dfft_clean()
+
+
+def test_unknown_op_is_an_error(torch_cuda):
+    import p3dfft_gb300 as pg
+    plan = pg.Plan(8, 8, 8)
+    x = torch_cuda.zeros((8, 8, 8), dtype=torch_cuda.float64, device="cuda")
+    with pytest.raises(pg.P3DFFTError, match="Unknown transform type"):
+        plan.ftran_r2c(x, op="ffx")
