@@ -181,6 +181,9 @@ def run_ours(args):
     npts = nx * ny * nz
     stream = torch.cuda.Stream(device=dev)
     peak, peak_kind = load_peaks()
+    # every torch op and every plan call below runs on one stream
+    ctx = torch.cuda.stream(stream)
+    ctx.__enter__()
 
     # ---- FP64 (headline)
     plan = pg.Plan(nx, ny, nz, precision=pg.F64, timers=True)
@@ -267,6 +270,7 @@ def run_ours(args):
     }
     if e2e:
         line["e2e"] = e2e
+    ctx.__exit__(None, None, None)
     if rank == 0 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
     if dist:
