@@ -42,6 +42,9 @@ CONFIGS = {
 }
 
 
+MODES = {"pipe_tma": (True, True), "pipe_cpasync": (True, False), "single_tile": (False, False)}
+
+
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -187,6 +190,7 @@ def run_ours(args):
 
     # ---- FP64 (headline)
     plan = pg.Plan(nx, ny, nz, precision=pg.F64, timers=True)
+    plan.set_options(*MODES[args.mode])
     kind = "uniform" if args.config == "small" else "modes"
     x = make_input(torch, grid, 1234 + rank, dev, kind)
     b = torch.empty(plan.complex_shape, dtype=torch.complex128, device=dev)
@@ -224,6 +228,7 @@ def run_ours(args):
 
     # ---- FP32 form on the same grid
     plan32 = pg.Plan(nx, ny, nz, precision=pg.F32)
+    plan32.set_options(*MODES[args.mode])
     x32 = x.float()
     b32 = torch.empty(plan32.complex_shape, dtype=torch.complex64, device=dev)
     r32 = torch.empty_like(x32)
@@ -266,6 +271,7 @@ def run_ours(args):
                      "step_bytes_model": bm["rt"],
                      "step_frac": round(bm["rt"] / (ms64 * 1e-3) / 1e9 / peak, 4)},
         "gpu_launches": launches,
+        "kernel_mode": args.mode,
         "clocks": clk.summary(),
     }
     if e2e:
@@ -376,6 +382,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="large", choices=sorted(CONFIGS))
+    ap.add_argument("--mode", default="pipe_tma", choices=sorted(MODES),
+                    help="kernel family: persistent pipelined with TMA or cp.async copies, or single-tile")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

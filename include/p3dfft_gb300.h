@@ -86,6 +86,14 @@ long long p3g_plan_device_bytes(p3g_plan plan);
 /* Kernel launches issued by this plan since creation. */
 long long p3g_plan_launches(p3g_plan plan);
 
+/* Synchronises and reports a kernel-side failure recorded on the plan's
+ * device flag (a pipelined pass whose bounded wait for a tile copy expired). */
+int p3g_plan_status(p3g_plan plan);
+/* Kernel selection: use_pipe = persistent double-buffered passes (default 1),
+ * use_tma = TMA tensor-tile copies where the layout allows (default 1).  With
+ * both 0 every pass runs the single-tile kernels. */
+int p3g_plan_set_options(p3g_plan plan, int use_pipe, int use_tma);
+
 const char* p3g_last_error(void);
 int p3g_version(void);
 

@@ -131,6 +131,14 @@ class Plan:
         _check(_core().p3g_cheby(self._h, _ptr(x), _ptr(out), float(lz), nv, dim_in, dim_out, _stream_ptr(stream)))
         return out
 
+    def set_options(self, pipe=True, tma=True):
+        """Kernel selection (see p3g_plan_set_options)."""
+        _check(_core().p3g_plan_set_options(self._h, int(pipe), int(tma)))
+
+    def check(self):
+        """Synchronise and raise if a kernel recorded a failure."""
+        _check(_core().p3g_plan_status(self._h))
+
     def timers(self):
         t = (ctypes.c_double * 12)()
         _check(_core().p3g_get_timers(self._h, t))

@@ -39,7 +39,7 @@ struct StagePlan {
 // complex float4 (re.hi, im.hi, re.lo, im.lo); the backward direction
 // multiplies by the conjugate.
 P3G_D cdf load_tw(const float4* __restrict__ tw, int idx) {
-  const float4 v = __ldg(tw + idx);
+  const float4 v = tw[idx];  // shared memory (pipelined passes) or global
   return cdf{df{v.x, v.z}, df{v.y, v.w}};
 }
 
@@ -69,15 +69,25 @@ P3G_D void cta_barrier() {
   asm volatile("bar.sync %0;" ::"n"(ID) : "memory");
 }
 
-template <class P, int DIR, int R>
+template <class P, int DIR, int R, int E = kElemsPerThread>
 __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const float4* __restrict__ tw) {
   using C = typename P::C;
-  constexpr int MAXB = (kElemsPerThread + R - 1) / R;
+  constexpr int MAXB = (E + R - 1) / R;
   const int per_line = N / R;
   const int nb = t.M * per_line;
   const int T = blockDim.x;
+  // Explicitly initialised: the arrays are written and read under correlated
+  // guards (b < nb) the compiler cannot prove, and inside a persistent tile
+  // loop an uninitialised element would otherwise be kept live around the
+  // loop, with every codelet's registers.
   C v[MAXB][R];
   int oline[MAXB], obase[MAXB];
+#pragma unroll
+  for (int i = 0; i < MAXB; ++i) {
+    obase[i] = 0;
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[i][q] = P::zero();
+  }
 #pragma unroll
   for (int i = 0; i < MAXB; ++i) {
     const int b = threadIdx.x + i * T;
@@ -147,11 +157,12 @@ __device__ __noinline__ void stage_generic(const Tile<P>& t, int N, int p, int n
   __syncthreads();
 }
 
-template <class P, int DIR, int R>
+template <class P, int DIR, int R, int E>
 __device__ __forceinline__ int run_family(const Tile<P>& t, const StagePlan* __restrict__ sp,
-                                          const float4* __restrict__ tw, int N, int s, int cnt) {
+                                          const float4* __restrict__ tw, int tw_base, int N, int s, int cnt) {
 #pragma unroll 1
-  for (int c = 0; c < cnt; ++c, ++s) stage_reg<P, DIR, R>(t, N, __ldg(&sp->ns[s]), tw + __ldg(&sp->tw_off[s]));
+  for (int c = 0; c < cnt; ++c, ++s)
+    stage_reg<P, DIR, R, E>(t, N, __ldg(&sp->ns[s]), tw + (__ldg(&sp->tw_off[s]) - tw_base));
   return s;
 }
 
@@ -163,22 +174,26 @@ __device__ __forceinline__ int run_family(const Tile<P>& t, const StagePlan* __r
 // memory, read with uniform cached loads.  Radix 16 is compiled only for the
 // F32 path (the F64 codelet needs ~200 registers; radix 8 has the same
 // double-float operation count per point for the sizes used here).
-template <class P, int DIR>
+// tw points at the twiddle table entry tw_base (the full table with
+// tw_base = 0, or a pass's slice copied to shared memory).
+// E = elements each thread holds per stage; the launch uses
+// ceil(M N / E) threads.
+template <class P, int DIR, int E = kElemsPerThread>
 __device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __restrict__ sp,
-                                        const float4* __restrict__ tw) {
+                                        const float4* __restrict__ tw, int tw_base = 0) {
   const int N = __ldg(&sp->n);
   int s = 0;
-  if constexpr (!P::kF64) s = run_family<P, DIR, 16>(t, sp, tw, N, s, __ldg(&sp->cnt[0]));
-  s = run_family<P, DIR, 8>(t, sp, tw, N, s, __ldg(&sp->cnt[1]));
-  s = run_family<P, DIR, 4>(t, sp, tw, N, s, __ldg(&sp->cnt[2]));
-  s = run_family<P, DIR, 2>(t, sp, tw, N, s, __ldg(&sp->cnt[3]));
-  s = run_family<P, DIR, 3>(t, sp, tw, N, s, __ldg(&sp->cnt[4]));
-  s = run_family<P, DIR, 5>(t, sp, tw, N, s, __ldg(&sp->cnt[5]));
+  if constexpr (!P::kF64) s = run_family<P, DIR, 16, E>(t, sp, tw, tw_base, N, s, __ldg(&sp->cnt[0]));
+  s = run_family<P, DIR, 8, E>(t, sp, tw, tw_base, N, s, __ldg(&sp->cnt[1]));
+  s = run_family<P, DIR, 4, E>(t, sp, tw, tw_base, N, s, __ldg(&sp->cnt[2]));
+  s = run_family<P, DIR, 2, E>(t, sp, tw, tw_base, N, s, __ldg(&sp->cnt[3]));
+  s = run_family<P, DIR, 3, E>(t, sp, tw, tw_base, N, s, __ldg(&sp->cnt[4]));
+  s = run_family<P, DIR, 5, E>(t, sp, tw, tw_base, N, s, __ldg(&sp->cnt[5]));
   const int nst = __ldg(&sp->nstages);
 #pragma unroll 1
   for (; s < nst; ++s)
-    stage_generic<P, DIR>(t, N, __ldg(&sp->radix[s]), __ldg(&sp->ns[s]), tw + __ldg(&sp->tw_off[s]),
-                          tw + __ldg(&sp->root_off[s]));
+    stage_generic<P, DIR>(t, N, __ldg(&sp->radix[s]), __ldg(&sp->ns[s]), tw + (__ldg(&sp->tw_off[s]) - tw_base),
+                          tw + (__ldg(&sp->root_off[s]) - tw_base));
 }
 
 }  // namespace p3g

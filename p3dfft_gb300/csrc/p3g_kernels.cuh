@@ -1,6 +1,7 @@
 // Kernel parameter blocks and launch entry points shared by the host plan.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "p3g_engine.cuh"
@@ -54,6 +55,17 @@ struct ChebyParams {
   float l_hi, l_lo;    // 4/Lz as double-float
 };
 
+template <class P>
+P3G_D typename P::C load_elem(const void* base, int user, long long idx) {
+  if (user) return P::from_uc(static_cast<const typename P::UC*>(base)[idx]);
+  return P::from_w(static_cast<const typename P::W*>(base)[idx]);
+}
+template <class P>
+P3G_D void store_elem(void* base, int user, long long idx, typename P::C v) {
+  if (user) static_cast<typename P::UC*>(base)[idx] = P::to_uc(v);
+  else static_cast<typename P::W*>(base)[idx] = P::to_w(v);
+}
+
 // Launchers (one per path).  Return the cudaError_t of the launch.
 template <class P>
 cudaError_t launch_x_r2c(const XParams& p, const StagePlan* sp, const float4* tw, int threads, size_t smem,
@@ -66,5 +78,18 @@ cudaError_t launch_strided(const SParams& p, const StagePlan* sp, const float4* 
                            size_t smem, int nfields, cudaStream_t st);
 template <class P>
 cudaError_t launch_cheby(const ChebyParams& p, int nfields, cudaStream_t st);
+
+// pipelined kernels (p3g_pipe.cuh)
+struct SPipeParams;
+struct XPipeParams;
+template <class P>
+cudaError_t launch_strided_pipe(const CUtensorMap* map, const SPipeParams& p, const StagePlan* sp, const float4* tw,
+                                bool forward_sign, int E, int threads, size_t smem, int grid, cudaStream_t st);
+template <class P>
+cudaError_t launch_xr2c_pipe(const XPipeParams& p, const StagePlan* sp, const float4* tw, int E, int threads,
+                             size_t smem, int grid, cudaStream_t st);
+template <class P>
+cudaError_t launch_xc2r_pipe(const XPipeParams& p, const StagePlan* sp, const float4* tw, int E, int threads,
+                             size_t smem, int grid, cudaStream_t st);
 
 }  // namespace p3g

@@ -1,7 +1,7 @@
 // Pass kernels, instantiated once per path by p3g_kernels_f64.cu / _f32.cu.
 #pragma once
 
-#include "p3g_kernels.cuh"
+#include "p3g_pipe.cuh"
 
 namespace p3g {
 
@@ -122,16 +122,6 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
 }
 
 // ------------------------------------------------------------- strided Y/Z
-template <class P>
-P3G_D typename P::C load_elem(const void* base, int user, long long idx) {
-  if (user) return P::from_uc(static_cast<const typename P::UC*>(base)[idx]);
-  return P::from_w(static_cast<const typename P::W*>(base)[idx]);
-}
-template <class P>
-P3G_D void store_elem(void* base, int user, long long idx, typename P::C v) {
-  if (user) static_cast<typename P::UC*>(base)[idx] = P::to_uc(v);
-  else static_cast<typename P::W*>(base)[idx] = P::to_w(v);
-}
 
 template <class P, int DIR>
 __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
@@ -263,6 +253,45 @@ cudaError_t launch_cheby(const ChebyParams& p, int nfields, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+template <class P>
+cudaError_t launch_strided_pipe(const CUtensorMap* map, const SPipeParams& p, const StagePlan* sp, const float4* tw,
+                                bool forward_sign, int E, int threads, size_t smem, int grid, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_strided_pipe<P, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_strided_pipe<P, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr = true;
+  }
+  (void)E;
+  if (forward_sign) k_strided_pipe<P, -1><<<grid, threads, smem, st>>>(*map, p, sp, tw);
+  else k_strided_pipe<P, 1><<<grid, threads, smem, st>>>(*map, p, sp, tw);
+  return cudaGetLastError();
+}
+template <class P>
+cudaError_t launch_xr2c_pipe(const XPipeParams& p, const StagePlan* sp, const float4* tw, int E, int threads,
+                             size_t smem, int grid, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_xr2c_pipe<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr = true;
+  }
+  (void)E;
+  k_xr2c_pipe<P><<<grid, threads, smem, st>>>(p, sp, tw);
+  return cudaGetLastError();
+}
+template <class P>
+cudaError_t launch_xc2r_pipe(const XPipeParams& p, const StagePlan* sp, const float4* tw, int E, int threads,
+                             size_t smem, int grid, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_xc2r_pipe<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr = true;
+  }
+  (void)E;
+  k_xc2r_pipe<P><<<grid, threads, smem, st>>>(p, sp, tw);
+  return cudaGetLastError();
+}
+
 #define P3G_INSTANTIATE(P)                                                                                          \
   template cudaError_t launch_x_r2c<P>(const XParams&, const StagePlan*, const float4*, int, size_t, int,          \
                                        cudaStream_t);                                                              \
@@ -270,6 +299,12 @@ cudaError_t launch_cheby(const ChebyParams& p, int nfields, cudaStream_t st) {
                                        cudaStream_t);                                                              \
   template cudaError_t launch_strided<P>(const SParams&, const StagePlan*, const float4*, bool, int, size_t, int,  \
                                          cudaStream_t);                                                            \
-  template cudaError_t launch_cheby<P>(const ChebyParams&, int, cudaStream_t);
+  template cudaError_t launch_cheby<P>(const ChebyParams&, int, cudaStream_t);                                     \
+  template cudaError_t launch_strided_pipe<P>(const CUtensorMap*, const SPipeParams&, const StagePlan*,             \
+                                              const float4*, bool, int, int, size_t, int, cudaStream_t);          \
+  template cudaError_t launch_xr2c_pipe<P>(const XPipeParams&, const StagePlan*, const float4*, int, int, size_t,  \
+                                           int, cudaStream_t);                                                     \
+  template cudaError_t launch_xc2r_pipe<P>(const XPipeParams&, const StagePlan*, const float4*, int, int, size_t,  \
+                                           int, cudaStream_t);
 
 }  // namespace p3g

@@ -1,0 +1,489 @@
+// Pipelined (persistent, double-buffered) pass kernels.
+//
+// One CTA per SM walks a strided list of tiles.  While it transforms tile i
+// in shared buffer b, the copy of tile i+1 into buffer b^1 is already in
+// flight (TMA tensor tiles or cp.async), so HBM traffic overlaps the
+// double-float butterflies.  Each tile goes through: a fix-up step in shared
+// memory (format conversion of user data, DCT-I/DST-I extension), the Stockham
+// stages of p3g_engine.cuh with the pass's twiddles held in shared memory for
+// the life of the CTA, and a store step with the pruning map and output
+// format conversion fused in.
+#pragma once
+
+#include "p3g_async.cuh"
+#include "p3g_kernels.cuh"
+
+namespace p3g {
+
+// ------------------------------------------------------------ parameters
+struct PipeCommon {
+  int ntiles;               // tiles over all fields
+  int tiles_per_field;
+  int tw_base, tw_count;    // this pass's slice of the twiddle table (float4)
+  int buf_elems;            // elements (W) per buffer
+  int* err;                 // device error flag
+};
+
+struct SPipeParams {
+  SParams s;
+  PipeCommon c;
+  int use_tma;              // 1: TMA tensor tiles, 0: cp.async
+  int brows, nbox;          // TMA: rows per box, boxes per tile
+  int box_bytes;
+  int chunk;                // cp.async bytes per element copy (16 or 8)
+};
+
+struct XPipeParams {
+  XParams x;
+  PipeCommon c;
+  int chunk;                // r2c: cp.async bytes per copy (4, 8 or 16)
+};
+
+// Hides a pointer's value from the optimiser.  The persistent loops below
+// re-derive their parameter block through it in every phase: otherwise the
+// compiler hoists the loads of all pass parameters out of the tile loop and
+// keeps them live across the FFT, which spills.
+template <class T>
+P3G_D T* opaque(T* p) {
+  asm volatile("" : "+l"(p));
+  return p;
+}
+
+P3G_D unsigned char* align1k(unsigned char* p) {
+  return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
+}
+
+// Tiles hold at most 4096 (F64) or 8192 (F32) elements, kElemsPerThread per
+// thread.
+template <class P>
+struct PipeLimits {
+  static constexpr int kMaxThreads = (P::kF64 ? 4096 : 8192) / kElemsPerThread;
+  // caps registers at 128 per thread: with a larger budget the scheduler
+  // hoists shared-memory loads across codelets and spills
+  static constexpr int kMinBlocks = 65536 / 128 / kMaxThreads;
+};
+
+// ------------------------------------------------------------ strided Y/Z
+template <class P>
+struct StridedSmem {
+  typename P::W* buf0;
+  float4* tw;
+  uint64_t* mbar;
+};
+template <class P>
+P3G_D StridedSmem<P> strided_smem(const PipeCommon& pc) {
+  extern __shared__ unsigned char p3g_pipe_smem[];
+  StridedSmem<P> r;
+  r.buf0 = reinterpret_cast<typename P::W*>(align1k(p3g_pipe_smem));
+  r.tw = reinterpret_cast<float4*>(r.buf0 + 2 * pc.buf_elems);
+  r.mbar = reinterpret_cast<uint64_t*>(r.tw + pc.tw_count);
+  return r;
+}
+
+P3G_D void strided_decode(const SPipeParams& q, int tile, int& xt, int& o1, int& o2) {
+  o2 = tile / q.c.tiles_per_field;
+  const int r = tile - o2 * q.c.tiles_per_field;
+  o1 = r / q.s.xtiles;
+  xt = r - o1 * q.s.xtiles;
+}
+
+// Copies of one tile into buffer b.  TMA: thread 0 arms the barrier and
+// issues the boxes.  cp.async: every thread, one commit group per call; the
+// DCT-I/DST-I extension rows are extra copies of the same elements (the
+// DST-I negation happens in the fix-up step).
+template <class P>
+P3G_D void strided_issue(const SPipeParams& q, const CUtensorMap* tin, int tile, int b) {
+  using W = typename P::W;
+  const StridedSmem<P> sm = strided_smem<P>(q.c);
+  W* dst = sm.buf0 + b * q.c.buf_elems;
+  const SParams& s = q.s;
+  const int M = s.M, L = s.L;
+  int xt, o1, o2;
+  strided_decode(q, tile, xt, o1, o2);
+  if (q.use_tma) {
+    if (threadIdx.x == 0) {
+      constexpr int kWords = sizeof(W) / 4;
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&sm.mbar[b], (uint32_t)(q.nbox * q.box_bytes));
+      for (int i = 0; i < q.nbox; ++i)
+        tma_load_4d(dst + i * q.brows * M, tin, &sm.mbar[b], xt * M * kWords, i * q.brows, o1, o2);
+    }
+    return;
+  }
+  const long long ib = (long long)o1 * s.in_o1 + (long long)o2 * s.in_o2 + (long long)xt * M;
+  const char* in = static_cast<const char*>(s.in);
+  constexpr int esz = (int)sizeof(W);
+  for (int e = threadIdx.x; e < M * L; e += blockDim.x) {
+    const int m = e & (M - 1);
+    const int j = e >> s.log2m;
+    const int src = j >= s.lmap_a1 ? j - s.lmap_d : (j < s.lmap_a0 ? j : -1);
+    const bool ok = src >= 0 && xt * M + m < s.X;
+    const char* g = ok ? in + (ib + m + src * s.in_axis) * esz : in;
+    const uint32_t nb = ok ? (uint32_t)esz : 0u;
+    int r0 = j, r1 = -1;
+    if (s.pre == 2) {
+      r0 = j + 1;
+      r1 = 2 * (L + 1) - (j + 1);
+    } else if (s.pre == 1 && j >= 1 && j <= L - 2) {
+      r1 = 2 * (L - 1) - j;
+    }
+    if constexpr (esz == 16) {
+      cp_async16(dst + r0 * M + m, g, nb);
+      if (r1 >= 0) cp_async16(dst + r1 * M + m, g, nb);
+      if (s.pre == 2 && j == 0) {  // rows 0 and L+1 of the odd extension are zero
+        cp_async16(dst + m, in, 0);
+        cp_async16(dst + (L + 1) * M + m, in, 0);
+      }
+    } else {
+      cp_async8(dst + r0 * M + m, g, nb);
+      if (r1 >= 0) cp_async8(dst + r1 * M + m, g, nb);
+      if (s.pre == 2 && j == 0) {
+        cp_async8(dst + m, in, 0);
+        cp_async8(dst + (L + 1) * M + m, in, 0);
+      }
+    }
+  }
+  cp_async_commit();
+}
+
+template <class P, int DIR>
+__global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMinBlocks)
+    k_strided_pipe(const __grid_constant__ CUtensorMap tin, const __grid_constant__ SPipeParams pp,
+                   const StagePlan* __restrict__ sp, const float4* __restrict__ tw_g) {
+  using W = typename P::W;
+  using C = typename P::C;
+  {
+    const StridedSmem<P> sm = strided_smem<P>(pp.c);
+    for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) sm.tw[i] = __ldg(tw_g + pp.c.tw_base + i);
+    if (threadIdx.x == 0 && pp.use_tma) {
+      mbar_init(&sm.mbar[0], 1);
+      mbar_init(&sm.mbar[1], 1);
+      mbar_fence_init();
+    }
+  }
+  __syncthreads();
+  int it = 0;
+  int tile = blockIdx.x;
+  bool next_pending = false;
+  if (tile < pp.c.ntiles) strided_issue<P>(*opaque(&pp), &tin, tile, 0);
+#pragma unroll 1
+  for (; tile < pp.c.ntiles; tile += gridDim.x, ++it) {
+    const int b = it & 1;
+    bool ok = true;
+    {
+      const SPipeParams& q = *opaque(&pp);
+      const int next = tile + gridDim.x;
+      next_pending = next < q.c.ntiles;
+      if (next_pending) strided_issue<P>(q, &tin, next, b ^ 1);
+      else if (!q.use_tma) cp_async_commit();  // one group per iteration
+      if (q.use_tma) ok = mbar_wait_bounded(&strided_smem<P>(q.c).mbar[b], (it >> 1) & 1, q.c.err);
+      else cp_async_wait<1>();
+    }
+    if (__syncthreads_or(!ok)) break;
+    {
+      // fix-up, element-wise in place: user format -> working format, DST-I
+      // negation, DCT-I mirror after a TMA load
+      const SPipeParams& q = *opaque(&pp);
+      const SParams& s = q.s;
+      const bool raw_user = s.in_user != 0;
+      if (raw_user || s.pre == 2 || (q.use_tma && s.pre == 1)) {
+        W* sm = strided_smem<P>(q.c).buf0 + b * q.c.buf_elems;
+        const int M = s.M, L = s.L;
+        const int rows = q.use_tma ? L : s.N;
+        for (int e = threadIdx.x; e < M * rows; e += blockDim.x) {
+          const int m = e & (M - 1);
+          const int j = e >> s.log2m;
+          C v = raw_user ? P::from_uc(reinterpret_cast<const typename P::UC*>(sm)[j * M + m]) : P::from_w(sm[j * M + m]);
+          if (s.pre == 2 && j >= L + 2) v = cneg(v);
+          const W w = P::to_w(v);
+          sm[j * M + m] = w;
+          if (q.use_tma && s.pre == 1 && j >= 1 && j <= L - 2) sm[(2 * (L - 1) - j) * M + m] = w;
+        }
+        __syncthreads();
+      }
+    }
+    {
+      const SPipeParams& q = *opaque(&pp);
+      const StridedSmem<P> sm = strided_smem<P>(q.c);
+      Tile<P> t{sm.buf0 + b * q.c.buf_elems, nullptr, q.s.M, q.s.log2m, 1, q.s.M};
+      cta_fft<P, DIR>(t, opaque(sp), sm.tw, q.c.tw_base);
+    }
+    {
+      const SPipeParams& q = *opaque(&pp);
+      const SParams& s = q.s;
+      const W* sm = strided_smem<P>(q.c).buf0 + b * q.c.buf_elems;
+      const int M = s.M;
+      int xt, o1, o2;
+      strided_decode(q, tile, xt, o1, o2);
+      const int x0 = xt * M;
+      const long long obase = (long long)o1 * s.out_o1 + (long long)o2 * s.out_o2 + x0;
+      for (int e = threadIdx.x; e < M * s.Lout; e += blockDim.x) {
+        const int m = e & (M - 1);
+        const int jo = e >> s.log2m;
+        if (x0 + m >= s.X) continue;
+        const int k = jo < s.smap_s0 ? jo : jo + s.smap_d;
+        C v;
+        if (s.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
+        else v = P::from_w(sm[k * M + m]);
+        store_elem<P>(s.out, s.out_user, obase + m + (long long)jo * s.out_axis, v);
+      }
+    }
+    __syncthreads();
+  }
+  // early exit after a timed-out wait: wait (bounded) for copies in flight
+  if (pp.use_tma) {
+    if (threadIdx.x == 0 && tile < pp.c.ntiles) {
+      const StridedSmem<P> sm = strided_smem<P>(pp.c);
+      mbar_wait_bounded(&sm.mbar[it & 1], (it >> 1) & 1, nullptr);
+      if (next_pending) mbar_wait_bounded(&sm.mbar[(it + 1) & 1], ((it + 1) >> 1) & 1, nullptr);
+    }
+  } else {
+    cp_async_wait<0>();
+  }
+}
+
+// ---------------------------------------------------------------- X passes
+template <class P>
+P3G_D typename P::W* xpipe_buf(const PipeCommon& pc, int b) {
+  extern __shared__ unsigned char p3g_pipe_smem[];
+  return reinterpret_cast<typename P::W*>(align1k(p3g_pipe_smem)) + b * pc.buf_elems;
+}
+template <class P>
+P3G_D float4* xpipe_tw(const PipeCommon& pc) {
+  return reinterpret_cast<float4*>(xpipe_buf<P>(pc, 2));
+}
+
+// r2c: real lines 2p, 2p+1 of the tile copied raw ([line][x])
+template <class P>
+P3G_D void xr2c_issue(const XPipeParams& q, int tile, int b) {
+  using UR = typename P::UR;
+  const XParams& x = q.x;
+  const int M = x.M, N = x.nx;
+  const int field = tile / q.c.tiles_per_field;
+  const int p0 = (tile - field * q.c.tiles_per_field) * M;
+  const char* in = reinterpret_cast<const char*>(static_cast<const UR*>(x.in) + field * x.in_field);
+  char* dst = reinterpret_cast<char*>(xpipe_buf<P>(q.c, b));
+  const int cpl = N * (int)sizeof(UR) / q.chunk;  // copies per line
+  for (int e = threadIdx.x; e < 2 * M * cpl; e += blockDim.x) {
+    const int lt = e / cpl;
+    const int c = e - lt * cpl;
+    const int line = 2 * p0 + lt;
+    const bool ok = line < x.nlines;
+    const char* g = ok ? in + (long long)line * x.in_line * (long long)sizeof(UR) + (long long)c * q.chunk : in;
+    char* d = dst + ((long long)lt * N * (long long)sizeof(UR) + (long long)c * q.chunk);
+    const uint32_t nb = ok ? (uint32_t)q.chunk : 0u;
+    if (q.chunk == 16) cp_async16(d, g, nb);
+    else if (q.chunk == 8) cp_async8(d, g, nb);
+    else cp_async4(d, g, nb);
+  }
+  cp_async_commit();
+}
+
+template <class P>
+__global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMinBlocks)
+    k_xr2c_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
+                const float4* __restrict__ tw_g) {
+  using W = typename P::W;
+  using C = typename P::C;
+  using UR = typename P::UR;
+  {
+    float4* tw_s = xpipe_tw<P>(pp.c);
+    for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) tw_s[i] = __ldg(tw_g + pp.c.tw_base + i);
+  }
+  __syncthreads();
+  constexpr int MAXI = kElemsPerThread;  // (pair, x) items per thread: M N / T <= E
+  int it = 0;
+  int tile = blockIdx.x;
+  if (tile < pp.c.ntiles) xr2c_issue<P>(*opaque(&pp), tile, 0);
+#pragma unroll 1
+  for (; tile < pp.c.ntiles; tile += gridDim.x, ++it) {
+    const int b = it & 1;
+    {
+      const XPipeParams& q = *opaque(&pp);
+      const int next = tile + gridDim.x;
+      if (next < q.c.ntiles) xr2c_issue<P>(q, next, b ^ 1);
+      else cp_async_commit();
+      cp_async_wait<1>();
+    }
+    __syncthreads();
+    {
+      // real lines 2p, 2p+1 -> complex line p (z = x1 + i x2): read all, then write
+      const XPipeParams& q = *opaque(&pp);
+      W* sm = xpipe_buf<P>(q.c, b);
+      const UR* raw = reinterpret_cast<const UR*>(sm);
+      const int MN = q.x.M * q.x.nx, N = q.x.nx;
+      C v[MAXI];
+#pragma unroll
+      for (int i = 0; i < MAXI; ++i) v[i] = P::zero();  // see stage_reg
+#pragma unroll
+      for (int i = 0; i < MAXI; ++i) {
+        const int e = threadIdx.x + i * blockDim.x;
+        if (e < MN) {
+          const int pr = e / N;
+          const int xi = e - pr * N;
+          v[i] = P::make(P::from_ur(raw[(2 * pr) * N + xi]), P::from_ur(raw[(2 * pr + 1) * N + xi]));
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < MAXI; ++i) {
+        const int e = threadIdx.x + i * blockDim.x;
+        if (e < MN) sm[e] = P::to_w(v[i]);
+      }
+    }
+    __syncthreads();
+    {
+      const XPipeParams& q = *opaque(&pp);
+      Tile<P> t{xpipe_buf<P>(q.c, b), nullptr, q.x.M, q.x.log2m, q.x.nx, 1};
+      cta_fft<P, -1>(t, opaque(sp), xpipe_tw<P>(q.c), q.c.tw_base);
+    }
+    {
+      // X1[k] = (Z[k] + conj Z[N-k]) / 2, X2[k] = -i (Z[k] - conj Z[N-k]) / 2
+      const XPipeParams& q = *opaque(&pp);
+      const XParams& x = q.x;
+      const W* sm = xpipe_buf<P>(q.c, b);
+      const int M = x.M, N = x.nx, nk = x.nkeep;
+      const int field = tile / q.c.tiles_per_field;
+      const int p0 = (tile - field * q.c.tiles_per_field) * M;
+      W* out = static_cast<W*>(x.out) + field * x.out_field;
+      for (int e = threadIdx.x; e < M * nk; e += blockDim.x) {
+        const int pr = e / nk;
+        const int k = e - pr * nk;
+        const int line = 2 * (p0 + pr);
+        if (line >= x.nlines) continue;
+        const C a = P::from_w(sm[pr * N + k]);
+        const C bb = cconj(P::from_w(sm[pr * N + (k == 0 ? 0 : N - k)]));
+        out[(long long)line * x.out_line + k] = P::to_w(cscale2(a + bb, 0.5f));
+        if (line + 1 < x.nlines)
+          out[(long long)(line + 1) * x.out_line + k] = P::to_w(cscale2(rot<-1>(a - bb), 0.5f));
+      }
+    }
+    __syncthreads();
+  }
+  cp_async_wait<0>();
+}
+
+// c2r: complex lines 2p, 2p+1 of nh = N/2+1 modes copied raw (pair stride 2 nh)
+template <class P>
+P3G_D void xc2r_issue(const XPipeParams& q, int tile, int b) {
+  using W = typename P::W;
+  const XParams& x = q.x;
+  const int M = x.M, nh = x.nx / 2 + 1;
+  const int field = tile / q.c.tiles_per_field;
+  const int p0 = (tile - field * q.c.tiles_per_field) * M;
+  const W* in = static_cast<const W*>(x.in) + field * x.in_field;
+  W* dst = xpipe_buf<P>(q.c, b);
+  for (int e = threadIdx.x; e < 2 * M * nh; e += blockDim.x) {
+    const int lt = e / nh;
+    const int k = e - lt * nh;
+    const int line = 2 * p0 + lt;
+    const bool ok = line < x.nlines && k < x.nkeep;
+    const W* g = ok ? in + (long long)line * x.in_line + k : in;
+    if constexpr (sizeof(W) == 16) cp_async16(dst + lt * nh + k, g, ok ? 16u : 0u);
+    else cp_async8(dst + lt * nh + k, g, ok ? 8u : 0u);
+  }
+  cp_async_commit();
+}
+
+template <class P>
+__global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMinBlocks)
+    k_xc2r_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
+                const float4* __restrict__ tw_g) {
+  using W = typename P::W;
+  using C = typename P::C;
+  using UR = typename P::UR;
+  {
+    float4* tw_s = xpipe_tw<P>(pp.c);
+    for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) tw_s[i] = __ldg(tw_g + pp.c.tw_base + i);
+  }
+  __syncthreads();
+  constexpr int MAXI = kElemsPerThread / 2 + 2;  // host guarantees T * MAXI >= M nh
+  int it = 0;
+  int tile = blockIdx.x;
+  if (tile < pp.c.ntiles) xc2r_issue<P>(*opaque(&pp), tile, 0);
+#pragma unroll 1
+  for (; tile < pp.c.ntiles; tile += gridDim.x, ++it) {
+    const int b = it & 1;
+    {
+      const XPipeParams& q = *opaque(&pp);
+      const int next = tile + gridDim.x;
+      if (next < q.c.ntiles) xc2r_issue<P>(q, next, b ^ 1);
+      else cp_async_commit();
+      cp_async_wait<1>();
+    }
+    __syncthreads();
+    {
+      // Hermitian extension into Z (in place, pair stride NP = 2 nh): read all, then write
+      const XPipeParams& q = *opaque(&pp);
+      W* sm = xpipe_buf<P>(q.c, b);
+      const int N = q.x.nx, nh = N / 2 + 1, NP = 2 * nh, Mnh = q.x.M * nh;
+      C z0[MAXI], z1[MAXI];
+      int ip[MAXI], ik[MAXI];
+#pragma unroll
+      for (int i = 0; i < MAXI; ++i) {  // see stage_reg
+        z0[i] = P::zero();
+        z1[i] = P::zero();
+        ik[i] = 0;
+      }
+#pragma unroll
+      for (int i = 0; i < MAXI; ++i) {
+        const int e = threadIdx.x + i * blockDim.x;
+        ip[i] = -1;
+        if (e < Mnh) {
+          const int pr = e / nh;
+          const int k = e - pr * nh;
+          C x1 = P::from_w(sm[pr * NP + k]);
+          C x2 = P::from_w(sm[pr * NP + nh + k]);
+          if (k == 0 || 2 * k == N) {
+            x1 = P::make(P::re(x1), P::re(P::zero()));
+            x2 = P::make(P::re(x2), P::re(P::zero()));
+          }
+          z0[i] = x1 + rot<1>(x2);
+          z1[i] = cconj(x1) + rot<1>(cconj(x2));
+          ip[i] = pr;
+          ik[i] = k;
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < MAXI; ++i) {
+        if (ip[i] >= 0) {
+          sm[ip[i] * NP + ik[i]] = P::to_w(z0[i]);
+          if (ik[i] > 0 && 2 * ik[i] < N) sm[ip[i] * NP + N - ik[i]] = P::to_w(z1[i]);
+        }
+      }
+    }
+    __syncthreads();
+    {
+      const XPipeParams& q = *opaque(&pp);
+      const int NP = 2 * (q.x.nx / 2 + 1);
+      Tile<P> t{xpipe_buf<P>(q.c, b), nullptr, q.x.M, q.x.log2m, NP, 1};
+      cta_fft<P, 1>(t, opaque(sp), xpipe_tw<P>(q.c), q.c.tw_base);
+    }
+    {
+      const XPipeParams& q = *opaque(&pp);
+      const XParams& x = q.x;
+      const W* sm = xpipe_buf<P>(q.c, b);
+      const int M = x.M, N = x.nx, NP = 2 * (N / 2 + 1);
+      const int field = tile / q.c.tiles_per_field;
+      const int p0 = (tile - field * q.c.tiles_per_field) * M;
+      UR* out = static_cast<UR*>(x.out) + field * x.out_field;
+      const float* smf = reinterpret_cast<const float*>(sm);
+      constexpr int kW = sizeof(W) / sizeof(float);
+      for (int e = threadIdx.x; e < 2 * M * N; e += blockDim.x) {
+        const int lt = e / N;
+        const int n = e - lt * N;
+        const int line = 2 * p0 + lt;
+        if (line >= x.nlines) continue;
+        const int c = lt & 1;
+        const float* f = smf + ((lt >> 1) * NP + n) * kW;
+        if constexpr (P::kF64) out[(long long)line * x.out_line + n] = P::to_ur(df{f[c], f[2 + c]});
+        else out[(long long)line * x.out_line + n] = f[c];
+      }
+    }
+    __syncthreads();
+  }
+  cp_async_wait<0>();
+}
+
+}  // namespace p3g

@@ -19,8 +19,13 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
+#include <cstdint>
+#include <cstdlib>
+
 #include "../../include/p3dfft_gb300.h"
-#include "p3g_kernels.cuh"
+#include "p3g_pipe.cuh"
 
 namespace p3g {
 
@@ -92,6 +97,7 @@ static bool factor(int n, bool allow16, std::vector<int>& radices) {
 
 struct HostTw {
   std::vector<float4> v;
+  int mark = 0;  // start of the axis being built
   int push_root(long long num, long long den) {  // exp(-2 pi i num/den), split into hi/lo
     const long double two_pi = 6.283185307179586476925286766559L;
     long long t = num % den;
@@ -110,10 +116,17 @@ struct AxisPlan {
   int M = 1, log2m = 0, threads = 32;
   size_t smem = 0;
   int sp_index = 0;  // index into the device StagePlan array
+  int tw_lo = 0, tw_cnt = 0;  // this axis's contiguous slice of the twiddle table
+  // pipelined kernels (p3g_pipe.cuh): same tile, double buffered
+  bool pipe_ok = false;
+  int pipe_threads = 0;
+  int buf_elems = 0;
+  size_t pipe_smem = 0;
 };
 
 static bool build_stages(int n, bool allow16, HostTw& tw, StagePlan& sp) {
   std::memset(&sp, 0, sizeof(sp));
+  tw.mark = (int)tw.v.size();
   sp.n = n;
   std::vector<int> rad;
   if (n > 1 && !factor(n, allow16, rad)) return false;
@@ -177,6 +190,40 @@ static bool size_tile(AxisPlan& ap, int n, int lines_avail, bool f64) {
   return ap.smem <= 227 * 1024;
 }
 
+// Pipelined kernels: two tile buffers (1 KB aligned), the axis's twiddles
+// and two mbarriers in shared memory.  kind: 0 strided, 1 r2c, 2 c2r.
+static void size_pipe(AxisPlan& ap, int kind, bool f64) {
+  ap.pipe_ok = false;
+  if (ap.sp.nstages < 1 || ap.sp.has_generic || ap.n < 2) return;
+  const size_t esize = f64 ? 16 : 8;
+  const int max_threads = f64 ? PipeLimits<PathF64>::kMaxThreads : PipeLimits<PathF32>::kMaxThreads;
+  const int n = ap.n;
+  const int nh = n / 2 + 1;
+  int M = ap.M;
+  for (;; M /= 2) {
+    int t = (M * n + kElemsPerThread - 1) / kElemsPerThread;
+    if (kind == 2) {
+      const int maxi = kElemsPerThread / 2 + 2;
+      const int t2 = (M * nh + maxi - 1) / maxi;
+      t = t > t2 ? t : t2;
+    }
+    t = (t + 31) / 32 * 32;
+    if (t < 32) t = 32;
+    if (t <= max_threads) {
+      ap.pipe_threads = t;
+      break;
+    }
+    if (M == 1) return;
+  }
+  if (M != ap.M) return;  // keep one tile shape per axis
+  // buffer stride rounded to 1 KB so both buffers (TMA destinations) stay aligned
+  const size_t need = (size_t)(kind == 2 ? M * 2 * nh : M * n) * esize;
+  const size_t buf_bytes = (need + 1023) / 1024 * 1024;
+  ap.buf_elems = (int)(buf_bytes / esize);
+  ap.pipe_smem = 1024 + 2 * buf_bytes + (size_t)ap.tw_cnt * 16 + 16;
+  ap.pipe_ok = ap.pipe_smem <= 227 * 1024;
+}
+
 struct TimerRec {
   int slot;
   cudaEvent_t a, b;
@@ -203,6 +250,9 @@ struct p3g_plan_s {
   std::vector<cudaEvent_t> free_events;
   long long launches = 0;
   std::mutex mu;
+  int sm_count = 0;
+  int* d_err = nullptr;  // set by a kernel whose bounded wait timed out
+  bool use_pipe = true, use_tma = true;
 
   size_t esize() const { return prec == P3G_F64 ? 16 : 8; }
 };
@@ -286,14 +336,156 @@ int op_index(char c, bool& forward_sign, bool natural_forward) {
   }
 }
 
+using EncodeTiledFn = PFN_cuTensorMapEncodeTiled_v12000;
+
+EncodeTiledFn tensor_map_encoder() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// Rows per TMA box: at most 256, boxes land back to back in the tile buffer
+// (128-byte aligned), and ceil(L / rows) * rows must fit in the buffer's
+// buf_rows rows (rows past L read as zeros through the tensor bounds).
+int pick_box_rows(int L, int buf_rows, int M, int esize) {
+  for (int b = L < 256 ? L : 256; b >= 1; --b) {
+    const long long rows = (long long)((L + b - 1) / b) * b;
+    if (rows > buf_rows) continue;
+    if (((long long)b * M * esize) % 128 != 0) continue;
+    return b;
+  }
+  return 0;
+}
+
+// 4-D map over (x words, axis rows, o1, o2) of a strided pass's source.
+bool encode_strided_map(CUtensorMap* m, const void* base, int esize, long long X, long long rows, long long o1n,
+                        long long o2n, long long s_axis, long long s_o1, long long s_o2, int M, int brows) {
+  EncodeTiledFn fn = tensor_map_encoder();
+  if (!fn || reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
+  const int w = esize / 4;
+  if ((long long)M * w > 256 || ((long long)M * esize) % 16 != 0) return false;
+  if (o2n == 1) s_o2 = ((s_o1 * o1n * esize + 15) / 16 * 16) / esize + (esize == 8 ? 0 : 0);
+  const cuuint64_t dims[4] = {(cuuint64_t)(X * w), (cuuint64_t)rows, (cuuint64_t)o1n, (cuuint64_t)o2n};
+  const cuuint64_t strides[3] = {(cuuint64_t)(s_axis * esize), (cuuint64_t)(s_o1 * esize),
+                                 (cuuint64_t)(s_o2 * esize)};
+  for (int i = 0; i < 3; ++i)
+    if (strides[i] % 16 != 0 || strides[i] >= (1ull << 40)) return false;
+  if (dims[0] >= (1ull << 32)) return false;
+  const cuuint32_t box[4] = {(cuuint32_t)(M * w), (cuuint32_t)brows, 1, 1};
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<void*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool aligned_to(const void* ptr, size_t a) { return reinterpret_cast<uintptr_t>(ptr) % a == 0; }
+
 template <class P>
 int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int nv, cudaStream_t st) {
   s.M = ap.M;
   s.log2m = ap.log2m;
   s.N = ap.n;
   s.xtiles = (s.X + ap.M - 1) / ap.M;
+  const int esize = (int)sizeof(typename P::W);
+  if (p->use_pipe && ap.pipe_ok && aligned_to(s.in, esize)) {
+    SPipeParams pp{};
+    pp.s = s;
+    pp.c.tiles_per_field = s.xtiles * s.O1;
+    pp.c.ntiles = pp.c.tiles_per_field * nv;
+    pp.c.tw_base = ap.tw_lo;
+    pp.c.tw_count = ap.tw_cnt;
+    pp.c.buf_elems = ap.buf_elems;
+    pp.c.err = p->d_err;
+    pp.chunk = esize;
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof(map));
+    if (p->use_tma && s.pre <= 1 && s.lmap_a0 >= s.L && s.lmap_a1 >= s.L) {
+      const int brows = pick_box_rows(s.L, ap.n, ap.M, esize);
+      if (brows > 0 && encode_strided_map(&map, s.in, esize, s.X, s.L, s.O1, nv, s.in_axis, s.in_o1, s.in_o2, ap.M,
+                                          brows)) {
+        pp.use_tma = 1;
+        pp.brows = brows;
+        pp.nbox = (s.L + brows - 1) / brows;
+        pp.box_bytes = brows * ap.M * esize;
+      }
+    }
+    const int grid = pp.c.ntiles < p->sm_count ? pp.c.ntiles : p->sm_count;
+    cudaError_t e = launch_strided_pipe<P>(&map, pp, p->d_sp + ap.sp_index, p->d_tw, fwd_sign, kElemsPerThread,
+                                           ap.pipe_threads, ap.pipe_smem, grid, st);
+    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("strided pass launch: ") + cudaGetErrorString(e));
+    p->launches++;
+    return P3G_OK;
+  }
   cudaError_t e = launch_strided<P>(s, p->d_sp + ap.sp_index, p->d_tw, fwd_sign, ap.threads, ap.smem, nv, st);
   if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("strided pass launch: ") + cudaGetErrorString(e));
+  p->launches++;
+  return P3G_OK;
+}
+
+template <class P>
+int run_x_r2c(p3g_plan p, XParams& x, int nv, cudaStream_t st) {
+  const AxisPlan& ap = p->ax_x;
+  using UR = typename P::UR;
+  if (p->use_pipe && ap.pipe_ok) {
+    const long long us = sizeof(UR);
+    int chunk = (int)us;
+    if ((x.nx * us) % 16 == 0 && (x.in_field * us) % 16 == 0 && aligned_to(x.in, 16)) chunk = 16;
+    else if ((x.nx * us) % 8 == 0 && (x.in_field * us) % 8 == 0 && aligned_to(x.in, 8)) chunk = 8;
+    XPipeParams xp{};
+    xp.x = x;
+    xp.chunk = chunk;
+    xp.c.tiles_per_field = x.tiles;
+    xp.c.ntiles = x.tiles * nv;
+    xp.c.tw_base = ap.tw_lo;
+    xp.c.tw_count = ap.tw_cnt;
+    xp.c.buf_elems = ap.buf_elems;
+    xp.c.err = p->d_err;
+    const int grid = xp.c.ntiles < p->sm_count ? xp.c.ntiles : p->sm_count;
+    cudaError_t e = launch_xr2c_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, kElemsPerThread, ap.pipe_threads,
+                                        ap.pipe_smem, grid, st);
+    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X r2c launch: ") + cudaGetErrorString(e));
+    p->launches++;
+    return P3G_OK;
+  }
+  cudaError_t e = launch_x_r2c<P>(x, p->d_sp + ap.sp_index, p->d_tw, ap.threads, ap.smem, nv, st);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X r2c launch: ") + cudaGetErrorString(e));
+  p->launches++;
+  return P3G_OK;
+}
+
+template <class P>
+int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st) {
+  const AxisPlan& ap = p->ax_x;
+  if (p->use_pipe && ap.pipe_ok) {
+    XPipeParams xp{};
+    xp.x = x;
+    xp.chunk = (int)sizeof(typename P::W);
+    xp.c.tiles_per_field = x.tiles;
+    xp.c.ntiles = x.tiles * nv;
+    xp.c.tw_base = ap.tw_lo;
+    xp.c.tw_count = ap.tw_cnt;
+    xp.c.buf_elems = ap.buf_elems;
+    xp.c.err = p->d_err;
+    const int grid = xp.c.ntiles < p->sm_count ? xp.c.ntiles : p->sm_count;
+    cudaError_t e = launch_xc2r_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, kElemsPerThread, ap.pipe_threads,
+                                        ap.pipe_smem, grid, st);
+    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X c2r launch: ") + cudaGetErrorString(e));
+    p->launches++;
+    return P3G_OK;
+  }
+  cudaError_t e = launch_x_c2r<P>(x, p->d_sp + ap.sp_index, p->d_tw, ap.threads, ap.smem, nv, st);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X c2r launch: ") + cudaGetErrorString(e));
   p->launches++;
   return P3G_OK;
 }
@@ -329,9 +521,8 @@ int do_ftran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
     x.M = p->ax_x.M;
     x.log2m = p->ax_x.log2m;
     x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
-    cudaError_t e = launch_x_r2c<P>(x, p->d_sp + p->ax_x.sp_index, p->d_tw, p->ax_x.threads, p->ax_x.smem, nv, st);
-    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X r2c launch: ") + cudaGetErrorString(e));
-    p->launches++;
+    rc = run_x_r2c<P>(p, x, nv, st);
+    if (rc) return rc;
     tm.done();
   }
   // Y c2c: wa -> ybuf, keeping y modes 0..nycph-1 and the top nyc-nycph (seg_copy_y, ftran.F90:736-738)
@@ -482,9 +673,8 @@ int do_btran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
     x.M = p->ax_x.M;
     x.log2m = p->ax_x.log2m;
     x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
-    cudaError_t e = launch_x_c2r<P>(x, p->d_sp + p->ax_x.sp_index, p->d_tw, p->ax_x.threads, p->ax_x.smem, nv, st);
-    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X c2r launch: ") + cudaGetErrorString(e));
-    p->launches++;
+    rc = run_x_c2r<P>(p, x, nv, st);
+    if (rc) return rc;
     tm.done();
   }
   return P3G_OK;
@@ -543,6 +733,8 @@ int p3g_plan_create(p3g_plan* out, int nx, int ny, int nz, int nxc, int nyc, int
   std::vector<StagePlan> sps;
   auto add_axis = [&](AxisPlan& ap, int n, int lines) -> bool {
     if (!build_stages(n, !f64, tw, ap.sp)) return false;
+    ap.tw_lo = tw.mark;
+    ap.tw_cnt = (int)tw.v.size() - tw.mark;
     if (!size_tile(ap, n, lines, f64)) return false;
     ap.sp_index = (int)sps.size();
     sps.push_back(ap.sp);
@@ -565,10 +757,37 @@ int p3g_plan_create(p3g_plan* out, int nx, int ny, int nz, int nxc, int nyc, int
     if (!size_tile(p->ax_z[3], nz, p->nxhpc, f64)) p->z_ok[3] = false;
   }
   if (!p->z_ok[0] && !p->z_ok[1] && !p->z_ok[3]) return bad("z length " + std::to_string(nz) + " is too long");
+  size_pipe(p->ax_x, 1, f64);  // r2c and c2r share the tile; c2r needs the larger buffer
+  {
+    AxisPlan c2r = p->ax_x;
+    size_pipe(c2r, 2, f64);
+    if (!c2r.pipe_ok || c2r.pipe_threads != p->ax_x.pipe_threads) p->ax_x.pipe_ok = false;
+    p->ax_x.buf_elems = c2r.buf_elems;
+    p->ax_x.pipe_smem = c2r.pipe_smem;
+  }
+  size_pipe(p->ax_y, 0, f64);
+  for (int i = 0; i < 4; ++i)
+    if (p->z_ok[i]) size_pipe(p->ax_z[i], 0, f64);
+  {
+    const char* e = std::getenv("P3G_NO_PIPE");
+    p->use_pipe = !(e && *e && *e != '0');
+    e = std::getenv("P3G_NO_TMA");
+    p->use_tma = !(e && *e && *e != '0');
+  }
+  if (cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, 0) != cudaSuccess) {
+    cudaGetLastError();
+    p->sm_count = 132;
+  }
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  }
 
   p->tw_bytes = tw.v.size() * sizeof(float4);
   if (cudaMalloc(&p->d_tw, p->tw_bytes) != cudaSuccess ||
-      cudaMalloc(&p->d_sp, sps.size() * sizeof(StagePlan)) != cudaSuccess) {
+      cudaMalloc(&p->d_sp, sps.size() * sizeof(StagePlan)) != cudaSuccess ||
+      cudaMalloc(&p->d_err, sizeof(int)) != cudaSuccess || cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     if (p->d_tw) cudaFree(p->d_tw);
     delete p;
@@ -597,6 +816,7 @@ int p3g_plan_destroy(p3g_plan p) {
   if (p->wb) cudaFree(p->wb);
   if (p->d_tw) cudaFree(p->d_tw);
   if (p->d_sp) cudaFree(p->d_sp);
+  if (p->d_err) cudaFree(p->d_err);
   delete p;
   return P3G_OK;
 }
@@ -739,5 +959,21 @@ long long p3g_plan_device_bytes(p3g_plan p) {
 }
 
 long long p3g_plan_launches(p3g_plan p) { return p ? p->launches : 0; }
+
+int p3g_plan_status(p3g_plan p) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  int flag = 0;
+  if (cudaMemcpy(&flag, p->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(P3G_E_CUDA, std::string("status read: ") + cudaGetErrorString(cudaGetLastError()));
+  if (flag) return fail(P3G_E_CUDA, "a pipelined pass timed out waiting for its tile copy (results invalid)");
+  return P3G_OK;
+}
+
+int p3g_plan_set_options(p3g_plan p, int use_pipe, int use_tma) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  p->use_pipe = use_pipe != 0;
+  p->use_tma = use_tma != 0;
+  return P3G_OK;
+}
 
 }  // extern "C"

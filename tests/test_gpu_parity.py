@@ -33,11 +33,15 @@ def _spectrum(shape, seed):
     return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
 
 
-def _run_pair(torch, plan_args, a, op_f, op_b, precision, seed=0):
+MODES = {"pipe_tma": (True, True), "pipe_cpasync": (True, False), "single_tile": (False, False)}
+
+
+def _run_pair(torch, plan_args, a, op_f, op_b, precision, seed=0, mode="pipe_tma"):
     import p3dfft_gb300 as pg
     nx, ny, nz = plan_args[:3]
     pruned = plan_args[3:] if len(plan_args) > 3 else (nx, ny, nz)
     plan = pg.Plan(nx, ny, nz, *pruned, precision=precision)
+    plan.set_options(*MODES[mode])
     ref = orc.OraclePlan(nx, ny, nz, *pruned)
     rdt = torch.float64 if precision == pg.F64 else torch.float32
     x = torch.from_numpy(a).to("cuda", rdt)
@@ -48,6 +52,7 @@ def _run_pair(torch, plan_args, a, op_f, op_b, precision, seed=0):
     r = plan.btran_c2r(torch.from_numpy(c_in).to("cuda", cdt), op=op_b)
     want_r = ref.btran_c2r(c_in, op_b)
     torch.cuda.synchronize()
+    plan.check()
     got_b = b.cpu().numpy().astype(np.complex128)
     got_r = r.cpu().numpy().astype(np.float64)
     plan.close()
@@ -95,6 +100,26 @@ def test_f64_pruned_parity(torch_cuda, args):
     gb, wb, gr, wr = _run_pair(torch_cuda, args, a, "fft", "tff", pg.F64)
     assert orc.normalised_linf(gb, wb) <= F64_TOL
     assert orc.normalised_linf(gr, wr) <= F64_TOL
+
+
+@pytest.mark.parametrize("mode", sorted(MODES))
+@pytest.mark.parametrize("case", [((64, 48, 40), "fft", "tff", 0), ((32, 24, 33), "ffc", "cff", 0),
+                                  ((16, 12, 10), "ffs", "sff", 0), ((64, 64, 64, 32, 32, 32), "fft", "tff", 0),
+                                  ((96, 80, 60), "fft", "tff", 1), ((30, 18, 17), "ffc", "cff", 1),
+                                  ((33, 20, 16, 20, 9, 10), "fft", "tff", 1)])
+def test_kernel_paths_agree(torch_cuda, mode, case):
+    # every kernel family (pipelined TMA, pipelined cp.async, single-tile) on
+    # the same cases, F64 (last field 0) and F32 (1)
+    import p3dfft_gb300 as pg
+    args, op_f, op_b, f32 = case
+    a = _rand(args[:3][::-1], 17)
+    gb, wb, gr, wr = _run_pair(torch_cuda, args, a, op_f, op_b, pg.F32 if f32 else pg.F64, mode=mode)
+    if f32:
+        assert orc.relative_l2(gb, wb) <= F32_TOL
+        assert orc.relative_l2(gr, wr) <= F32_TOL
+    else:
+        assert orc.normalised_linf(gb, wb) <= F64_TOL
+        assert orc.normalised_linf(gr, wr) <= F64_TOL
 
 
 @pytest.mark.parametrize("shape", [(32, 32, 32), (14, 26, 38), (120, 160, 192), (128, 128, 128)])
