@@ -157,41 +157,50 @@ __device__ __noinline__ void stage_generic(const Tile<P>& t, int N, int p, int n
   __syncthreads();
 }
 
+// Stage s of radix R reads its twiddles at tw_off(s) and has sub-transform
+// length ns(s) = product of the radices before it; both follow from the
+// family counts, so they are carried in registers instead of being loaded
+// per stage (stage 0 owns one placeholder twiddle, see build_stages).
 template <class P, int DIR, int R, int E>
-__device__ __forceinline__ int run_family(const Tile<P>& t, const StagePlan* __restrict__ sp,
-                                          const float4* __restrict__ tw, int tw_base, int N, int s, int cnt) {
+__device__ __forceinline__ void run_family(const Tile<P>& t, const float4* __restrict__ tw, int N, int cnt, int& ns,
+                                           int& off) {
 #pragma unroll 1
-  for (int c = 0; c < cnt; ++c, ++s)
-    stage_reg<P, DIR, R, E>(t, N, __ldg(&sp->ns[s]), tw + (__ldg(&sp->tw_off[s]) - tw_base));
-  return s;
+  for (int c = 0; c < cnt; ++c) {
+    stage_reg<P, DIR, R, E>(t, N, ns, tw + off);
+    off += ns > 1 ? ns * (R - 1) : 1;
+    ns *= R;
+  }
 }
 
 // Runs all stages of the plan on the tile (sm must be filled and
 // synchronised).  The plan orders its stages by radix family (16, 8, 4, 2, 3,
 // 5, then generic primes) and each family runs in its own loop: a single loop
 // with a switch over the radix makes the register allocator keep the live
-// ranges of every codelet at once and spill.  The stage plan lives in device
-// memory, read with uniform cached loads.  Radix 16 is compiled only for the
-// F32 path (the F64 codelet needs ~200 registers; radix 8 has the same
+// ranges of every codelet at once and spill.  Radix 16 is compiled only for
+// the F32 path (the F64 codelet needs ~200 registers; radix 8 has the same
 // double-float operation count per point for the sizes used here).
 // tw points at the twiddle table entry tw_base (the full table with
-// tw_base = 0, or a pass's slice copied to shared memory).
-// E = elements each thread holds per stage; the launch uses
-// ceil(M N / E) threads.
+// tw_base = 0, or a pass's slice copied to shared memory).  E = elements each
+// thread holds per stage; the launch uses ceil(M N / E) threads.
 template <class P, int DIR, int E = kElemsPerThread>
 __device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __restrict__ sp,
                                         const float4* __restrict__ tw, int tw_base = 0) {
   const int N = __ldg(&sp->n);
-  int s = 0;
-  if constexpr (!P::kF64) s = run_family<P, DIR, 16, E>(t, sp, tw, tw_base, N, s, __ldg(&sp->cnt[0]));
-  s = run_family<P, DIR, 8, E>(t, sp, tw, tw_base, N, s, __ldg(&sp->cnt[1]));
-  s = run_family<P, DIR, 4, E>(t, sp, tw, tw_base, N, s, __ldg(&sp->cnt[2]));
-  s = run_family<P, DIR, 2, E>(t, sp, tw, tw_base, N, s, __ldg(&sp->cnt[3]));
-  s = run_family<P, DIR, 3, E>(t, sp, tw, tw_base, N, s, __ldg(&sp->cnt[4]));
-  s = run_family<P, DIR, 5, E>(t, sp, tw, tw_base, N, s, __ldg(&sp->cnt[5]));
+  int c[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) c[i] = __ldg(&sp->cnt[i]);
   const int nst = __ldg(&sp->nstages);
+  int ns = 1;
+  int off = __ldg(&sp->tw_off[0]) - tw_base;
+  if constexpr (!P::kF64) run_family<P, DIR, 16, E>(t, tw, N, c[0], ns, off);
+  run_family<P, DIR, 8, E>(t, tw, N, c[1], ns, off);
+  run_family<P, DIR, 4, E>(t, tw, N, c[2], ns, off);
+  run_family<P, DIR, 2, E>(t, tw, N, c[3], ns, off);
+  run_family<P, DIR, 3, E>(t, tw, N, c[4], ns, off);
+  run_family<P, DIR, 5, E>(t, tw, N, c[5], ns, off);
+  const int sg = c[0] + c[1] + c[2] + c[3] + c[4] + c[5];
 #pragma unroll 1
-  for (; s < nst; ++s)
+  for (int s = sg; s < nst; ++s)
     stage_generic<P, DIR>(t, N, __ldg(&sp->radix[s]), __ldg(&sp->ns[s]), tw + (__ldg(&sp->tw_off[s]) - tw_base),
                           tw + (__ldg(&sp->root_off[s]) - tw_base));
 }

@@ -53,11 +53,13 @@ P3G_D unsigned char* align1k(unsigned char* p) {
   return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
 }
 
-// Tiles hold at most 4096 (F64) or 8192 (F32) elements, kElemsPerThread per
-// thread.
+// Tiles hold at most 4096 (F64) or 8192 (F32) elements; a thread holds
+// kE of them per stage (8 on the F64 path: 512 threads, 16 warps per SM to
+// hide the latency of the dependent double-float chains; 16 on F32).
 template <class P>
 struct PipeLimits {
-  static constexpr int kMaxThreads = (P::kF64 ? 4096 : 8192) / kElemsPerThread;
+  static constexpr int kE = P::kF64 ? 8 : 16;
+  static constexpr int kMaxThreads = (P::kF64 ? 4096 : 8192) / kE;
   // caps registers at 128 per thread: with a larger budget the scheduler
   // hoists shared-memory loads across codelets and spills
   static constexpr int kMinBlocks = 65536 / 128 / kMaxThreads;
@@ -165,13 +167,13 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
   int it = 0;
   int tile = blockIdx.x;
   bool next_pending = false;
-  if (tile < pp.c.ntiles) strided_issue<P>(*opaque(&pp), &tin, tile, 0);
+  if (tile < pp.c.ntiles) strided_issue<P>(pp, &tin, tile, 0);
 #pragma unroll 1
   for (; tile < pp.c.ntiles; tile += gridDim.x, ++it) {
     const int b = it & 1;
     bool ok = true;
     {
-      const SPipeParams& q = *opaque(&pp);
+      const SPipeParams& q = pp;
       const int next = tile + gridDim.x;
       next_pending = next < q.c.ntiles;
       if (next_pending) strided_issue<P>(q, &tin, next, b ^ 1);
@@ -183,7 +185,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
     {
       // fix-up, element-wise in place: user format -> working format, DST-I
       // negation, DCT-I mirror after a TMA load
-      const SPipeParams& q = *opaque(&pp);
+      const SPipeParams& q = pp;
       const SParams& s = q.s;
       const bool raw_user = s.in_user != 0;
       if (raw_user || s.pre == 2 || (q.use_tma && s.pre == 1)) {
@@ -203,13 +205,13 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       }
     }
     {
-      const SPipeParams& q = *opaque(&pp);
+      const SPipeParams& q = pp;
       const StridedSmem<P> sm = strided_smem<P>(q.c);
       Tile<P> t{sm.buf0 + b * q.c.buf_elems, nullptr, q.s.M, q.s.log2m, 1, q.s.M};
-      cta_fft<P, DIR>(t, opaque(sp), sm.tw, q.c.tw_base);
+      cta_fft<P, DIR, PipeLimits<P>::kE>(t, sp, sm.tw, q.c.tw_base);
     }
     {
-      const SPipeParams& q = *opaque(&pp);
+      const SPipeParams& q = pp;
       const SParams& s = q.s;
       const W* sm = strided_smem<P>(q.c).buf0 + b * q.c.buf_elems;
       const int M = s.M;
@@ -291,15 +293,15 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
     for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) tw_s[i] = __ldg(tw_g + pp.c.tw_base + i);
   }
   __syncthreads();
-  constexpr int MAXI = kElemsPerThread;  // (pair, x) items per thread: M N / T <= E
+  constexpr int MAXI = PipeLimits<P>::kE;  // (pair, x) items per thread: M N / T <= E
   int it = 0;
   int tile = blockIdx.x;
-  if (tile < pp.c.ntiles) xr2c_issue<P>(*opaque(&pp), tile, 0);
+  if (tile < pp.c.ntiles) xr2c_issue<P>(pp, tile, 0);
 #pragma unroll 1
   for (; tile < pp.c.ntiles; tile += gridDim.x, ++it) {
     const int b = it & 1;
     {
-      const XPipeParams& q = *opaque(&pp);
+      const XPipeParams& q = pp;
       const int next = tile + gridDim.x;
       if (next < q.c.ntiles) xr2c_issue<P>(q, next, b ^ 1);
       else cp_async_commit();
@@ -308,7 +310,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
     __syncthreads();
     {
       // real lines 2p, 2p+1 -> complex line p (z = x1 + i x2): read all, then write
-      const XPipeParams& q = *opaque(&pp);
+      const XPipeParams& q = pp;
       W* sm = xpipe_buf<P>(q.c, b);
       const UR* raw = reinterpret_cast<const UR*>(sm);
       const int MN = q.x.M * q.x.nx, N = q.x.nx;
@@ -333,13 +335,13 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
     }
     __syncthreads();
     {
-      const XPipeParams& q = *opaque(&pp);
+      const XPipeParams& q = pp;
       Tile<P> t{xpipe_buf<P>(q.c, b), nullptr, q.x.M, q.x.log2m, q.x.nx, 1};
-      cta_fft<P, -1>(t, opaque(sp), xpipe_tw<P>(q.c), q.c.tw_base);
+      cta_fft<P, -1, PipeLimits<P>::kE>(t, sp, xpipe_tw<P>(q.c), q.c.tw_base);
     }
     {
       // X1[k] = (Z[k] + conj Z[N-k]) / 2, X2[k] = -i (Z[k] - conj Z[N-k]) / 2
-      const XPipeParams& q = *opaque(&pp);
+      const XPipeParams& q = pp;
       const XParams& x = q.x;
       const W* sm = xpipe_buf<P>(q.c, b);
       const int M = x.M, N = x.nx, nk = x.nkeep;
@@ -397,15 +399,15 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
     for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) tw_s[i] = __ldg(tw_g + pp.c.tw_base + i);
   }
   __syncthreads();
-  constexpr int MAXI = kElemsPerThread / 2 + 2;  // host guarantees T * MAXI >= M nh
+  constexpr int MAXI = PipeLimits<P>::kE / 2 + 2;  // host guarantees T * MAXI >= M nh
   int it = 0;
   int tile = blockIdx.x;
-  if (tile < pp.c.ntiles) xc2r_issue<P>(*opaque(&pp), tile, 0);
+  if (tile < pp.c.ntiles) xc2r_issue<P>(pp, tile, 0);
 #pragma unroll 1
   for (; tile < pp.c.ntiles; tile += gridDim.x, ++it) {
     const int b = it & 1;
     {
-      const XPipeParams& q = *opaque(&pp);
+      const XPipeParams& q = pp;
       const int next = tile + gridDim.x;
       if (next < q.c.ntiles) xc2r_issue<P>(q, next, b ^ 1);
       else cp_async_commit();
@@ -414,7 +416,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
     __syncthreads();
     {
       // Hermitian extension into Z (in place, pair stride NP = 2 nh): read all, then write
-      const XPipeParams& q = *opaque(&pp);
+      const XPipeParams& q = pp;
       W* sm = xpipe_buf<P>(q.c, b);
       const int N = q.x.nx, nh = N / 2 + 1, NP = 2 * nh, Mnh = q.x.M * nh;
       C z0[MAXI], z1[MAXI];
@@ -455,13 +457,13 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
     }
     __syncthreads();
     {
-      const XPipeParams& q = *opaque(&pp);
+      const XPipeParams& q = pp;
       const int NP = 2 * (q.x.nx / 2 + 1);
       Tile<P> t{xpipe_buf<P>(q.c, b), nullptr, q.x.M, q.x.log2m, NP, 1};
-      cta_fft<P, 1>(t, opaque(sp), xpipe_tw<P>(q.c), q.c.tw_base);
+      cta_fft<P, 1, PipeLimits<P>::kE>(t, sp, xpipe_tw<P>(q.c), q.c.tw_base);
     }
     {
-      const XPipeParams& q = *opaque(&pp);
+      const XPipeParams& q = pp;
       const XParams& x = q.x;
       const W* sm = xpipe_buf<P>(q.c, b);
       const int M = x.M, N = x.nx, NP = 2 * (N / 2 + 1);

@@ -197,13 +197,14 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   if (ap.sp.nstages < 1 || ap.sp.has_generic || ap.n < 2) return;
   const size_t esize = f64 ? 16 : 8;
   const int max_threads = f64 ? PipeLimits<PathF64>::kMaxThreads : PipeLimits<PathF32>::kMaxThreads;
+  const int E = f64 ? PipeLimits<PathF64>::kE : PipeLimits<PathF32>::kE;
   const int n = ap.n;
   const int nh = n / 2 + 1;
   int M = ap.M;
   for (;; M /= 2) {
-    int t = (M * n + kElemsPerThread - 1) / kElemsPerThread;
+    int t = (M * n + E - 1) / E;
     if (kind == 2) {
-      const int maxi = kElemsPerThread / 2 + 2;
+      const int maxi = E / 2 + 2;
       const int t2 = (M * nh + maxi - 1) / maxi;
       t = t > t2 ? t : t2;
     }
