@@ -43,12 +43,53 @@ P3G_D cdf load_tw(const float4* __restrict__ tw, int idx) {
   return cdf{df{v.x, v.z}, df{v.y, v.w}};
 }
 
+// Division by a runtime divisor d <= 2^15 for dividends x < 2^15 with one
+// multiply-high: q = floor(2x * ceil(2^31/d) / 2^32).  Exact because the
+// magic's excess over 2^31/d is below 1/d and x < 2^15 (the error term stays
+// under 1/d).  Tiles hold at most 2^14 elements, so every index fits.
+// Powers of two use a shift (m == 0).
+struct FastDiv {
+  uint32_t d, m, sh;
+  P3G_D explicit FastDiv(uint32_t dd) : d(dd), m(0), sh(0) {
+    if ((dd & (dd - 1)) == 0) sh = (uint32_t)(__ffs((int)dd) - 1);
+    else m = 0x7FFFFFFFu / dd + 1;  // ceil(2^31 / d)
+  }
+  P3G_D uint32_t div(uint32_t x) const { return m ? __umulhi(x << 1, m) : (x >> sh); }
+  P3G_D void divmod(uint32_t x, uint32_t& q, uint32_t& r) const {
+    q = div(x);
+    r = x - q * d;
+  }
+};
+
+// Shared-memory element access through 32-bit shared addresses (ld/st.shared)
+// rather than generic pointers.
+P3G_D float4 lds(uint32_t a, float4*) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];\n" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+  return v;
+}
+P3G_D float2 lds(uint32_t a, float2*) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];\n" : "=f"(v.x), "=f"(v.y) : "r"(a));
+  return v;
+}
+P3G_D void sts(uint32_t a, float4 v) {
+  asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};\n" ::"r"(a), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+               : "memory");
+}
+P3G_D void sts(uint32_t a, float2 v) {
+  asm volatile("st.shared.v2.f32 [%0], {%1, %2};\n" ::"r"(a), "f"(v.x), "f"(v.y) : "memory");
+}
+
 template <class P>
 struct Tile {
   typename P::W* sm;       // M lines x N points
   typename P::W* scratch;  // same size, generic stages only
   int M, log2m, LS, JS;
   P3G_D int addr(int line, int j) const { return line * LS + j * JS; }
+  P3G_D uint32_t saddr(int line, int j) const {
+    return (uint32_t)__cvta_generic_to_shared(sm) + (uint32_t)((line * LS + j * JS) * (int)sizeof(typename P::W));
+  }
   // butterfly b -> (line, j) over M lines x (N / R) butterflies per line
   P3G_D void decode(int b, int per_line, int& line, int& j) const {
     if (LS == 1) {  // point-major: line fastest
@@ -57,6 +98,17 @@ struct Tile {
     } else {
       line = b / per_line;
       j = b - line * per_line;
+    }
+  }
+  P3G_D void decode(int b, const FastDiv& per_line, int& line, int& j) const {
+    if (LS == 1) {
+      line = b & (M - 1);
+      j = b >> log2m;
+    } else {
+      uint32_t q, r;
+      per_line.divmod((uint32_t)b, q, r);
+      line = (int)q;
+      j = (int)r;
     }
   }
 };
@@ -72,48 +124,54 @@ P3G_D void cta_barrier() {
 template <class P, int DIR, int R, int E = kElemsPerThread>
 __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const float4* __restrict__ tw) {
   using C = typename P::C;
+  using W = typename P::W;
   constexpr int MAXB = (E + R - 1) / R;
   const int per_line = N / R;
+  const FastDiv fd_line((uint32_t)per_line), fd_ns((uint32_t)ns);
   const int nb = t.M * per_line;
   const int T = blockDim.x;
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(t.sm);
+  const uint32_t jstride = (uint32_t)(t.JS * (int)sizeof(W)) * (uint32_t)per_line;  // bytes between inputs q, q+1
+  const uint32_t ostride = (uint32_t)(t.JS * (int)sizeof(W)) * (uint32_t)ns;        // bytes between outputs
   // Explicitly initialised: the arrays are written and read under correlated
   // guards (b < nb) the compiler cannot prove, and inside a persistent tile
   // loop an uninitialised element would otherwise be kept live around the
   // loop, with every codelet's registers.
   C v[MAXB][R];
-  int oline[MAXB], obase[MAXB];
+  uint32_t oaddr[MAXB];
+  bool live[MAXB];
 #pragma unroll
   for (int i = 0; i < MAXB; ++i) {
-    obase[i] = 0;
+    oaddr[i] = 0;
 #pragma unroll
     for (int q = 0; q < R; ++q) v[i][q] = P::zero();
   }
 #pragma unroll
   for (int i = 0; i < MAXB; ++i) {
     const int b = threadIdx.x + i * T;
-    oline[i] = -1;
-    if (b < nb) {
+    live[i] = b < nb;
+    if (live[i]) {
       int line, j;
-      t.decode(b, per_line, line, j);
+      t.decode(b, fd_line, line, j);
+      const uint32_t ia = sbase + (uint32_t)(t.addr(line, j) * (int)sizeof(W));
 #pragma unroll
-      for (int q = 0; q < R; ++q) v[i][q] = P::from_w(t.sm[t.addr(line, j + q * per_line)]);
-      const int k = j % ns;
+      for (int q = 0; q < R; ++q) v[i][q] = P::from_w(lds(ia + q * jstride, (W*)nullptr));
+      const int k = (int)(j - fd_ns.div((uint32_t)j) * (uint32_t)ns);
       if (ns > 1) {
         const float4* twp = tw + k * (R - 1) - 1;
 #pragma unroll
         for (int q = 1; q < R; ++q) v[i][q] = cmul<(DIR > 0)>(v[i][q], load_tw(twp, q));
       }
       dft<R, DIR>(v[i]);
-      oline[i] = line;
-      obase[i] = (j - k) * R + k;
+      oaddr[i] = sbase + (uint32_t)(t.addr(line, (j - k) * R + k) * (int)sizeof(W));
     }
   }
   cta_barrier<(R == 16 ? 1 : R)>();
 #pragma unroll
   for (int i = 0; i < MAXB; ++i) {
-    if (oline[i] >= 0) {
+    if (live[i]) {
 #pragma unroll
-      for (int q = 0; q < R; ++q) t.sm[t.addr(oline[i], obase[i] + q * ns)] = P::to_w(v[i][q]);
+      for (int q = 0; q < R; ++q) sts(oaddr[i] + q * ostride, P::to_w(v[i][q]));
     }
   }
   cta_barrier<(R == 16 ? 1 : R)>();

@@ -266,8 +266,9 @@ P3G_D void xr2c_issue(const XPipeParams& q, int tile, int b) {
   const char* in = reinterpret_cast<const char*>(static_cast<const UR*>(x.in) + field * x.in_field);
   char* dst = reinterpret_cast<char*>(xpipe_buf<P>(q.c, b));
   const int cpl = N * (int)sizeof(UR) / q.chunk;  // copies per line
+  const FastDiv fcpl((uint32_t)cpl);
   for (int e = threadIdx.x; e < 2 * M * cpl; e += blockDim.x) {
-    const int lt = e / cpl;
+    const int lt = (int)fcpl.div((uint32_t)e);
     const int c = e - lt * cpl;
     const int line = 2 * p0 + lt;
     const bool ok = line < x.nlines;
@@ -314,6 +315,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       W* sm = xpipe_buf<P>(q.c, b);
       const UR* raw = reinterpret_cast<const UR*>(sm);
       const int MN = q.x.M * q.x.nx, N = q.x.nx;
+      const FastDiv fN((uint32_t)N);
       C v[MAXI];
 #pragma unroll
       for (int i = 0; i < MAXI; ++i) v[i] = P::zero();  // see stage_reg
@@ -321,7 +323,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       for (int i = 0; i < MAXI; ++i) {
         const int e = threadIdx.x + i * blockDim.x;
         if (e < MN) {
-          const int pr = e / N;
+          const int pr = (int)fN.div((uint32_t)e);
           const int xi = e - pr * N;
           v[i] = P::make(P::from_ur(raw[(2 * pr) * N + xi]), P::from_ur(raw[(2 * pr + 1) * N + xi]));
         }
@@ -348,8 +350,9 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       const int field = tile / q.c.tiles_per_field;
       const int p0 = (tile - field * q.c.tiles_per_field) * M;
       W* out = static_cast<W*>(x.out) + field * x.out_field;
+      const FastDiv fnk((uint32_t)nk);
       for (int e = threadIdx.x; e < M * nk; e += blockDim.x) {
-        const int pr = e / nk;
+        const int pr = (int)fnk.div((uint32_t)e);
         const int k = e - pr * nk;
         const int line = 2 * (p0 + pr);
         if (line >= x.nlines) continue;
@@ -375,8 +378,9 @@ P3G_D void xc2r_issue(const XPipeParams& q, int tile, int b) {
   const int p0 = (tile - field * q.c.tiles_per_field) * M;
   const W* in = static_cast<const W*>(x.in) + field * x.in_field;
   W* dst = xpipe_buf<P>(q.c, b);
+  const FastDiv fnh((uint32_t)nh);
   for (int e = threadIdx.x; e < 2 * M * nh; e += blockDim.x) {
-    const int lt = e / nh;
+    const int lt = (int)fnh.div((uint32_t)e);
     const int k = e - lt * nh;
     const int line = 2 * p0 + lt;
     const bool ok = line < x.nlines && k < x.nkeep;
@@ -419,6 +423,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       const XPipeParams& q = pp;
       W* sm = xpipe_buf<P>(q.c, b);
       const int N = q.x.nx, nh = N / 2 + 1, NP = 2 * nh, Mnh = q.x.M * nh;
+      const FastDiv fnh((uint32_t)nh);
       C z0[MAXI], z1[MAXI];
       int ip[MAXI], ik[MAXI];
 #pragma unroll
@@ -432,7 +437,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
         const int e = threadIdx.x + i * blockDim.x;
         ip[i] = -1;
         if (e < Mnh) {
-          const int pr = e / nh;
+          const int pr = (int)fnh.div((uint32_t)e);
           const int k = e - pr * nh;
           C x1 = P::from_w(sm[pr * NP + k]);
           C x2 = P::from_w(sm[pr * NP + nh + k]);
@@ -472,8 +477,9 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       UR* out = static_cast<UR*>(x.out) + field * x.out_field;
       const float* smf = reinterpret_cast<const float*>(sm);
       constexpr int kW = sizeof(W) / sizeof(float);
+      const FastDiv fN((uint32_t)N);
       for (int e = threadIdx.x; e < 2 * M * N; e += blockDim.x) {
-        const int lt = e / N;
+        const int lt = (int)fN.div((uint32_t)e);
         const int n = e - lt * N;
         const int line = 2 * p0 + lt;
         if (line >= x.nlines) continue;
