@@ -26,6 +26,7 @@
 
 #include "../../include/p3dfft_gb300.h"
 #include "p3g_pipe.cuh"
+#include "p3g_plan_internal.h"
 
 namespace p3g {
 
@@ -110,19 +111,7 @@ struct HostTw {
   }
 };
 
-struct AxisPlan {
-  StagePlan sp{};
-  int n = 0;
-  int M = 1, log2m = 0, threads = 32;
-  size_t smem = 0;
-  int sp_index = 0;  // index into the device StagePlan array
-  int tw_lo = 0, tw_cnt = 0;  // this axis's contiguous slice of the twiddle table
-  // pipelined kernels (p3g_pipe.cuh): same tile, double buffered
-  bool pipe_ok = false;
-  int pipe_threads = 0;
-  int buf_elems = 0;
-  size_t pipe_smem = 0;
-};
+
 
 static bool build_stages(int n, bool allow16, HostTw& tw, StagePlan& sp) {
   std::memset(&sp, 0, sizeof(sp));
@@ -225,38 +214,13 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   ap.pipe_ok = ap.pipe_smem <= 227 * 1024;
 }
 
-struct TimerRec {
-  int slot;
-  cudaEvent_t a, b;
-};
+
 
 }  // namespace p3g
 
 using namespace p3g;
 
-struct p3g_plan_s {
-  int nx, ny, nz, nxc, nyc, nzc, prec, layout, flags;
-  int nxh, nxhp, nxhc, nxhpc, nycph, nzcph;
-  long long pitch;
-  AxisPlan ax_x, ax_y, ax_z[4];  // z: 0 fft, 1 dct (2(nz-1)), 2 dst (2(nz+1)), 3 none
-  bool z_ok[4];
-  float4* d_tw = nullptr;
-  StagePlan* d_sp = nullptr;
-  size_t tw_bytes = 0;
-  void* wa = nullptr;  // nz*ny*pitch*nv elements
-  void* wb = nullptr;  // nz*nyc*pitch*nv elements (only if nyc < ny)
-  size_t w_fields = 0;
-  double timers[12];
-  std::vector<TimerRec> pending;
-  std::vector<cudaEvent_t> free_events;
-  long long launches = 0;
-  std::mutex mu;
-  int sm_count = 0;
-  int* d_err = nullptr;  // set by a kernel whose bounded wait timed out
-  bool use_pipe = true, use_tma = true;
 
-  size_t esize() const { return prec == P3G_F64 ? 16 : 8; }
-};
 
 namespace {
 
