@@ -86,6 +86,20 @@ long long p3g_plan_device_bytes(p3g_plan plan);
 /* Kernel launches issued by this plan since creation. */
 long long p3g_plan_launches(p3g_plan plan);
 
+/* Allocation-free forward transform (one field, XYZ layout, single-tile
+ * kernels).  No counterpart in the reference.  For callers that must not
+ * allocate device memory after start-up (fixed-budget serving workers,
+ * frameworks that route every allocation through their own pool, loops that
+ * cannot afford cudaMalloc's device synchronisation): the workspace is a
+ * fixed 32 MiB device array inside the library, not a cudaMalloc.  Grids
+ * whose workspace (nz*ny*pitch*16 bytes for F64, *8 for F32, pitch =
+ * nxc/2+1 rounded up to 8 resp. 16, plus nz*nyc*pitch*... when nyc < ny)
+ * exceeds it are rejected with P3G_E_UNSUPPORTED.  The plan must exist
+ * already (p3g_plan_create allocates).  The first call on each device looks
+ * up the array's device address, so make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race. */
+int p3g_ftran_r2c_noalloc(p3g_plan plan, const void* in, void* out, const char* op, void* stream);
+
 /* Synchronises and reports a kernel-side failure recorded on the plan's
  * device flag (a pipelined pass whose bounded wait for a tile copy expired). */
 int p3g_plan_status(p3g_plan plan);

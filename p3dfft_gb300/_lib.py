@@ -26,6 +26,8 @@ CORE_SIGNATURES = {
     "p3g_set_timers": (ctypes.c_int, [ctypes.c_void_p]),
     "p3g_plan_device_bytes": (ctypes.c_longlong, [ctypes.c_void_p]),
     "p3g_plan_launches": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "p3g_ftran_r2c_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
+                                             ctypes.c_void_p]),
     "p3g_plan_status": (ctypes.c_int, [ctypes.c_void_p]),
     "p3g_plan_set_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "p3g_last_error": (ctypes.c_char_p, []),

@@ -32,7 +32,7 @@ namespace p3g {
 
 static thread_local std::string g_last_error;
 
-static int fail(int code, const std::string& msg) {
+int fail(int code, const std::string& msg) {
   g_last_error = msg;
   return code;
 }

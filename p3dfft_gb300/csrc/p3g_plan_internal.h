@@ -3,12 +3,16 @@
 #pragma once
 
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "../../include/p3dfft_gb300.h"
 #include "p3g_kernels.cuh"
 
 namespace p3g {
+
+// Records msg as the calling thread's p3g_last_error() and returns code.
+int fail(int code, const std::string& msg);
 
 struct AxisPlan {
   StagePlan sp{};
