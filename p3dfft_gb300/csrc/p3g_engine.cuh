@@ -81,12 +81,21 @@ P3G_D void sts(uint32_t a, float2 v) {
   asm volatile("st.shared.v2.f32 [%0], {%1, %2};\n" ::"r"(a), "f"(v.x), "f"(v.y) : "memory");
 }
 
+// Line-major tiles may be padded by one element every 2^ps elements
+// (ps = log2 of the plan's first radix, 0 = no padding) so that the first
+// stage's stride-R writes hit distinct banks.  For the plans that use it
+// (all radices powers of two, every stage's N/R and every later stage's
+// sub-length multiples of 2^ps) each stage's R inputs and R outputs stay
+// equally spaced in the padded layout.
+P3G_D int pad_index(int j, int ps) { return ps ? j + (j >> ps) : j; }
+
 template <class P>
 struct Tile {
   typename P::W* sm;       // M lines x N points
   typename P::W* scratch;  // same size, generic stages only
   int M, log2m, LS, JS;
-  P3G_D int addr(int line, int j) const { return line * LS + j * JS; }
+  int ps = 0;              // line-major padding shift (0: none)
+  P3G_D int addr(int line, int j) const { return line * LS + (LS == 1 ? j * JS : pad_index(j, ps)); }
   P3G_D uint32_t saddr(int line, int j) const {
     return (uint32_t)__cvta_generic_to_shared(sm) + (uint32_t)((line * LS + j * JS) * (int)sizeof(typename P::W));
   }
@@ -131,8 +140,10 @@ __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const
   const int nb = t.M * per_line;
   const int T = blockDim.x;
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(t.sm);
-  const uint32_t jstride = (uint32_t)(t.JS * (int)sizeof(W)) * (uint32_t)per_line;  // bytes between inputs q, q+1
-  const uint32_t ostride = (uint32_t)(t.JS * (int)sizeof(W)) * (uint32_t)ns;        // bytes between outputs
+  const int ps = t.LS == 1 ? 0 : t.ps;
+  // bytes between inputs q, q+1 and between outputs q, q+1
+  const uint32_t jstride = (uint32_t)(t.JS * (int)sizeof(W)) * (uint32_t)pad_index(per_line, ps);
+  const uint32_t ostride = (uint32_t)(t.JS * (int)sizeof(W)) * (uint32_t)pad_index(ns, ps);
   // Explicitly initialised: the arrays are written and read under correlated
   // guards (b < nb) the compiler cannot prove, and inside a persistent tile
   // loop an uninitialised element would otherwise be kept live around the

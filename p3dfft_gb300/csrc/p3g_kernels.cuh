@@ -20,6 +20,8 @@ struct XParams {
   int nkeep;                      // complex modes per line stored (r2c) / read (c2r)
   int M, log2m;                   // line pairs per tile
   int tiles;                      // tiles per field
+  int LS;                         // shared-memory stride between line pairs (>= padded N)
+  int ps;                         // line padding shift (see pad_index), 0 = none
 };
 
 // Strided Y/Z passes: a tile is M consecutive x columns of one (o1, o2) row

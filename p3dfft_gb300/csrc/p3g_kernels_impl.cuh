@@ -38,12 +38,13 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
 
   float* smf = reinterpret_cast<float*>(sm);
   constexpr int kW = sizeof(W) / sizeof(float);  // floats per element: 4 (F64) or 2 (F32)
+  const int LS = prm.LS, ps = prm.ps;
   for (int e = threadIdx.x; e < 2 * M * N; e += blockDim.x) {
     const int lt = e / N;
     const int x = e - lt * N;
     const int line = 2 * p0 + lt;
     const int c = lt & 1;
-    float* f = smf + ((lt >> 1) * N + x) * kW;
+    float* f = smf + ((lt >> 1) * LS + pad_index(x, ps)) * kW;
     if constexpr (P::kF64) {
       const df v = line < prm.nlines ? P::from_ur(in[(long long)line * prm.in_line + x]) : df{0.f, 0.f};
       f[c] = v.hi;
@@ -53,7 +54,7 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
     }
   }
   __syncthreads();
-  Tile<P> t{sm, sm + M * N, M, prm.log2m, N, 1};
+  Tile<P> t{sm, sm + M * LS, M, prm.log2m, LS, 1, ps};
   cta_fft<P, -1>(t, sp, tw);
   const int nk = prm.nkeep;
   for (int e = threadIdx.x; e < M * nk; e += blockDim.x) {
@@ -61,8 +62,8 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
     const int k = e - pr * nk;
     const int line = 2 * (p0 + pr);
     if (line >= prm.nlines) continue;
-    const C a = P::from_w(sm[pr * N + k]);
-    const C b = cconj(P::from_w(sm[pr * N + (k == 0 ? 0 : N - k)]));
+    const C a = P::from_w(sm[pr * LS + pad_index(k, ps)]);
+    const C b = cconj(P::from_w(sm[pr * LS + pad_index(k == 0 ? 0 : N - k, ps)]));
     out[(long long)line * prm.out_line + k] = P::to_w(cscale2(a + b, 0.5f));
     if (line + 1 < prm.nlines) out[(long long)(line + 1) * prm.out_line + k] = P::to_w(cscale2(rot<-1>(a - b), 0.5f));
   }
@@ -85,6 +86,7 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
   const W* in = static_cast<const W*>(prm.in) + field * prm.in_field;
   auto* out = static_cast<typename P::UR*>(prm.out) + field * prm.out_field;
   const int nh = N / 2 + 1;
+  const int LS = prm.LS, ps = prm.ps;
   for (int e = threadIdx.x; e < M * nh; e += blockDim.x) {
     const int pr = e / nh;
     const int k = e - pr * nh;
@@ -98,11 +100,11 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
       x1 = P::make(P::re(x1), P::re(P::zero()));
       x2 = P::make(P::re(x2), P::re(P::zero()));
     }
-    sm[pr * N + k] = P::to_w(x1 + rot<1>(x2));
-    if (k > 0 && 2 * k < N) sm[pr * N + N - k] = P::to_w(cconj(x1) + rot<1>(cconj(x2)));
+    sm[pr * LS + pad_index(k, ps)] = P::to_w(x1 + rot<1>(x2));
+    if (k > 0 && 2 * k < N) sm[pr * LS + pad_index(N - k, ps)] = P::to_w(cconj(x1) + rot<1>(cconj(x2)));
   }
   __syncthreads();
-  Tile<P> t{sm, sm + M * N, M, prm.log2m, N, 1};
+  Tile<P> t{sm, sm + M * LS, M, prm.log2m, LS, 1, ps};
   cta_fft<P, 1>(t, sp, tw);
   const float* smf = reinterpret_cast<const float*>(sm);
   constexpr int kW = sizeof(W) / sizeof(float);
@@ -112,7 +114,7 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
     const int line = 2 * p0 + lt;
     if (line >= prm.nlines) continue;
     const int c = lt & 1;
-    const float* f = smf + ((lt >> 1) * N + n) * kW;
+    const float* f = smf + ((lt >> 1) * LS + pad_index(n, ps)) * kW;
     if constexpr (P::kF64) {
       out[(long long)line * prm.out_line + n] = P::to_ur(df{f[c], f[2 + c]});
     } else {

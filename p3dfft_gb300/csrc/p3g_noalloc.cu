@@ -75,6 +75,8 @@ int forward_passes(p3g_plan p, const void* in, void* out, int zi, bool fsign, vo
     x.nkeep = p->nxhpc;
     x.M = p->ax_x.M;
     x.log2m = p->ax_x.log2m;
+    x.LS = p->ax_x.ls;
+    x.ps = p->ax_x.ps;
     x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
     cudaError_t e = launch_x_r2c<P>(x, p->d_sp + p->ax_x.sp_index, p->d_tw, p->ax_x.threads, p->ax_x.smem, 1, st);
     if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X r2c launch: ") + cudaGetErrorString(e));

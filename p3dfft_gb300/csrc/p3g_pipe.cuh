@@ -115,12 +115,10 @@ P3G_D void strided_issue(const SPipeParams& q, const CUtensorMap* tin, int tile,
   const long long ib = (long long)o1 * s.in_o1 + (long long)o2 * s.in_o2 + (long long)xt * M;
   const char* in = static_cast<const char*>(s.in);
   constexpr int esz = (int)sizeof(W);
-  for (int e = threadIdx.x; e < M * L; e += blockDim.x) {
-    const int m = e & (M - 1);
-    const int j = e >> s.log2m;
+  auto one = [&](int m, int j) {
     const int src = j >= s.lmap_a1 ? j - s.lmap_d : (j < s.lmap_a0 ? j : -1);
     const bool ok = src >= 0 && xt * M + m < s.X;
-    const char* g = ok ? in + (ib + m + src * s.in_axis) * esz : in;
+    const char* g = ok ? in + (ib + m + (long long)src * s.in_axis) * esz : in;
     const uint32_t nb = ok ? (uint32_t)esz : 0u;
     int r0 = j, r1 = -1;
     if (s.pre == 2) {
@@ -144,6 +142,13 @@ P3G_D void strided_issue(const SPipeParams& q, const CUtensorMap* tin, int tile,
         cp_async8(dst + (L + 1) * M + m, in, 0);
       }
     }
+  };
+  const int T = blockDim.x;
+  if ((T & (M - 1)) == 0) {  // each thread keeps one column m: rows strided by T/M
+    const int m = threadIdx.x & (M - 1);
+    for (int j = threadIdx.x >> s.log2m; j < L; j += T >> s.log2m) one(m, j);
+  } else {
+    for (int e = threadIdx.x; e < M * L; e += T) one(e & (M - 1), e >> s.log2m);
   }
   cp_async_commit();
 }
@@ -219,15 +224,23 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       strided_decode(q, tile, xt, o1, o2);
       const int x0 = xt * M;
       const long long obase = (long long)o1 * s.out_o1 + (long long)o2 * s.out_o2 + x0;
-      for (int e = threadIdx.x; e < M * s.Lout; e += blockDim.x) {
-        const int m = e & (M - 1);
-        const int jo = e >> s.log2m;
-        if (x0 + m >= s.X) continue;
+      auto one = [&](int m, int jo) {
         const int k = jo < s.smap_s0 ? jo : jo + s.smap_d;
         C v;
         if (s.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
         else v = P::from_w(sm[k * M + m]);
         store_elem<P>(s.out, s.out_user, obase + m + (long long)jo * s.out_axis, v);
+      };
+      const int T = blockDim.x;
+      if ((T & (M - 1)) == 0) {
+        const int m = threadIdx.x & (M - 1);
+        if (x0 + m < s.X)
+          for (int jo = threadIdx.x >> s.log2m; jo < s.Lout; jo += T >> s.log2m) one(m, jo);
+      } else {
+        for (int e = threadIdx.x; e < M * s.Lout; e += T) {
+          const int m = e & (M - 1);
+          if (x0 + m < s.X) one(m, e >> s.log2m);
+        }
       }
     }
     __syncthreads();
@@ -332,13 +345,16 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
 #pragma unroll
       for (int i = 0; i < MAXI; ++i) {
         const int e = threadIdx.x + i * blockDim.x;
-        if (e < MN) sm[e] = P::to_w(v[i]);
+        if (e < MN) {
+          const int pr = (int)fN.div((uint32_t)e);
+          sm[pr * q.x.LS + pad_index(e - pr * N, q.x.ps)] = P::to_w(v[i]);
+        }
       }
     }
     __syncthreads();
     {
       const XPipeParams& q = pp;
-      Tile<P> t{xpipe_buf<P>(q.c, b), nullptr, q.x.M, q.x.log2m, q.x.nx, 1};
+      Tile<P> t{xpipe_buf<P>(q.c, b), nullptr, q.x.M, q.x.log2m, q.x.LS, 1, q.x.ps};
       cta_fft<P, -1, PipeLimits<P>::kE>(t, sp, xpipe_tw<P>(q.c), q.c.tw_base);
     }
     {
@@ -356,8 +372,8 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
         const int k = e - pr * nk;
         const int line = 2 * (p0 + pr);
         if (line >= x.nlines) continue;
-        const C a = P::from_w(sm[pr * N + k]);
-        const C bb = cconj(P::from_w(sm[pr * N + (k == 0 ? 0 : N - k)]));
+        const C a = P::from_w(sm[pr * x.LS + pad_index(k, x.ps)]);
+        const C bb = cconj(P::from_w(sm[pr * x.LS + pad_index(k == 0 ? 0 : N - k, x.ps)]));
         out[(long long)line * x.out_line + k] = P::to_w(cscale2(a + bb, 0.5f));
         if (line + 1 < x.nlines)
           out[(long long)(line + 1) * x.out_line + k] = P::to_w(cscale2(rot<-1>(a - bb), 0.5f));
@@ -452,26 +468,26 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
         }
       }
       __syncthreads();
+      const int LS = q.x.LS, ps = q.x.ps;  // Z layout (padded), raw lines used NP = 2 nh
 #pragma unroll
       for (int i = 0; i < MAXI; ++i) {
         if (ip[i] >= 0) {
-          sm[ip[i] * NP + ik[i]] = P::to_w(z0[i]);
-          if (ik[i] > 0 && 2 * ik[i] < N) sm[ip[i] * NP + N - ik[i]] = P::to_w(z1[i]);
+          sm[ip[i] * LS + pad_index(ik[i], ps)] = P::to_w(z0[i]);
+          if (ik[i] > 0 && 2 * ik[i] < N) sm[ip[i] * LS + pad_index(N - ik[i], ps)] = P::to_w(z1[i]);
         }
       }
     }
     __syncthreads();
     {
       const XPipeParams& q = pp;
-      const int NP = 2 * (q.x.nx / 2 + 1);
-      Tile<P> t{xpipe_buf<P>(q.c, b), nullptr, q.x.M, q.x.log2m, NP, 1};
+      Tile<P> t{xpipe_buf<P>(q.c, b), nullptr, q.x.M, q.x.log2m, q.x.LS, 1, q.x.ps};
       cta_fft<P, 1, PipeLimits<P>::kE>(t, sp, xpipe_tw<P>(q.c), q.c.tw_base);
     }
     {
       const XPipeParams& q = pp;
       const XParams& x = q.x;
       const W* sm = xpipe_buf<P>(q.c, b);
-      const int M = x.M, N = x.nx, NP = 2 * (N / 2 + 1);
+      const int M = x.M, N = x.nx, LS = x.LS, ps = x.ps;
       const int field = tile / q.c.tiles_per_field;
       const int p0 = (tile - field * q.c.tiles_per_field) * M;
       UR* out = static_cast<UR*>(x.out) + field * x.out_field;
@@ -484,7 +500,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
         const int line = 2 * p0 + lt;
         if (line >= x.nlines) continue;
         const int c = lt & 1;
-        const float* f = smf + ((lt >> 1) * NP + n) * kW;
+        const float* f = smf + ((lt >> 1) * LS + pad_index(n, ps)) * kW;
         if constexpr (P::kF64) out[(long long)line * x.out_line + n] = P::to_ur(df{f[c], f[2 + c]});
         else out[(long long)line * x.out_line + n] = f[c];
       }

@@ -158,12 +158,14 @@ static int ilog2(int v) {
 // Tile sizing: M lines of n points so that one tile holds about `budget`
 // elements (64 KB), M a power of two not larger than needed, threads =
 // ceil(M n / E) rounded up to a warp.
-static bool size_tile(AxisPlan& ap, int n, int lines_avail, bool f64) {
+// max_m caps the tile width of strided passes so that one TMA box row
+// (M elements) stays within the 256-word box limit.
+static bool size_tile(AxisPlan& ap, int n, int lines_avail, bool f64, int max_m = 1 << 30) {
   const int budget = f64 ? 4096 : 8192;
   const int max_threads = f64 ? 256 : 512;
   const size_t esize = f64 ? 16 : 8;
   int M = 1;
-  while (M * 2 * n <= budget && M * 2 <= (1 << ilog2(lines_avail > 0 ? lines_avail : 1))) M *= 2;
+  while (M * 2 * n <= budget && M * 2 <= (1 << ilog2(lines_avail > 0 ? lines_avail : 1)) && M * 2 <= max_m) M *= 2;
   auto threads_for = [&](int m) {
     int t = (m * n + kElemsPerThread - 1) / kElemsPerThread;
     t = (t + 31) / 32 * 32;
@@ -207,7 +209,7 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   }
   if (M != ap.M) return;  // keep one tile shape per axis
   // buffer stride rounded to 1 KB so both buffers (TMA destinations) stay aligned
-  const size_t need = (size_t)(kind == 2 ? M * 2 * nh : M * n) * esize;
+  const size_t need = (size_t)(kind == 0 ? M * n : M * (ap.ls > 2 * nh ? ap.ls : 2 * nh)) * esize;
   const size_t buf_bytes = (need + 1023) / 1024 * 1024;
   ap.buf_elems = (int)(buf_bytes / esize);
   ap.pipe_smem = 1024 + 2 * buf_bytes + (size_t)ap.tw_cnt * 16 + 16;
@@ -485,6 +487,8 @@ int do_ftran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
     x.nkeep = p->nxhpc;
     x.M = p->ax_x.M;
     x.log2m = p->ax_x.log2m;
+    x.LS = p->ax_x.ls;
+    x.ps = p->ax_x.ps;
     x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
     rc = run_x_r2c<P>(p, x, nv, st);
     if (rc) return rc;
@@ -637,6 +641,8 @@ int do_btran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
     x.nkeep = p->nxhpc;
     x.M = p->ax_x.M;
     x.log2m = p->ax_x.log2m;
+    x.LS = p->ax_x.ls;
+    x.ps = p->ax_x.ps;
     x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
     rc = run_x_c2r<P>(p, x, nv, st);
     if (rc) return rc;
@@ -696,11 +702,12 @@ int p3g_plan_create(p3g_plan* out, int nx, int ny, int nz, int nxc, int nyc, int
 
   HostTw tw;
   std::vector<StagePlan> sps;
+  const int strided_max_m = f64 ? 64 : 128;  // 256 words per TMA box row
   auto add_axis = [&](AxisPlan& ap, int n, int lines) -> bool {
     if (!build_stages(n, !f64, tw, ap.sp)) return false;
     ap.tw_lo = tw.mark;
     ap.tw_cnt = (int)tw.v.size() - tw.mark;
-    if (!size_tile(ap, n, lines, f64)) return false;
+    if (!size_tile(ap, n, lines, f64, &ap == &p->ax_x ? (1 << 30) : strided_max_m)) return false;
     ap.sp_index = (int)sps.size();
     sps.push_back(ap.sp);
     return true;
@@ -710,6 +717,30 @@ int p3g_plan_create(p3g_plan* out, int nx, int ny, int nz, int nxc, int nyc, int
     return fail(P3G_E_UNSUPPORTED, m);
   };
   if (!add_axis(p->ax_x, nx, (ny * nz + 1) / 2)) return bad("x length " + std::to_string(nx) + " is too long");
+  {
+    // line padding for the X tiles (pad_index in p3g_engine.cuh): only for
+    // all-power-of-two plans whose every N/R is a multiple of the first radix
+    AxisPlan& ax = p->ax_x;
+    int ps = 0;
+    if (ax.sp.nstages > 0 && !ax.sp.has_generic) {
+      const int r0 = ax.sp.radix[0];
+      bool ok = (r0 & (r0 - 1)) == 0 && r0 >= 4;
+      for (int i = 0; ok && i < ax.sp.nstages; ++i) {
+        const int r = ax.sp.radix[i];
+        ok = (r & (r - 1)) == 0 && (nx / r) % r0 == 0;
+      }
+      if (ok) ps = ilog2(r0);
+    }
+    const int nh2 = 2 * (nx / 2 + 1);
+    ax.ps = ps;
+    ax.ls = nx + (ps ? nx >> ps : 0);
+    if (ax.ls < nh2) ax.ls = nh2;
+    ax.smem = (size_t)ax.M * ax.ls * (f64 ? 16 : 8) * (ax.sp.has_generic ? 2 : 1);
+    if (ax.smem > 227 * 1024) {
+      delete p;
+      return fail(P3G_E_UNSUPPORTED, "x length " + std::to_string(nx) + " is too long");
+    }
+  }
   if (!add_axis(p->ax_y, ny, p->nxhpc)) return bad("y length " + std::to_string(ny) + " is too long");
   p->z_ok[0] = add_axis(p->ax_z[0], nz, p->nxhpc);
   p->z_ok[1] = nz >= 2 && add_axis(p->ax_z[1], 2 * (nz - 1), p->nxhpc);
@@ -719,7 +750,7 @@ int p3g_plan_create(p3g_plan* out, int nx, int ny, int nz, int nxc, int nyc, int
     p->ax_z[3].n = nz;
     sps[p->ax_z[3].sp_index].n = nz;
     p->ax_z[3].sp.n = nz;
-    if (!size_tile(p->ax_z[3], nz, p->nxhpc, f64)) p->z_ok[3] = false;
+    if (!size_tile(p->ax_z[3], nz, p->nxhpc, f64, strided_max_m)) p->z_ok[3] = false;
   }
   if (!p->z_ok[0] && !p->z_ok[1] && !p->z_ok[3]) return bad("z length " + std::to_string(nz) + " is too long");
   size_pipe(p->ax_x, 1, f64);  // r2c and c2r share the tile; c2r needs the larger buffer

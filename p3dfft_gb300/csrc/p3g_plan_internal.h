@@ -21,6 +21,7 @@ struct AxisPlan {
   size_t smem = 0;
   int sp_index = 0;  // index into the device StagePlan array
   int tw_lo = 0, tw_cnt = 0;  // this axis's contiguous slice of the twiddle table
+  int ls = 0, ps = 0;         // X axis: shared-memory line-pair stride and padding shift
   // pipelined kernels (p3g_pipe.cuh): same tile, double buffered
   bool pipe_ok = false;
   int pipe_threads = 0;
