@@ -44,6 +44,13 @@ CONFIGS = {
 
 MODES = {"pipe_tma": (True, True), "pipe_cpasync": (True, False), "single_tile": (False, False)}
 
+# DRAM bytes (read + write) per algorithmic byte of one launch, from the ncu
+# capture summarised in profiles/k_strided_pipe_f64.md (1024x1024x32 Y pass:
+# 272.75 MB read + 217.33 MB written for 538.97 MB of 2C model traffic).  The
+# full-size launch moves the same bytes per line, so traffic scales with the
+# model.
+TRAFFIC_PER_ALGO_BYTE = {"k_strided_pipe": (272.753152e6 + 217.333504e6) / 538968064.0}
+
 
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -221,8 +228,18 @@ def run_ours(args):
     }
     pass_bytes = {"x_r2c": bm["x"], "y_fwd": bm["y"], "z_fwd": bm["z"], "z_bwd": bm["z"], "y_bwd": bm["y"],
                   "x_c2r": bm["x"]}
-    dom = max(pass_ms, key=lambda k: pass_ms[k])
-    achieved = pass_bytes[dom] / (pass_ms[dom] * 1e-3) / 1e9 if pass_ms[dom] > 0 else None
+    # passes grouped by kernel; the dominant kernel is the one with the largest
+    # total time per round trip (4 strided launches, 1 r2c, 1 c2r)
+    groups = {"k_strided_pipe": ["y_fwd", "z_fwd", "z_bwd", "y_bwd"], "k_xr2c_pipe": ["x_r2c"],
+              "k_xc2r_pipe": ["x_c2r"]}
+    dom = max(groups, key=lambda k: sum(pass_ms[p] for p in groups[k]))
+    nl = len(groups[dom])
+    dom_ms = sum(pass_ms[p] for p in groups[dom]) / nl
+    dom_bytes = sum(pass_bytes[p] for p in groups[dom]) / nl
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9 if dom_ms > 0 else None
+    traffic = None
+    if dom in TRAFFIC_PER_ALGO_BYTE:
+        traffic = int(TRAFFIC_PER_ALGO_BYTE[dom] * dom_bytes)
     del r
     plan.close()
 
@@ -265,9 +282,13 @@ def run_ours(args):
         "f32": {"value": round(world * npts / (ms32 * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_step": round(ms32, 4),
                 "rel_l2_vs_f64": err32, "speedup_vs_f64": round(ms64 / ms32, 3)},
         "passes_ms": {k: round(v, 4) for k, v in pass_ms.items()},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1) if achieved else None,
+        "roofline": {"bound": "hbm", "kernel": dom, "launches_per_step": nl,
+                     "algorithmic_bytes_per_launch": int(dom_bytes),
+                     "avg_launch_ms": round(dom_ms, 4),
+                     "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
-                     "peak_kind": peak_kind, "traffic": None,
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "traffic_source": "profiles/k_strided_pipe_f64.md (1024x1024x32 capture scaled by lines)",
                      "step_bytes_model": bm["rt"],
                      "step_frac": round(bm["rt"] / (ms64 * 1e-3) / 1e9 / peak, 4)},
         "gpu_launches": launches,

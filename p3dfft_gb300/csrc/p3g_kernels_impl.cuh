@@ -294,6 +294,21 @@ cudaError_t launch_xc2r_pipe(const XPipeParams& p, const StagePlan* sp, const fl
   return cudaGetLastError();
 }
 
+// Resident CTAs per SM of a pipelined kernel (kind 0 strided, 1 r2c, 2 c2r)
+// for the given block size and dynamic shared memory; 1 if the query fails.
+template <class P>
+int pipe_blocks_per_sm(int kind, int threads, size_t smem) {
+  const void* f = kind == 0 ? (const void*)k_strided_pipe<P, -1>
+                            : (kind == 1 ? (const void*)k_xr2c_pipe<P> : (const void*)k_xc2r_pipe<P>);
+  cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem) != cudaSuccess || n < 1) {
+    cudaGetLastError();
+    return 1;
+  }
+  return n;
+}
+
 #define P3G_INSTANTIATE(P)                                                                                          \
   template cudaError_t launch_x_r2c<P>(const XParams&, const StagePlan*, const float4*, int, size_t, int,          \
                                        cudaStream_t);                                                              \
@@ -302,6 +317,7 @@ cudaError_t launch_xc2r_pipe(const XPipeParams& p, const StagePlan* sp, const fl
   template cudaError_t launch_strided<P>(const SParams&, const StagePlan*, const float4*, bool, int, size_t, int,  \
                                          cudaStream_t);                                                            \
   template cudaError_t launch_cheby<P>(const ChebyParams&, int, cudaStream_t);                                     \
+  template int pipe_blocks_per_sm<P>(int, int, size_t);                                                            \
   template cudaError_t launch_strided_pipe<P>(const CUtensorMap*, const SPipeParams&, const StagePlan*,             \
                                               const float4*, bool, int, int, size_t, int, cudaStream_t);          \
   template cudaError_t launch_xr2c_pipe<P>(const XPipeParams&, const StagePlan*, const float4*, int, int, size_t,  \

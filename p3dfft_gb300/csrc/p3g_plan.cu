@@ -387,7 +387,8 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
         pp.box_bytes = brows * ap.M * esize;
       }
     }
-    const int grid = pp.c.ntiles < p->sm_count ? pp.c.ntiles : p->sm_count;
+    const int slots = p->sm_count * ap.pipe_bps;
+    const int grid = pp.c.ntiles < slots ? pp.c.ntiles : slots;
     cudaError_t e = launch_strided_pipe<P>(&map, pp, p->d_sp + ap.sp_index, p->d_tw, fwd_sign, kElemsPerThread,
                                            ap.pipe_threads, ap.pipe_smem, grid, st);
     if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("strided pass launch: ") + cudaGetErrorString(e));
@@ -418,7 +419,8 @@ int run_x_r2c(p3g_plan p, XParams& x, int nv, cudaStream_t st) {
     xp.c.tw_count = ap.tw_cnt;
     xp.c.buf_elems = ap.buf_elems;
     xp.c.err = p->d_err;
-    const int grid = xp.c.ntiles < p->sm_count ? xp.c.ntiles : p->sm_count;
+    const int slots = p->sm_count * ap.pipe_bps;
+    const int grid = xp.c.ntiles < slots ? xp.c.ntiles : slots;
     cudaError_t e = launch_xr2c_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, kElemsPerThread, ap.pipe_threads,
                                         ap.pipe_smem, grid, st);
     if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X r2c launch: ") + cudaGetErrorString(e));
@@ -444,7 +446,8 @@ int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st) {
     xp.c.tw_count = ap.tw_cnt;
     xp.c.buf_elems = ap.buf_elems;
     xp.c.err = p->d_err;
-    const int grid = xp.c.ntiles < p->sm_count ? xp.c.ntiles : p->sm_count;
+    const int slots = p->sm_count * ap.pipe_bps;
+    const int grid = xp.c.ntiles < slots ? xp.c.ntiles : slots;
     cudaError_t e = launch_xc2r_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, kElemsPerThread, ap.pipe_threads,
                                         ap.pipe_smem, grid, st);
     if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X c2r launch: ") + cudaGetErrorString(e));
@@ -764,6 +767,16 @@ int p3g_plan_create(p3g_plan* out, int nx, int ny, int nz, int nxc, int nyc, int
   size_pipe(p->ax_y, 0, f64);
   for (int i = 0; i < 4; ++i)
     if (p->z_ok[i]) size_pipe(p->ax_z[i], 0, f64);
+  {
+    auto bps = [&](AxisPlan& ap, int kind) {
+      if (ap.pipe_ok)
+        ap.pipe_bps = f64 ? pipe_blocks_per_sm<PathF64>(kind, ap.pipe_threads, ap.pipe_smem)
+                          : pipe_blocks_per_sm<PathF32>(kind, ap.pipe_threads, ap.pipe_smem);
+    };
+    bps(p->ax_x, 2);
+    bps(p->ax_y, 0);
+    for (int i = 0; i < 4; ++i) bps(p->ax_z[i], 0);
+  }
   {
     const char* e = std::getenv("P3G_NO_PIPE");
     p->use_pipe = !(e && *e && *e != '0');

@@ -27,6 +27,7 @@ struct AxisPlan {
   int pipe_threads = 0;
   int buf_elems = 0;
   size_t pipe_smem = 0;
+  int pipe_bps = 1;  // resident CTAs per SM of the pipelined kernel
 };
 
 struct TimerRec {
