@@ -44,9 +44,9 @@ CONFIGS = {
 
 MODES = {"pipe_tma": (True, True), "pipe_cpasync": (True, False), "single_tile": (False, False)}
 
-# DRAM bytes (read + write) per algorithmic byte of one launch, from the ncu
-# capture summarised in profiles/k_strided_pipe_f64.md (1024x1024x32 Y pass:
-# 272.75 MB read + 217.33 MB written for 538.97 MB of 2C model traffic).  The
+# DRAM bytes (read + write) per algorithmic byte of one launch, from an ncu
+# capture of the strided Y pass on a 1024x1024x32 grid (272.75 MB read +
+# 217.33 MB written for 538.97 MB of 2C model traffic).  The
 # full-size launch moves the same bytes per line, so traffic scales with the
 # model.
 TRAFFIC_PER_ALGO_BYTE = {"k_strided_pipe": (272.753152e6 + 217.333504e6) / 538968064.0}
@@ -288,7 +288,7 @@ def run_ours(args):
                      "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                      "peak_kind": peak_kind, "traffic": traffic,
-                     "traffic_source": "profiles/k_strided_pipe_f64.md (1024x1024x32 capture scaled by lines)",
+                     "traffic_source": "ncu DRAM read+write of the 1024x1024x32 Y-pass launch, 0.909 per algorithmic byte, scaled to this launch",
                      "step_bytes_model": bm["rt"],
                      "step_frac": round(bm["rt"] / (ms64 * 1e-3) / 1e9 / peak, 4)},
         "gpu_launches": launches,

@@ -57,10 +57,14 @@ extern void FORT_MOD_NAME(p3dfft_clean)(void);
 extern void FORT_MOD_NAME(p3dfft_get_mpi_info)(int* taskid, int* ntasks, int* comm);
 
 /* GB300 additions: status of the last call (0 = success, negative = error),
- * its message, and the abort-on-error switch (default on). */
+ * its message, and the abort-on-error switch (default on).
+ * p3dfft_gb_set_layout(0 | 1), called before p3dfft_setup, selects the
+ * (nxhpc, nyc, nzc) output layout (0, the default) or the (nzc, nyc, nxhpc)
+ * layout of the reference's STRIDE1 build (1; module.F90:245-254). */
 extern int p3dfft_gb_status(void);
 extern const char* p3dfft_gb_last_error(void);
 extern void p3dfft_gb_set_abort(int on);
+extern void p3dfft_gb_set_layout(int layout);
 
 /* by-value helpers, as the reference's Cp3dfft_* (p3dfft.h:165-264) */
 static inline void Cp3dfft_setup(int* dims, int nx, int ny, int nz, int comm, int nxc, int nyc, int nzc,

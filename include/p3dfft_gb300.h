@@ -74,6 +74,22 @@ int p3g_btran_c2r(p3g_plan plan, const void* in, void* out, const char* op, int 
 int p3g_cheby(p3g_plan plan, const void* in, void* out, double lz, int nv, long long dim_in, long long dim_out,
               void* stream);
 
+/* Shell spectrum of a forward transform's output `in` (device, ip=2 layout),
+ * restating compute_spectrum of the reference's spectrum sample
+ * (sample/FORTRAN/driver_spec.F90:263-341) for one rank.  For each of nv
+ * fields, E[f*(kmax+1) + ik] (device, binary64) = scale^2 * sum of
+ * weight * |B|^2 over the kept modes with ik = int(sqrt(kx^2+ky^2+kz^2)+0.5),
+ * ky and kz folded to |frequency| as the sample folds them.  weight is k^2
+ * with P3G_SPEC_K2 (the sample's choice), else 1, and is doubled with
+ * P3G_SPEC_HERMITIAN for modes 0 < kx, 2 kx != nx (the conjugate half of a
+ * real field).  Accumulated in binary64; E is cleared first.  kmax <= 0
+ * selects the sample's int(sqrt(nx^2+ny^2+nz^2)/2 + 0.5); a kmax below the
+ * sample's own check (driver_spec.F90:271-274) is an error, and modes beyond
+ * kmax are not counted. */
+enum { P3G_SPEC_K2 = 1, P3G_SPEC_HERMITIAN = 2 };
+int p3g_spectrum(p3g_plan plan, const void* in, double* E, int kmax, double scale, int flags, int nv,
+                 long long dim_in, void* stream);
+
 /* The reference's 12 accumulating stage timers (build/module.F90:106,709-744),
  * in seconds: slot 5 X r2c, 7 Y forward, 8 Z forward, 9 Z backward,
  * 10 Y backward, 12 X c2r (1-based; communication slots stay 0).  Needs

@@ -300,14 +300,20 @@ def _normalise_op(op) -> str:
 # --------------------------------------------------------------------------
 # caller-side pieces used by the sample programs
 # --------------------------------------------------------------------------
-def shell_spectrum(b: np.ndarray, nx: int, ny: int, nz: int, stride1: bool = False) -> np.ndarray:
+def shell_spectrum(b: np.ndarray, nx: int, ny: int, nz: int, stride1: bool = False, k2_weight: bool = True,
+                   hermitian: bool = False, kmax: int = 0) -> np.ndarray:
     """compute_spectrum, driver_spec.F90:263-341, single rank.
 
     ``b`` is the (normalised) forward output in the ip=2 layout.  Returns
-    E(0..kmax) with kmax = int(sqrt(nx^2+ny^2+nz^2)*0.5+0.5) (driver_spec.F90:198),
-    E(ik) = sum k^2 |B|^2, ik = int(sqrt(k^2)+0.5); the r2c half is not doubled.
+    E(0..kmax) with kmax = int(sqrt(nx^2+ny^2+nz^2)*0.5+0.5) by default
+    (driver_spec.F90:198), E(ik) = sum k^2 |B|^2, ik = int(sqrt(k^2)+0.5); the
+    r2c half is not doubled.  k2_weight=False gives unit weights and
+    hermitian=True doubles the modes 0 < kx, 2 kx != nx (the conjugate half of
+    a real field), the power spectrum of the serving form; modes with
+    ik > kmax are not counted.
     """
-    kmax = int(np.sqrt(float(nx) * nx + ny * ny + nz * nz) * 0.5 + 0.5)
+    if kmax <= 0:
+        kmax = int(np.sqrt(float(nx) * nx + ny * ny + nz * nz) * 0.5 + 0.5)
     if stride1:
         b = b.transpose(2, 1, 0)
     nzc, nyc, nxhpc = b.shape
@@ -318,8 +324,14 @@ def shell_spectrum(b: np.ndarray, nx: int, ny: int, nz: int, stride1: bool = Fal
     kx = np.arange(nxhpc)
     k2 = (kz[:, None, None] ** 2 + ky[None, :, None] ** 2 + kx[None, None, :] ** 2).astype(np.float64)
     ik = (np.sqrt(k2) + 0.5).astype(np.int64)
-    w = k2 * (b.real ** 2 + b.imag ** 2)
-    return np.bincount(ik.ravel(), weights=w.ravel(), minlength=kmax + 1)[: kmax + 1]
+    w = b.real.astype(np.float64) ** 2 + b.imag.astype(np.float64) ** 2
+    if k2_weight:
+        w = k2 * w
+    if hermitian:
+        kxb = np.broadcast_to(kx[None, None, :], w.shape)
+        w = np.where((kxb > 0) & (2 * kxb != nx), 2.0 * w, w)
+    keep = ik <= kmax
+    return np.bincount(ik[keep].ravel(), weights=w[keep].ravel(), minlength=kmax + 1)[: kmax + 1]
 
 
 def normalised_linf(a: np.ndarray, ref: np.ndarray) -> float:

@@ -32,6 +32,8 @@ F64 = 0
 F32 = 1
 LAYOUT_XYZ = 0
 LAYOUT_STRIDE1 = 1
+SPEC_K2 = 1
+SPEC_HERMITIAN = 2
 FLAG_TIMERS = 1
 
 
@@ -131,6 +133,23 @@ class Plan:
         _check(_core().p3g_cheby(self._h, _ptr(x), _ptr(out), float(lz), nv, dim_in, dim_out, _stream_ptr(stream)))
         return out
 
+    def spectrum(self, b, kmax=0, scale=1.0, flags=None, nv=1, dim_in=0, out=None, stream=None):
+        """Shell spectrum of the forward output b (see p3g_spectrum); returns a
+        float64 CUDA tensor of kmax + 1 bins (nv rows when nv > 1).  flags
+        defaults to SPEC_K2, the spectrum sample's k^2 |B|^2 weighting."""
+        import math
+        import torch
+        if flags is None:
+            flags = SPEC_K2
+        if kmax <= 0:
+            kmax = int(math.sqrt(float(self.nx) ** 2 + float(self.ny) ** 2 + float(self.nz) ** 2) * 0.5 + 0.5)
+        if out is None:
+            shape = ((nv,) if nv > 1 else ()) + (kmax + 1,)
+            out = torch.empty(shape, dtype=torch.float64, device=b.device)
+        _check(_core().p3g_spectrum(self._h, _ptr(b), _ptr(out), kmax, float(scale), int(flags), nv, dim_in,
+                                    _stream_ptr(stream)))
+        return out
+
     def set_options(self, pipe=True, tma=True):
         """Kernel selection (see p3g_plan_set_options)."""
         _check(_core().p3g_plan_set_options(self._h, int(pipe), int(tma)))
@@ -189,12 +208,17 @@ def _legacy_check():
         raise P3DFFTError(lib.p3dfft_gb_last_error().decode())
 
 
-def p3dfft_setup(dims, nx, ny, nz, comm=0, nxc=None, nyc=None, nzc=None, overwrite=True, single=False):
-    """setup.F90:107: returns memsize (the padded in-place size)."""
+def p3dfft_setup(dims, nx, ny, nz, comm=0, nxc=None, nyc=None, nzc=None, overwrite=True, single=False,
+                 stride1=False):
+    """setup.F90:107: returns memsize (the padded in-place size).  stride1
+    selects the (nzc, nyc, nxhpc) output layout of the reference's STRIDE1
+    build."""
     global _single
     _single = bool(single)
     d = (ctypes.c_int * 2)(*dims)
     mem = (ctypes.c_int * 3)()
+    _legacy().p3dfft_gb_set_layout(LAYOUT_STRIDE1 if stride1 else LAYOUT_XYZ)
+    _legacy_check()
     _legacy().p3dfft_setup(d, ctypes.byref(_ci(nx)), ctypes.byref(_ci(ny)), ctypes.byref(_ci(nz)),
                            ctypes.byref(_ci(comm)), ctypes.byref(_ci(nxc or nx)), ctypes.byref(_ci(nyc or ny)),
                            ctypes.byref(_ci(nzc or nz)), ctypes.byref(_ci(1 if overwrite else 0)), mem)

@@ -29,6 +29,8 @@ CORE_SIGNATURES = {
     "p3g_ftran_r2c_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
                                              ctypes.c_void_p]),
     "p3g_plan_status": (ctypes.c_int, [ctypes.c_void_p]),
+    "p3g_spectrum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_int, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p]),
     "p3g_plan_set_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "p3g_last_error": (ctypes.c_char_p, []),
     "p3g_version": (ctypes.c_int, []),
@@ -55,6 +57,7 @@ LEGACY_SIGNATURES = {
     "p3dfft_gb_status": (ctypes.c_int, []),
     "p3dfft_gb_last_error": (ctypes.c_char_p, []),
     "p3dfft_gb_set_abort": (None, [ctypes.c_int]),
+    "p3dfft_gb_set_layout": (None, [ctypes.c_int]),
 }
 
 

@@ -34,6 +34,7 @@ struct SParams {
   int in_user, out_user;  // 1: user complex format, 0: workspace format
   long long in_axis, in_o1, in_o2;
   long long out_axis, out_o1, out_o2;
+  long long in_xs, out_xs;  // stride between x columns: 1, or nyc*nzc for the STRIDE1 user layout
   int X;            // valid x columns
   int M, log2m;     // tile width (power of two)
   int xtiles, O1;   // tiles per row, number of o1 rows (o2 = fields from the grid)

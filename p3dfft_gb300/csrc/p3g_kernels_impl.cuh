@@ -140,19 +140,30 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
   const int o1 = (int)(bid % prm.O1);
   const int o2 = (int)(bid / prm.O1);
   const int x0 = xt * M;
-  const long long ibase = (long long)o1 * prm.in_o1 + (long long)o2 * prm.in_o2 + x0;
-  const long long obase = (long long)o1 * prm.out_o1 + (long long)o2 * prm.out_o2 + x0;
+  const long long ibase = (long long)o1 * prm.in_o1 + (long long)o2 * prm.in_o2 + x0 * prm.in_xs;
+  const long long obase = (long long)o1 * prm.out_o1 + (long long)o2 * prm.out_o2 + x0 * prm.out_xs;
 
   if (prm.pre == 2 && threadIdx.x < M) {  // DST-I odd extension: zero rows 0 and L+1
     sm[threadIdx.x] = P::to_w(P::zero());
     sm[(L + 1) * M + threadIdx.x] = P::to_w(P::zero());
   }
+  // element e -> (column m, row j): columns fastest when columns are adjacent
+  // in memory, rows fastest when rows are (STRIDE1 user layout)
+  const bool in_rows_fast = prm.in_xs != 1;
+  const FastDiv div_l(L);
   for (int e = threadIdx.x; e < M * L; e += blockDim.x) {
-    const int m = e & (M - 1);
-    const int j = e >> prm.log2m;
+    int m, j;
+    if (in_rows_fast) {
+      m = div_l.div(e);
+      j = e - m * L;
+    } else {
+      m = e & (M - 1);
+      j = e >> prm.log2m;
+    }
     const int src = j >= prm.lmap_a1 ? j - prm.lmap_d : (j < prm.lmap_a0 ? j : -1);
     C v = P::zero();
-    if (x0 + m < prm.X && src >= 0) v = load_elem<P>(prm.in, prm.in_user, ibase + m + src * prm.in_axis);
+    if (x0 + m < prm.X && src >= 0)
+      v = load_elem<P>(prm.in, prm.in_user, ibase + m * prm.in_xs + src * prm.in_axis);
     if (prm.pre == 0) {
       sm[j * M + m] = P::to_w(v);
     } else if (prm.pre == 1) {
@@ -166,15 +177,23 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
   __syncthreads();
   Tile<P> t{sm, sm + M * N, M, prm.log2m, 1, M};
   cta_fft<P, DIR>(t, sp, tw);
+  const bool out_rows_fast = prm.out_xs != 1;
+  const FastDiv div_lo(prm.Lout);
   for (int e = threadIdx.x; e < M * prm.Lout; e += blockDim.x) {
-    const int m = e & (M - 1);
-    const int jo = e >> prm.log2m;
+    int m, jo;
+    if (out_rows_fast) {
+      m = div_lo.div(e);
+      jo = e - m * prm.Lout;
+    } else {
+      m = e & (M - 1);
+      jo = e >> prm.log2m;
+    }
     if (x0 + m >= prm.X) continue;
     const int k = jo < prm.smap_s0 ? jo : jo + prm.smap_d;
     C v;
     if (prm.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
     else v = P::from_w(sm[k * M + m]);
-    store_elem<P>(prm.out, prm.out_user, obase + m + jo * prm.out_axis, v);
+    store_elem<P>(prm.out, prm.out_user, obase + m * prm.out_xs + jo * prm.out_axis, v);
   }
 }
 

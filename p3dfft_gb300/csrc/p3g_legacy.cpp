@@ -1,7 +1,9 @@
 // The reference's drop-in entry points (include/p3dfft.h) on top of the
 // explicit device API.  Built twice: libp3dfft.so (binary64 arrays) and, with
 // -DSINGLE_PREC, libp3dfft_single.so (binary32 arrays), mirroring the
-// reference's --enable-single build.
+// reference's --enable-single build.  -DSTRIDE1 makes the (nzc, nyc, nxhpc)
+// output layout the default, as the reference's --enable-stride1 build does;
+// p3dfft_gb_set_layout picks the layout at run time before p3dfft_setup.
 //
 // State follows the reference's module-level SAVE variables
 // (build/module.F90:101-176): one global plan set up by p3dfft_setup and torn
@@ -32,6 +34,11 @@ p3g_plan g_plan = nullptr;
 int g_comm = 0;
 int g_status = 0;
 bool g_abort = true;
+#ifdef STRIDE1
+int g_layout = P3G_LAYOUT_STRIDE1;
+#else
+int g_layout = P3G_LAYOUT_XYZ;
+#endif
 std::string g_msg;
 cudaStream_t g_stream = nullptr;
 void* g_stage[2] = {nullptr, nullptr};
@@ -125,6 +132,14 @@ int p3dfft_gb_status(void) { return g_status; }
 const char* p3dfft_gb_last_error(void) { return g_msg.c_str(); }
 void p3dfft_gb_set_abort(int on) { g_abort = on != 0; }
 
+void p3dfft_gb_set_layout(int layout) {
+  if (layout != P3G_LAYOUT_XYZ && layout != P3G_LAYOUT_STRIDE1)
+    return error(P3G_E_ARG, "P3DFFT error: unknown layout " + std::to_string(layout));
+  if (g_plan) return error(P3G_E_STATE, "P3DFFT error: the layout can only change before p3dfft_setup");
+  g_layout = layout;
+  g_status = 0;
+}
+
 // setup.F90:83-104,107-605 for a single rank.  memsize receives the padded
 // in-place size (setup.F90:579-603).
 void p3dfft_setup(int* dims, int* nx, int* ny, int* nz, int* comm, int* nxc, int* nyc, int* nzc, int* ow,
@@ -142,7 +157,7 @@ void p3dfft_setup(int* dims, int* nx, int* ny, int* nz, int* comm, int* nxc, int
     return error(P3G_E_ARG, "Invalid processor geometry: " + std::to_string(dims[0]) + " " +
                                 std::to_string(dims[1]) + " for 1 tasks");
   const int cx = nxc ? *nxc : *nx, cy = nyc ? *nyc : *ny, cz = nzc ? *nzc : *nz;
-  if (!check(p3g_plan_create(&g_plan, *nx, *ny, *nz, cx, cy, cz, kPrec, P3G_LAYOUT_XYZ, P3G_FLAG_TIMERS))) return;
+  if (!check(p3g_plan_create(&g_plan, *nx, *ny, *nz, cx, cy, cz, kPrec, g_layout, P3G_FLAG_TIMERS))) return;
   if (!g_stream) cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
   std::memset(g_timers, 0, sizeof(g_timers));
   g_comm = comm ? *comm : 0;

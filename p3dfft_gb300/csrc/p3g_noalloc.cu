@@ -84,6 +84,7 @@ int forward_passes(p3g_plan p, const void* in, void* out, int zi, bool fsign, vo
   // Y c2c: wa -> ybuf, y pruning on store
   {
     SParams s{};
+    s.in_xs = s.out_xs = 1;
     s.in = wa;
     s.out = ybuf;
     s.in_axis = P_;
@@ -111,6 +112,7 @@ int forward_passes(p3g_plan p, const void* in, void* out, int zi, bool fsign, vo
   {
     const AxisPlan& az = p->ax_z[zi];
     SParams s{};
+    s.in_xs = s.out_xs = 1;
     s.in = ybuf;
     s.out = out;
     s.out_user = 1;

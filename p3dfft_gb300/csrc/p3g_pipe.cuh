@@ -112,13 +112,13 @@ P3G_D void strided_issue(const SPipeParams& q, const CUtensorMap* tin, int tile,
     }
     return;
   }
-  const long long ib = (long long)o1 * s.in_o1 + (long long)o2 * s.in_o2 + (long long)xt * M;
+  const long long ib = (long long)o1 * s.in_o1 + (long long)o2 * s.in_o2 + (long long)xt * M * s.in_xs;
   const char* in = static_cast<const char*>(s.in);
   constexpr int esz = (int)sizeof(W);
   auto one = [&](int m, int j) {
     const int src = j >= s.lmap_a1 ? j - s.lmap_d : (j < s.lmap_a0 ? j : -1);
     const bool ok = src >= 0 && xt * M + m < s.X;
-    const char* g = ok ? in + (ib + m + (long long)src * s.in_axis) * esz : in;
+    const char* g = ok ? in + (ib + (long long)m * s.in_xs + (long long)src * s.in_axis) * esz : in;
     const uint32_t nb = ok ? (uint32_t)esz : 0u;
     int r0 = j, r1 = -1;
     if (s.pre == 2) {
@@ -144,7 +144,13 @@ P3G_D void strided_issue(const SPipeParams& q, const CUtensorMap* tin, int tile,
     }
   };
   const int T = blockDim.x;
-  if ((T & (M - 1)) == 0) {  // each thread keeps one column m: rows strided by T/M
+  if (s.in_xs != 1) {  // rows adjacent in memory (STRIDE1 user layout): rows fastest
+    const FastDiv div_l(L);
+    for (int e = threadIdx.x; e < M * L; e += T) {
+      const int m = (int)div_l.div(e);
+      one(m, e - m * L);
+    }
+  } else if ((T & (M - 1)) == 0) {  // each thread keeps one column m: rows strided by T/M
     const int m = threadIdx.x & (M - 1);
     for (int j = threadIdx.x >> s.log2m; j < L; j += T >> s.log2m) one(m, j);
   } else {
@@ -223,16 +229,22 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       int xt, o1, o2;
       strided_decode(q, tile, xt, o1, o2);
       const int x0 = xt * M;
-      const long long obase = (long long)o1 * s.out_o1 + (long long)o2 * s.out_o2 + x0;
+      const long long obase = (long long)o1 * s.out_o1 + (long long)o2 * s.out_o2 + (long long)x0 * s.out_xs;
       auto one = [&](int m, int jo) {
         const int k = jo < s.smap_s0 ? jo : jo + s.smap_d;
         C v;
         if (s.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
         else v = P::from_w(sm[k * M + m]);
-        store_elem<P>(s.out, s.out_user, obase + m + (long long)jo * s.out_axis, v);
+        store_elem<P>(s.out, s.out_user, obase + (long long)m * s.out_xs + (long long)jo * s.out_axis, v);
       };
       const int T = blockDim.x;
-      if ((T & (M - 1)) == 0) {
+      if (s.out_xs != 1) {  // rows adjacent in memory (STRIDE1 user layout): rows fastest
+        const FastDiv div_lo(s.Lout);
+        for (int e = threadIdx.x; e < M * s.Lout; e += T) {
+          const int m = (int)div_lo.div(e);
+          if (x0 + m < s.X) one(m, e - m * s.Lout);
+        }
+      } else if ((T & (M - 1)) == 0) {
         const int m = threadIdx.x & (M - 1);
         if (x0 + m < s.X)
           for (int jo = threadIdx.x >> s.log2m; jo < s.Lout; jo += T >> s.log2m) one(m, jo);

@@ -377,7 +377,7 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
     pp.chunk = esize;
     CUtensorMap map;
     std::memset(&map, 0, sizeof(map));
-    if (p->use_tma && s.pre <= 1 && s.lmap_a0 >= s.L && s.lmap_a1 >= s.L) {
+    if (p->use_tma && s.in_xs == 1 && s.pre <= 1 && s.lmap_a0 >= s.L && s.lmap_a1 >= s.L) {
       const int brows = pick_box_rows(s.L, ap.n, ap.M, esize);
       if (brows > 0 && encode_strided_map(&map, s.in, esize, s.X, s.L, s.O1, nv, s.in_axis, s.in_o1, s.in_o2, ap.M,
                                           brows)) {
@@ -467,7 +467,6 @@ int do_ftran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   const int zi = op_index(op[2], fsign, true);
   if (zi < 0) return fail(P3G_E_ARG, std::string("Unknown transform type: ") + op[2]);
   if (!p->z_ok[zi]) return fail(P3G_E_UNSUPPORTED, std::string("Z transform '") + op[2] + "' unsupported for nz");
-  if (p->layout == P3G_LAYOUT_STRIDE1) return fail(P3G_E_UNSUPPORTED, "STRIDE1 layout is not built yet");
   int rc = ensure_workspace(p, nv);
   if (rc) return rc;
   const long long P_ = p->pitch;
@@ -501,6 +500,7 @@ int do_ftran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   {
     PassTimer tm(p, 6, st);
     SParams s{};
+    s.in_xs = s.out_xs = 1;
     s.in = p->wa;
     s.out = ybuf;
     s.in_user = 0;
@@ -530,6 +530,7 @@ int do_ftran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   {
     PassTimer tm(p, 7, st);
     SParams s{};
+    s.in_xs = s.out_xs = 1;
     s.in = ybuf;
     s.out = out;
     s.in_user = 0;
@@ -537,8 +538,14 @@ int do_ftran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
     s.in_axis = (long long)p->nyc * P_;
     s.in_o1 = P_;
     s.in_o2 = y_field;
-    s.out_axis = (long long)p->nxhpc * p->nyc;
-    s.out_o1 = p->nxhpc;
+    if (p->layout == P3G_LAYOUT_STRIDE1) {  // (nzc, nyc, nxhpc), z fastest (module.F90:245-254)
+      s.out_axis = 1;
+      s.out_o1 = p->nzc;
+      s.out_xs = (long long)p->nyc * p->nzc;
+    } else {
+      s.out_axis = (long long)p->nxhpc * p->nyc;
+      s.out_o1 = p->nxhpc;
+    }
     s.out_o2 = dim_out;
     s.X = p->nxhpc;
     s.O1 = p->nyc;
@@ -567,7 +574,6 @@ int do_btran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   if (!p->z_ok[zi]) return fail(P3G_E_UNSUPPORTED, std::string("Z transform '") + op[0] + "' unsupported for nz");
   int rc = ensure_workspace(p, nv);
   if (rc) return rc;
-  if (p->layout == P3G_LAYOUT_STRIDE1) return fail(P3G_E_UNSUPPORTED, "STRIDE1 layout is not built yet");
   const long long P_ = p->pitch;
   const long long wa_field = (long long)p->nz * p->ny * P_;
   const long long wb_field = (long long)p->nz * p->nyc * P_;
@@ -577,12 +583,19 @@ int do_btran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   {
     PassTimer tm(p, 8, st);
     SParams s{};
+    s.in_xs = s.out_xs = 1;
     s.in = in;
     s.out = zbuf;
     s.in_user = 1;
     s.out_user = 0;
-    s.in_axis = (long long)p->nxhpc * p->nyc;
-    s.in_o1 = p->nxhpc;
+    if (p->layout == P3G_LAYOUT_STRIDE1) {
+      s.in_axis = 1;
+      s.in_o1 = p->nzc;
+      s.in_xs = (long long)p->nyc * p->nzc;
+    } else {
+      s.in_axis = (long long)p->nxhpc * p->nyc;
+      s.in_o1 = p->nxhpc;
+    }
     s.in_o2 = dim_in;
     s.out_axis = (long long)p->nyc * P_;
     s.out_o1 = P_;
@@ -606,6 +619,7 @@ int do_btran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   {
     PassTimer tm(p, 9, st);
     SParams s{};
+    s.in_xs = s.out_xs = 1;
     s.in = zbuf;
     s.out = p->wa;
     s.in_user = 0;

@@ -36,13 +36,14 @@ def _spectrum(shape, seed):
 MODES = {"pipe_tma": (True, True), "pipe_cpasync": (True, False), "single_tile": (False, False)}
 
 
-def _run_pair(torch, plan_args, a, op_f, op_b, precision, seed=0, mode="pipe_tma"):
+def _run_pair(torch, plan_args, a, op_f, op_b, precision, seed=0, mode="pipe_tma", stride1=False):
     import p3dfft_gb300 as pg
     nx, ny, nz = plan_args[:3]
     pruned = plan_args[3:] if len(plan_args) > 3 else (nx, ny, nz)
-    plan = pg.Plan(nx, ny, nz, *pruned, precision=precision)
+    plan = pg.Plan(nx, ny, nz, *pruned, precision=precision,
+                   layout=pg.LAYOUT_STRIDE1 if stride1 else pg.LAYOUT_XYZ)
     plan.set_options(*MODES[mode])
-    ref = orc.OraclePlan(nx, ny, nz, *pruned)
+    ref = orc.OraclePlan(nx, ny, nz, *pruned, stride1=stride1)
     rdt = torch.float64 if precision == pg.F64 else torch.float32
     x = torch.from_numpy(a).to("cuda", rdt)
     b = plan.ftran_r2c(x, op=op_f)
@@ -284,3 +285,66 @@ def test_unknown_op_is_an_error(torch_cuda):
     x = torch_cuda.zeros((8, 8, 8), dtype=torch_cuda.float64, device="cuda")
     with pytest.raises(pg.P3DFFTError, match="Unknown transform type"):
         plan.ftran_r2c(x, op="ffx")
+
+
+# ------------------------------------------------------------ STRIDE1 layout
+# (nzc, nyc, nxhpc) in Fortran order, z fastest (module.F90:245-254,
+# reorder.F90:359-488): the Z pass stores and loads with z adjacent.
+
+@pytest.mark.parametrize("mode", sorted(MODES))
+@pytest.mark.parametrize("case", [((32, 32, 32), "fft", "tff"), ((14, 26, 38), "fft", "tff"),
+                                  ((24, 20, 17), "ffc", "cff"), ((16, 12, 9), "ffs", "sff"),
+                                  ((16, 12, 10), "ffn", "nff"), ((64, 64, 64, 32, 32, 32), "fft", "tff"),
+                                  ((33, 20, 16, 20, 9, 10), "fft", "tff"), ((96, 80, 60), "fft", "tff")])
+def test_stride1_parity(torch_cuda, mode, case):
+    import p3dfft_gb300 as pg
+    args, op_f, op_b = case
+    a = _rand(args[:3][::-1], 23)
+    gb, wb, gr, wr = _run_pair(torch_cuda, args, a, op_f, op_b, pg.F64, mode=mode, stride1=True)
+    assert gb.shape == wb.shape
+    assert orc.normalised_linf(gb, wb) <= F64_TOL
+    assert orc.normalised_linf(gr, wr) <= F64_TOL
+
+
+@pytest.mark.parametrize("args", [(48, 64, 96), (30, 18, 17, 30, 9, 10)])
+def test_stride1_f32(torch_cuda, args):
+    import p3dfft_gb300 as pg
+    a = _rand(args[:3][::-1], 29)
+    gb, wb, gr, wr = _run_pair(torch_cuda, args, a, "fft", "tff", pg.F32, stride1=True)
+    assert orc.relative_l2(gb, wb) <= F32_TOL
+    assert orc.relative_l2(gr, wr) <= F32_TOL
+
+
+def test_stride1_cheby_and_dims(torch_cuda):
+    import p3dfft_gb300 as pg
+    torch = torch_cuda
+    nx, ny, nz = 16, 12, 17
+    plan = pg.Plan(nx, ny, nz, precision=pg.F64, layout=pg.LAYOUT_STRIDE1)
+    ref = orc.OraclePlan(nx, ny, nz, stride1=True)
+    assert plan.get_dims(2) == ref.get_dims(2)
+    z = np.cos(np.pi * np.arange(nz) / (nz - 1))
+    a = np.cos(2 * np.pi * np.arange(nx) / nx)[None, None, :] * z[:, None, None] ** 3 * np.ones((1, ny, 1))
+    got = plan.cheby(torch.from_numpy(a).cuda(), 2.0).cpu().numpy()
+    want = ref.cheby(a, 2.0)
+    plan.close()
+    assert got.shape == want.shape == (nx // 2 + 1, ny, nz)
+    assert orc.normalised_linf(got, want) <= F64_TOL
+
+
+def test_stride1_drop_in(torch_cuda):
+    import p3dfft_gb300 as pg
+    nx, ny, nz = 24, 16, 10
+    a = _rand((nz, ny, nx), 31)
+    pg.p3dfft_setup((1, 1), nx, ny, nz, stride1=True)
+    try:
+        s, e, sz = pg.p3dfft_get_dims(2)
+        assert sz == (nz, ny, nx // 2 + 1)
+        b = np.zeros((nx // 2 + 1, ny, nz), dtype=np.complex128)
+        pg.p3dfft_ftran_r2c(a, b, "fft")
+        r = np.zeros_like(a)
+        pg.p3dfft_btran_c2r(b, r, "tff")
+    finally:
+        pg.p3dfft_clean()
+    ref = orc.OraclePlan(nx, ny, nz, stride1=True)
+    assert orc.normalised_linf(b, ref.ftran_r2c(a, "fft")) <= F64_TOL
+    assert np.max(np.abs(r / (nx * ny * nz) - a)) <= orc.roundtrip_tolerance(nx * ny * nz)

@@ -209,6 +209,20 @@ def test_spectrum_of_sine_field():
     np.testing.assert_allclose(e, expect, atol=1e-14)
 
 
+@pytest.mark.parametrize("shape", [(16, 12, 10), (15, 9, 7)])
+def test_power_spectrum_parseval(shape):
+    # unit weights with the conjugate half counted: sum_k E(k) = sum |x|^2 / N
+    nx, ny, nz = shape
+    a = np.random.default_rng(2).uniform(-1, 1, size=(nz, ny, nx))
+    p = orc.OraclePlan(nx, ny, nz)
+    b = p.ftran_r2c(a, "fft") / (nx * ny * nz)
+    e = orc.shell_spectrum(b, nx, ny, nz, k2_weight=False, hermitian=True)
+    assert abs(e.sum() - np.sum(a * a) / (nx * ny * nz)) <= 1e-14
+    # a kmax below the largest shell drops the outer modes
+    e5 = orc.shell_spectrum(b, nx, ny, nz, k2_weight=False, hermitian=True, kmax=5)
+    np.testing.assert_allclose(e5, e[:6], rtol=0, atol=0)
+
+
 def test_invalid_inputs_raise():
     with pytest.raises(orc.OracleError):
         orc.OraclePlan(0, 4, 4)
