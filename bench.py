@@ -45,11 +45,11 @@ CONFIGS = {
 MODES = {"pipe_tma": (True, True), "pipe_cpasync": (True, False), "single_tile": (False, False)}
 
 # DRAM bytes (read + write) per algorithmic byte of one launch, from an ncu
-# capture of the strided Y pass on a 1024x1024x32 grid (272.75 MB read +
-# 217.33 MB written for 538.97 MB of 2C model traffic).  The
+# capture of the strided Y pass on a 1024x1024x32 grid (272.84 MB read +
+# 217.36 MB written for 538.97 MB of 2C model traffic).  The
 # full-size launch moves the same bytes per line, so traffic scales with the
 # model.
-TRAFFIC_PER_ALGO_BYTE = {"k_strided_pipe": (272.753152e6 + 217.333504e6) / 538968064.0}
+TRAFFIC_PER_ALGO_BYTE = {"k_strided_pipe": (272.841216e6 + 217.356544e6) / 538968064.0}
 
 
 def load_peaks():
