@@ -47,6 +47,13 @@ enum { P3G_FLAG_TIMERS = 1 };                     /* record per-pass CUDA-event 
  * allocated on the first transform call and grown for larger nv. */
 int p3g_plan_create(p3g_plan* plan, int nx, int ny, int nz, int nxc, int nyc, int nzc, int precision, int layout,
                     int flags);
+/* p3g_plan_create with the tuning knobs the batch autotuner searches (no
+ * counterpart in the reference, whose FFTW planner makes these choices):
+ * max_radix caps the power-of-two radix of the FFT stages (2, 4, 8, or 16 on
+ * the F32 path; 0 = 8 on F64, 16 on F32) and max_lines caps the lines per
+ * shared-memory tile (a power of two; 0 = no cap). */
+int p3g_plan_create_tuned(p3g_plan* plan, int nx, int ny, int nz, int nxc, int nyc, int nzc, int precision,
+                          int layout, int flags, int max_radix, int max_lines);
 int p3g_plan_destroy(p3g_plan plan);
 
 /* Bounds of the local arrays, as p3dfft_get_dims (reference
@@ -89,6 +96,49 @@ int p3g_cheby(p3g_plan plan, const void* in, void* out, double lz, int nv, long 
 enum { P3G_SPEC_K2 = 1, P3G_SPEC_HERMITIAN = 2 };
 int p3g_spectrum(p3g_plan plan, const void* in, double* E, int kmax, double scale, int flags, int nv,
                  long long dim_in, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Batches: many independent transforms of different sizes in one persistent
+ * launch (no counterpart in the reference, which transforms one grid per
+ * call).  Each job runs on its own plan (XYZ or STRIDE1 layout, pruning
+ * allowed, Z transform 'fft') with its own device work buffer of
+ * p3g_job_work_bytes(plan, kind) bytes:
+ *   P3G_JOB_ROUNDTRIP  in real -> forward -> (complex kept in work) ->
+ *                      backward -> out real (unnormalised, as the reference)
+ *   P3G_JOB_FORWARD    in real -> out complex
+ *   P3G_JOB_BACKWARD   in complex -> out real (in is not modified)
+ *   P3G_JOB_SPECTRUM   in real -> forward (complex kept in work) ->
+ *                      out double[kmax+1] shell spectrum (p3g_spectrum with
+ *                      kmax, scale, flags)
+ * p3g_batch_set_jobs builds the work queue (jobs in windows of `window`,
+ * pass-major inside a window; <= 0 = one window) and uploads it;
+ * p3g_batch_launch enqueues one launch on a stream; p3g_batch_capture
+ * records the launch as a CUDA graph that p3g_batch_replay launches.  The job
+ * arrays are bound at set_jobs time.  One precision per batch. */
+enum { P3G_JOB_ROUNDTRIP = 0, P3G_JOB_FORWARD = 1, P3G_JOB_BACKWARD = 2, P3G_JOB_SPECTRUM = 3 };
+typedef struct {
+  p3g_plan plan;
+  int kind;
+  int kmax;      /* spectrum: bins - 1 (<= 0 selects the sample's default) */
+  int flags;     /* spectrum: P3G_SPEC_* */
+  int reserved;
+  double scale;  /* spectrum: B is multiplied by scale before squaring */
+  const void* in;
+  void* out;
+  void* work;
+} p3g_job;
+typedef struct p3g_batch_s* p3g_batch;
+long long p3g_job_work_bytes(p3g_plan plan, int kind);
+int p3g_batch_create(p3g_batch* batch, int precision);
+int p3g_batch_set_jobs(p3g_batch batch, int njobs, const p3g_job* jobs, int window);
+int p3g_batch_launch(p3g_batch batch, void* stream);
+int p3g_batch_capture(p3g_batch batch);
+int p3g_batch_replay(p3g_batch batch, void* stream);
+/* Synchronises the stream and reports a timed-out dependency wait. */
+int p3g_batch_status(p3g_batch batch, void* stream);
+/* info = {passes, work items, persistent CTAs, launches so far} */
+int p3g_batch_info(p3g_batch batch, long long info[4]);
+int p3g_batch_destroy(p3g_batch batch);
 
 /* The reference's 12 accumulating stage timers (build/module.F90:106,709-744),
  * in seconds: slot 5 X r2c, 7 Y forward, 8 Z forward, 9 Z backward,

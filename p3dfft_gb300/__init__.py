@@ -34,6 +34,10 @@ LAYOUT_XYZ = 0
 LAYOUT_STRIDE1 = 1
 SPEC_K2 = 1
 SPEC_HERMITIAN = 2
+JOB_ROUNDTRIP = 0
+JOB_FORWARD = 1
+JOB_BACKWARD = 2
+JOB_SPECTRUM = 3
 FLAG_TIMERS = 1
 
 
@@ -77,7 +81,8 @@ class Plan:
     complex (nzc, nyc, nxc//2+1) complex128/complex64 (or float views).
     """
 
-    def __init__(self, nx, ny, nz, nxc=None, nyc=None, nzc=None, precision=F64, layout=LAYOUT_XYZ, timers=False):
+    def __init__(self, nx, ny, nz, nxc=None, nyc=None, nzc=None, precision=F64, layout=LAYOUT_XYZ, timers=False,
+                 max_radix=0, max_lines=0):
         self._h = ctypes.c_void_p()
         self.nx, self.ny, self.nz = nx, ny, nz
         self.nxc = nxc or nx
@@ -85,8 +90,17 @@ class Plan:
         self.nzc = nzc or nz
         self.precision = precision
         self.layout = layout
-        _check(_core().p3g_plan_create(ctypes.byref(self._h), nx, ny, nz, self.nxc, self.nyc, self.nzc,
-                                       precision, layout, FLAG_TIMERS if timers else 0))
+        self.tuning = (int(max_radix), int(max_lines))
+        _check(_core().p3g_plan_create_tuned(ctypes.byref(self._h), nx, ny, nz, self.nxc, self.nyc, self.nzc,
+                                             precision, layout, FLAG_TIMERS if timers else 0, int(max_radix),
+                                             int(max_lines)))
+
+    def work_bytes(self, kind) -> int:
+        """Device work buffer a batch job of this kind needs (p3g_job_work_bytes)."""
+        n = _core().p3g_job_work_bytes(self._h, int(kind))
+        if n < 0:
+            _check(-1)
+        return n
 
     @property
     def real_shape(self):
@@ -178,6 +192,74 @@ class Plan:
         if self._h:
             _core().p3g_plan_destroy(self._h)
             self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent transforms in one persistent launch (p3g_batch_*).
+
+    ``jobs`` is a list of dicts with keys plan (a Plan of this batch's
+    precision), kind (JOB_*), in, out (CUDA tensors) and optionally kmax,
+    scale, flags (spectrum jobs) and work (a uint8 CUDA tensor of at least
+    plan.work_bytes(kind) bytes; allocated here when absent).  The tensors
+    are bound until the next set_jobs.
+    """
+
+    def __init__(self, precision=F64):
+        self.precision = precision
+        self._h = ctypes.c_void_p()
+        _check(_core().p3g_batch_create(ctypes.byref(self._h), precision))
+        self._keep = []
+
+    def set_jobs(self, jobs, window=0):
+        import torch
+        arr = (_lib.Job * len(jobs))()
+        keep = []
+        for i, j in enumerate(jobs):
+            plan = j["plan"]
+            work = j.get("work")
+            if work is None:
+                work = torch.empty(plan.work_bytes(j["kind"]), dtype=torch.uint8, device=j["in"].device)
+            keep += [plan, j["in"], j["out"], work]
+            arr[i].plan = plan._h.value
+            arr[i].kind = int(j["kind"])
+            arr[i].kmax = int(j.get("kmax", 0))
+            arr[i].flags = int(j.get("flags", SPEC_K2))
+            arr[i].scale = float(j.get("scale", 1.0))
+            arr[i].in_ = _ptr(j["in"])
+            arr[i].out = _ptr(j["out"])
+            arr[i].work = _ptr(work)
+        _check(_core().p3g_batch_set_jobs(self._h, len(jobs), arr, int(window)))
+        self._keep = keep
+        return self
+
+    def launch(self, stream=None):
+        _check(_core().p3g_batch_launch(self._h, _stream_ptr(stream)))
+
+    def capture(self):
+        _check(_core().p3g_batch_capture(self._h))
+
+    def replay(self, stream=None):
+        _check(_core().p3g_batch_replay(self._h, _stream_ptr(stream)))
+
+    def check(self, stream=None):
+        _check(_core().p3g_batch_status(self._h, _stream_ptr(stream)))
+
+    def info(self):
+        a = (ctypes.c_longlong * 4)()
+        _check(_core().p3g_batch_info(self._h, a))
+        return {"passes": a[0], "items": a[1], "ctas": a[2], "launches": a[3]}
+
+    def close(self):
+        if self._h:
+            _core().p3g_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+        self._keep = []
 
     def __del__(self):
         try:

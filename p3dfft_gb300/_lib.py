@@ -9,6 +9,13 @@ from . import build as _build
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 _c_double_p = ctypes.POINTER(ctypes.c_double)
 
+class Job(ctypes.Structure):
+    """p3g_job (include/p3dfft_gb300.h)."""
+    _fields_ = [("plan", ctypes.c_void_p), ("kind", ctypes.c_int), ("kmax", ctypes.c_int),
+                ("flags", ctypes.c_int), ("reserved", ctypes.c_int), ("scale", ctypes.c_double),
+                ("in_", ctypes.c_void_p), ("out", ctypes.c_void_p), ("work", ctypes.c_void_p)]
+
+
 # explicit device API (include/p3dfft_gb300.h)
 CORE_SIGNATURES = {
     "p3g_plan_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -29,6 +36,18 @@ CORE_SIGNATURES = {
     "p3g_ftran_r2c_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
                                              ctypes.c_void_p]),
     "p3g_plan_status": (ctypes.c_int, [ctypes.c_void_p]),
+    "p3g_plan_create_tuned": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "p3g_job_work_bytes": (ctypes.c_longlong, [ctypes.c_void_p, ctypes.c_int]),
+    "p3g_batch_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
+    "p3g_batch_set_jobs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Job), ctypes.c_int]),
+    "p3g_batch_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "p3g_batch_capture": (ctypes.c_int, [ctypes.c_void_p]),
+    "p3g_batch_replay": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "p3g_batch_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "p3g_batch_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "p3g_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "p3g_spectrum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
                                     ctypes.c_int, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p]),
     "p3g_plan_set_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),

@@ -1,0 +1,494 @@
+// Batches of independent transforms in one persistent launch: p3g_batch_*.
+//
+// A batch holds a list of jobs (forward, backward, round trip, or forward +
+// shell spectrum), each on its own plan (any sizes, one precision per batch)
+// and its own device workspace.  Every job is a chain of passes (X, Y, Z
+// forward; Z, Y, X backward; spectrum), every pass a set of tiles, and every
+// tile one work item of a single queue.  One persistent kernel (grid = SMs x
+// resident CTAs) takes items in queue order with an atomic ticket; an item
+// whose pass depends on the job's previous pass waits (bounded) until all
+// tiles of that pass have been counted done.  Items are taken in queue
+// order and every dependency points to an earlier item, which a running CTA
+// already holds, so the launch makes progress whether or not all CTAs are
+// resident.
+//
+// Queue order (the schedule): jobs in windows of `window` jobs; inside a
+// window pass-major (every job's X pass, then every job's Y pass, ...).  A
+// small window keeps a job's passes close together in time, so the data of a
+// small grid is still in the 129 MB L2 when its next pass reads it; a large
+// window gives each pass more parallel tiles.  The autotuner picks it.
+//
+// Visibility between CTAs: each thread fences after its stores, then the CTA
+// barrier, then one atomic increment of the pass counter; the waiting CTA's
+// thread 0 polls the counter with ld.acquire.gpu and fences; the CTA then
+// reads the data through L2 only (ld.global.cg), so no stale L1 line from an
+// earlier pass is seen.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "p3g_kernels_impl.cuh"
+#include "p3g_plan_internal.h"
+#include "p3g_spectrum.cuh"
+
+namespace p3g {
+namespace {
+
+enum BatchKind { kBXr2c = 0, kBFwd = 1, kBBwd = 2, kBXc2r = 3, kBSpec = 4, kBZero = 5 };
+
+struct BatchPass {
+  int kind;
+  int tiles;   // work items of the pass
+  int first;   // queue index of its first item
+  int dep;     // pass that must be complete first, -1 = none
+  int rows_per_item;  // spectrum passes
+  int pad_;
+  const StagePlan* sp;
+  const float4* tw;
+  XParams x;
+  SParams s;
+  SpecParams spec;
+};
+
+constexpr int kBatchSpinLimit = 1 << 22;  // polls of ~1 us: about 4 s
+
+P3G_D int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+P3G_D int ld_relaxed(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Waits until *cnt >= need.  false when the launch recorded an error or the
+// wait ran out (then it records error 2).
+P3G_D bool wait_count(const int* cnt, int need, int* err) {
+  for (int polls = 0;; ++polls) {
+    if (ld_acquire(cnt) >= need) {
+      __threadfence();
+      return true;
+    }
+    if (ld_relaxed(err) != 0) return false;
+    if (polls >= kBatchSpinLimit) {
+      atomicExch(err, 2);
+      return false;
+    }
+    __nanosleep(polls < 32 ? 64 : 1000);
+  }
+}
+
+// ctl[0] = next queue item, ctl[1] = error, ctl[2 + d] = finished tiles of pass d
+template <class P>
+__global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
+    k_batch(const BatchPass* __restrict__ passes, int npass, int nitems, int* __restrict__ ctl) {
+  using W = typename P::W;
+  __shared__ int s_item, s_pass;
+  W* sm = reinterpret_cast<W*>(p3g_smem);
+  for (;;) {
+    if (threadIdx.x == 0) {
+      int d = -1;
+      const int it = atomicAdd(&ctl[0], 1);
+      if (it < nitems && ld_relaxed(&ctl[1]) == 0) {
+        int lo = 0, hi = npass - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (passes[mid].first <= it) lo = mid;
+          else hi = mid - 1;
+        }
+        d = lo;
+        const int dep = passes[d].dep;
+        if (dep >= 0 && !wait_count(&ctl[2 + dep], passes[dep].tiles, &ctl[1])) d = -1;
+      }
+      s_item = it;
+      s_pass = d;
+    }
+    __syncthreads();
+    const int d = s_pass;
+    if (d < 0) break;
+    const BatchPass& bp = passes[d];
+    const int tile = s_item - bp.first;
+    switch (bp.kind) {
+      case kBXr2c: x_r2c_tile<P, true>(bp.x, bp.sp, bp.tw, sm, tile, 0); break;
+      case kBFwd: strided_tile<P, -1, true>(bp.s, bp.sp, bp.tw, sm, tile); break;
+      case kBBwd: strided_tile<P, 1, true>(bp.s, bp.sp, bp.tw, sm, tile); break;
+      case kBXc2r: x_c2r_tile<P, true>(bp.x, bp.sp, bp.tw, sm, tile, 0); break;
+      case kBSpec: {
+        double* hist = reinterpret_cast<double*>(p3g_smem);
+        const int nwarps = blockDim.x >> 5;
+        for (int i = threadIdx.x; i < nwarps * (bp.spec.kmax + 1); i += blockDim.x) hist[i] = 0.0;
+        __syncthreads();
+        const int r0 = tile * bp.rows_per_item;
+        const int r1 = min(r0 + bp.rows_per_item, bp.spec.rows);
+        spectrum_rows<P, true>(bp.spec, hist, r0 + (int)(threadIdx.x >> 5), r1, nwarps, 0);
+        __syncthreads();
+        spectrum_flush(bp.spec, hist, nwarps, 0);
+        break;
+      }
+      case kBZero:
+        for (int i = threadIdx.x; i <= bp.spec.kmax; i += blockDim.x) bp.spec.E[i] = 0.0;
+        break;
+      default: break;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(&ctl[2 + d], 1);
+  }
+}
+
+// Opts the kernel in to the largest dynamic shared memory the device allows
+// next to its static shared variables (once per path), then reads the
+// occupancy for this batch's tile size.
+template <class P>
+cudaError_t batch_config(size_t smem, int& threads, int& per_sm, size_t& max_dyn) {
+  threads = PathLimits<P>::kMaxThreads;
+  static size_t s_max_dyn = 0;
+  cudaError_t e = cudaSuccess;
+  if (!s_max_dyn) {
+    cudaFuncAttributes fa{};
+    int dev = 0, optin = 0;
+    e = cudaFuncGetAttributes(&fa, k_batch<P>);
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    const size_t dyn = (size_t)optin - fa.sharedSizeBytes;
+    e = cudaFuncSetAttribute(k_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+    s_max_dyn = dyn;
+  }
+  max_dyn = s_max_dyn;
+  if (smem > max_dyn) return cudaErrorInvalidValue;
+  per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<P>, threads, smem);
+  if (e == cudaSuccess && per_sm < 1) per_sm = 1;
+  return e;
+}
+
+template <class P>
+cudaError_t batch_launch(const BatchPass* d_pass, int npass, int nitems, int* ctl, int grid, int threads,
+                         size_t smem, cudaStream_t st) {
+  k_batch<P><<<grid, threads, smem, st>>>(d_pass, npass, nitems, ctl);
+  return cudaGetLastError();
+}
+
+size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+
+// Workspace of one job inside its work buffer: wa | wb (Y pruning) | complex
+// field (round trip and spectrum jobs).
+struct JobLayout {
+  size_t wa, wb, cplx, total;
+};
+JobLayout job_layout(p3g_plan p, int kind) {
+  JobLayout l{};
+  const size_t es = p->esize();
+  l.wa = round256((size_t)p->nz * p->ny * p->pitch * es);
+  l.wb = p->nyc < p->ny ? round256((size_t)p->nz * p->nyc * p->pitch * es) : 0;
+  l.cplx = (kind == P3G_JOB_ROUNDTRIP || kind == P3G_JOB_SPECTRUM)
+               ? round256((size_t)p->nxhpc * p->nyc * p->nzc * es)
+               : 0;
+  l.total = l.wa + l.wb + l.cplx;
+  return l;
+}
+
+}  // namespace
+}  // namespace p3g
+
+using namespace p3g;
+
+struct p3g_batch_s {
+  int prec = P3G_F64;
+  int sm_count = 0;
+  std::vector<BatchPass> host;
+  BatchPass* d_pass = nullptr;
+  size_t pass_cap = 0;
+  int* d_ctl = nullptr;
+  size_t ctl_cap = 0;
+  int npass = 0, nitems = 0;
+  size_t smem = 0;
+  int threads = 0, grid = 0;
+  cudaStream_t upload = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  long long launches = 0;
+  std::mutex mu;
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+};
+
+extern "C" {
+
+long long p3g_job_work_bytes(p3g_plan plan, int kind) {
+  if (!plan || kind < P3G_JOB_ROUNDTRIP || kind > P3G_JOB_SPECTRUM) {
+    fail(P3G_E_ARG, "invalid plan or job kind");
+    return -1;
+  }
+  return (long long)job_layout(plan, kind).total;
+}
+
+int p3g_batch_create(p3g_batch* out, int precision) {
+  if (!out) return fail(P3G_E_ARG, "batch pointer is NULL");
+  *out = nullptr;
+  if (precision != P3G_F64 && precision != P3G_F32) return fail(P3G_E_ARG, "unknown precision");
+  auto* b = new p3g_batch_s();
+  b->prec = precision;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->upload, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete b;
+    return fail(P3G_E_CUDA, std::string("batch create: ") + cudaGetErrorString(e));
+  }
+  *out = b;
+  return P3G_OK;
+}
+
+int p3g_batch_destroy(p3g_batch b) {
+  if (!b) return P3G_OK;
+  b->drop_graph();
+  if (b->d_pass) cudaFree(b->d_pass);
+  if (b->d_ctl) cudaFree(b->d_ctl);
+  if (b->upload) cudaStreamDestroy(b->upload);
+  delete b;
+  return P3G_OK;
+}
+
+int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) {
+  if (!b) return fail(P3G_E_STATE, "batch is NULL");
+  if (njobs <= 0 || !jobs) return fail(P3G_E_ARG, "no jobs");
+  if (window <= 0) window = njobs;
+  std::lock_guard<std::mutex> lk(b->mu);
+  const bool f64 = b->prec == P3G_F64;
+  const int threads = f64 ? PathLimits<PathF64>::kMaxThreads : PathLimits<PathF32>::kMaxThreads;
+  const int nwarps = threads / 32;
+  // per job: its chain of passes
+  std::vector<std::vector<BatchPass>> chains(njobs);
+  size_t smem = 0;
+  for (int j = 0; j < njobs; ++j) {
+    const p3g_job& jb = jobs[j];
+    p3g_plan p = jb.plan;
+    const std::string who = "job " + std::to_string(j) + ": ";
+    if (!p) return fail(P3G_E_ARG, who + "plan is NULL");
+    if (p->prec != b->prec) return fail(P3G_E_ARG, who + "plan precision differs from the batch's");
+    if (jb.kind < P3G_JOB_ROUNDTRIP || jb.kind > P3G_JOB_SPECTRUM) return fail(P3G_E_ARG, who + "unknown kind");
+    if (!jb.in || !jb.out || !jb.work) return fail(P3G_E_ARG, who + "NULL array");
+    if (!p->z_ok[0]) return fail(P3G_E_UNSUPPORTED, who + "Z FFT unsupported for nz");
+    const JobLayout L = job_layout(p, jb.kind);
+    unsigned char* w = static_cast<unsigned char*>(jb.work);
+    void* wa = w;
+    void* wb = L.wb ? w + L.wa : nullptr;
+    void* cplx = L.cplx ? w + L.wa + L.wb : nullptr;
+    const StagePlan* dsp = p->d_sp;
+    auto x_pass = [&](int kind, const XParams& x) {
+      BatchPass q{};
+      q.kind = kind;
+      q.x = x;
+      q.tiles = x.tiles;
+      q.sp = dsp + p->ax_x.sp_index;
+      q.tw = p->d_tw;
+      smem = std::max(smem, p->ax_x.smem);
+      chains[j].push_back(q);
+    };
+    auto s_pass = [&](int kind, const SParams& s, const AxisPlan& ap) {
+      BatchPass q{};
+      q.kind = kind;
+      q.s = s;
+      q.tiles = s.xtiles * s.O1;
+      q.sp = dsp + ap.sp_index;
+      q.tw = p->d_tw;
+      smem = std::max(smem, ap.smem);
+      chains[j].push_back(q);
+    };
+    const long long rsize = (long long)p->nx * p->ny * p->nz;
+    const long long csize = (long long)p->nxhpc * p->nyc * p->nzc;
+    if (jb.kind == P3G_JOB_SPECTRUM) {
+      SpecParams sp;
+      int rc = make_spectrum_params(p, cplx, static_cast<double*>(jb.out), jb.kmax, jb.scale, jb.flags, csize, sp);
+      if (rc) return rc;
+      BatchPass q{};
+      q.kind = kBZero;
+      q.spec = sp;
+      q.tiles = 1;
+      chains[j].push_back(q);
+    }
+    if (jb.kind != P3G_JOB_BACKWARD) {
+      XParams x;
+      SParams y, z;
+      void* fout = jb.kind == P3G_JOB_FORWARD ? jb.out : cplx;
+      make_forward_params(p, jb.in, fout, wa, wb, 0, rsize, csize, x, y, z);
+      x_pass(kBXr2c, x);
+      s_pass(kBFwd, y, p->ax_y);
+      s_pass(kBFwd, z, p->ax_z[0]);
+    }
+    if (jb.kind == P3G_JOB_ROUNDTRIP || jb.kind == P3G_JOB_BACKWARD) {
+      SParams z, y;
+      XParams x;
+      const void* bin = jb.kind == P3G_JOB_BACKWARD ? jb.in : cplx;
+      make_backward_params(p, bin, jb.out, wa, wb, 0, csize, rsize, z, y, x);
+      s_pass(kBBwd, z, p->ax_z[0]);
+      s_pass(kBBwd, y, p->ax_y);
+      x_pass(kBXc2r, x);
+    }
+    if (jb.kind == P3G_JOB_SPECTRUM) {
+      BatchPass q = chains[j][0];
+      q.kind = kBSpec;
+      q.rows_per_item = nwarps * 4;
+      q.tiles = (q.spec.rows + q.rows_per_item - 1) / q.rows_per_item;
+      smem = std::max(smem, (size_t)nwarps * (q.spec.kmax + 1) * sizeof(double));
+      chains[j].push_back(q);
+    }
+  }
+  if (smem > 227 * 1024) return fail(P3G_E_UNSUPPORTED, "a job's tile exceeds shared memory");
+  // queue: windows of jobs, pass-major inside a window
+  std::vector<BatchPass> table;
+  std::vector<int> last(njobs, -1);
+  long long items = 0;
+  for (int w0 = 0; w0 < njobs; w0 += window) {
+    const int w1 = std::min(njobs, w0 + window);
+    size_t depth = 0;
+    for (int j = w0; j < w1; ++j) depth = std::max(depth, chains[j].size());
+    for (size_t s = 0; s < depth; ++s)
+      for (int j = w0; j < w1; ++j) {
+        if (s >= chains[j].size()) continue;
+        BatchPass q = chains[j][s];
+        q.dep = last[j];
+        q.first = (int)items;
+        items += q.tiles;
+        last[j] = (int)table.size();
+        table.push_back(q);
+      }
+  }
+  if (items > 0x7FFFFFF0LL) return fail(P3G_E_UNSUPPORTED, "too many work items");
+  int per_sm = 1, thr = threads;
+  size_t max_dyn = 0;
+  cudaError_t e = f64 ? batch_config<PathF64>(smem, thr, per_sm, max_dyn)
+                      : batch_config<PathF32>(smem, thr, per_sm, max_dyn);
+  if (e != cudaSuccess && smem > max_dyn && max_dyn > 0)
+    return fail(P3G_E_UNSUPPORTED, "a job's tile needs " + std::to_string(smem) + " bytes of shared memory, above " +
+                                       std::to_string(max_dyn));
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch kernel attributes: ") + cudaGetErrorString(e));
+  const size_t pass_bytes = table.size() * sizeof(BatchPass);
+  const size_t ctl_bytes = (2 + table.size()) * sizeof(int);
+  b->drop_graph();
+  if (pass_bytes > b->pass_cap) {
+    if (b->d_pass) cudaFree(b->d_pass);
+    b->d_pass = nullptr;
+    b->pass_cap = 0;
+    if (cudaMalloc(&b->d_pass, pass_bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(P3G_E_NOMEM, "batch table allocation failed");
+    }
+    b->pass_cap = pass_bytes;
+  }
+  if (ctl_bytes > b->ctl_cap) {
+    if (b->d_ctl) cudaFree(b->d_ctl);
+    b->d_ctl = nullptr;
+    b->ctl_cap = 0;
+    if (cudaMalloc(&b->d_ctl, ctl_bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(P3G_E_NOMEM, "batch counter allocation failed");
+    }
+    b->ctl_cap = ctl_bytes;
+  }
+  e = cudaMemcpyAsync(b->d_pass, table.data(), pass_bytes, cudaMemcpyHostToDevice, b->upload);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_ctl, 0, ctl_bytes, b->upload);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->upload);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch table upload: ") + cudaGetErrorString(e));
+  b->host = std::move(table);
+  b->npass = (int)b->host.size();
+  b->nitems = (int)items;
+  b->smem = smem;
+  b->threads = thr;
+  const long long slots = (long long)b->sm_count * per_sm;
+  b->grid = (int)std::max(1LL, std::min(slots, items));
+  return P3G_OK;
+}
+
+static int batch_enqueue(p3g_batch b, cudaStream_t st) {
+  const size_t ctl_bytes = (2 + (size_t)b->npass) * sizeof(int);
+  cudaError_t e = cudaMemsetAsync(b->d_ctl, 0, ctl_bytes, st);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch clear: ") + cudaGetErrorString(e));
+  e = b->prec == P3G_F64
+          ? batch_launch<PathF64>(b->d_pass, b->npass, b->nitems, b->d_ctl, b->grid, b->threads, b->smem, st)
+          : batch_launch<PathF32>(b->d_pass, b->npass, b->nitems, b->d_ctl, b->grid, b->threads, b->smem, st);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+  return P3G_OK;
+}
+
+int p3g_batch_launch(p3g_batch b, void* stream) {
+  if (!b || b->nitems == 0) return fail(P3G_E_STATE, "batch has no jobs");
+  std::lock_guard<std::mutex> lk(b->mu);
+  int rc = batch_enqueue(b, static_cast<cudaStream_t>(stream));
+  if (rc == P3G_OK) b->launches++;
+  return rc;
+}
+
+int p3g_batch_capture(p3g_batch b) {
+  if (!b || b->nitems == 0) return fail(P3G_E_STATE, "batch has no jobs");
+  std::lock_guard<std::mutex> lk(b->mu);
+  b->drop_graph();
+  cudaStream_t cs = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("capture stream: ") + cudaGetErrorString(e));
+  e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  int rc = P3G_OK;
+  if (e == cudaSuccess) {
+    rc = batch_enqueue(b, cs);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(cs, &g);
+    if (e == cudaSuccess && rc == P3G_OK) {
+      b->graph = g;
+      e = cudaGraphInstantiate(&b->exec, g, 0);
+    } else if (g) {
+      cudaGraphDestroy(g);
+    }
+  }
+  cudaStreamDestroy(cs);
+  if (rc) return rc;
+  if (e != cudaSuccess) {
+    b->drop_graph();
+    return fail(P3G_E_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));
+  }
+  return P3G_OK;
+}
+
+int p3g_batch_replay(p3g_batch b, void* stream) {
+  if (!b || !b->exec) return fail(P3G_E_STATE, "batch has no captured graph");
+  std::lock_guard<std::mutex> lk(b->mu);
+  cudaError_t e = cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+  b->launches++;
+  return P3G_OK;
+}
+
+int p3g_batch_status(p3g_batch b, void* stream) {
+  if (!b) return fail(P3G_E_STATE, "batch is NULL");
+  cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch: ") + cudaGetErrorString(e));
+  if (!b->d_ctl) return P3G_OK;
+  int err = 0;
+  e = cudaMemcpy(&err, b->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch status: ") + cudaGetErrorString(e));
+  if (err) return fail(P3G_E_CUDA, "batch kernel: a dependency wait timed out");
+  return P3G_OK;
+}
+
+int p3g_batch_info(p3g_batch b, long long info[4]) {
+  if (!b) return fail(P3G_E_STATE, "batch is NULL");
+  info[0] = b->npass;
+  info[1] = b->nitems;
+  info[2] = b->grid;
+  info[3] = b->launches;
+  return P3G_OK;
+}
+
+}  // extern "C"

@@ -58,10 +58,18 @@ struct ChebyParams {
   float l_hi, l_lo;    // 4/Lz as double-float
 };
 
-template <class P>
+// Global loads.  CG = true reads through L2 only (ld.global.cg): the batch
+// kernel reads, within one launch, data that other CTAs wrote after this SM
+// may already have cached the same lines in L1.
+template <bool CG, class T>
+P3G_D T gload(const T* p) {
+  if constexpr (CG) return __ldcg(p);
+  else return *p;
+}
+template <class P, bool CG = false>
 P3G_D typename P::C load_elem(const void* base, int user, long long idx) {
-  if (user) return P::from_uc(static_cast<const typename P::UC*>(base)[idx]);
-  return P::from_w(static_cast<const typename P::W*>(base)[idx]);
+  if (user) return P::from_uc(gload<CG>(static_cast<const typename P::UC*>(base) + idx));
+  return P::from_w(gload<CG>(static_cast<const typename P::W*>(base) + idx));
 }
 template <class P>
 P3G_D void store_elem(void* base, int user, long long idx, typename P::C v) {

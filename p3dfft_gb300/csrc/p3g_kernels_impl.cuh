@@ -23,16 +23,15 @@ struct PathLimits<PathF32> {
 // ---------------------------------------------------------------- X r2c
 // Real lines 2p and 2p+1 form z = x1 + i x2; Z = FFT(z);
 // X1[k] = (Z[k] + conj Z[N-k]) / 2, X2[k] = -i (Z[k] - conj Z[N-k]) / 2.
-template <class P>
-__global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
-    k_x_r2c(const XParams prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw) {
+// One tile (M line pairs) of field `field`; sm = the tile's shared memory.
+template <class P, bool CG>
+P3G_D void x_r2c_tile(const XParams& prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw,
+                      typename P::W* sm, int tile, int field) {
   using W = typename P::W;
   using C = typename P::C;
-  W* sm = reinterpret_cast<W*>(p3g_smem);
   const int N = prm.nx;
   const int M = prm.M;
-  const int field = blockIdx.y;
-  const int p0 = blockIdx.x * M;  // first pair of the tile
+  const int p0 = tile * M;  // first pair of the tile
   const auto* in = static_cast<const typename P::UR*>(prm.in) + field * prm.in_field;
   W* out = static_cast<W*>(prm.out) + field * prm.out_field;
 
@@ -46,11 +45,11 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
     const int c = lt & 1;
     float* f = smf + ((lt >> 1) * LS + pad_index(x, ps)) * kW;
     if constexpr (P::kF64) {
-      const df v = line < prm.nlines ? P::from_ur(in[(long long)line * prm.in_line + x]) : df{0.f, 0.f};
+      const df v = line < prm.nlines ? P::from_ur(gload<CG>(in + (long long)line * prm.in_line + x)) : df{0.f, 0.f};
       f[c] = v.hi;
       f[2 + c] = v.lo;
     } else {
-      f[c] = line < prm.nlines ? in[(long long)line * prm.in_line + x] : 0.0f;
+      f[c] = line < prm.nlines ? gload<CG>(in + (long long)line * prm.in_line + x) : 0.0f;
     }
   }
   __syncthreads();
@@ -69,20 +68,24 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
   }
 }
 
+template <class P>
+__global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
+    k_x_r2c(const XParams prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw) {
+  x_r2c_tile<P, false>(prm, sp, tw, reinterpret_cast<typename P::W*>(p3g_smem), blockIdx.x, blockIdx.y);
+}
+
 // ---------------------------------------------------------------- X c2r
 // Z[k] = X1[k] + i X2[k] (k <= N/2, imaginary parts of DC and Nyquist
 // dropped as FFTW's c2r does), Z[N-k] = conj X1[k] + i conj X2[k];
 // z = IFFT(Z) (unnormalised) gives x1 = Re z, x2 = Im z.
-template <class P>
-__global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
-    k_x_c2r(const XParams prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw) {
+template <class P, bool CG>
+P3G_D void x_c2r_tile(const XParams& prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw,
+                      typename P::W* sm, int tile, int field) {
   using W = typename P::W;
   using C = typename P::C;
-  W* sm = reinterpret_cast<W*>(p3g_smem);
   const int N = prm.nx;
   const int M = prm.M;
-  const int field = blockIdx.y;
-  const int p0 = blockIdx.x * M;
+  const int p0 = tile * M;
   const W* in = static_cast<const W*>(prm.in) + field * prm.in_field;
   auto* out = static_cast<typename P::UR*>(prm.out) + field * prm.out_field;
   const int nh = N / 2 + 1;
@@ -93,8 +96,8 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
     const int line = 2 * (p0 + pr);
     C x1 = P::zero(), x2 = P::zero();
     if (k < prm.nkeep) {
-      if (line < prm.nlines) x1 = P::from_w(in[(long long)line * prm.in_line + k]);
-      if (line + 1 < prm.nlines) x2 = P::from_w(in[(long long)(line + 1) * prm.in_line + k]);
+      if (line < prm.nlines) x1 = P::from_w(gload<CG>(in + (long long)line * prm.in_line + k));
+      if (line + 1 < prm.nlines) x2 = P::from_w(gload<CG>(in + (long long)(line + 1) * prm.in_line + k));
     }
     if (k == 0 || 2 * k == N) {
       x1 = P::make(P::re(x1), P::re(P::zero()));
@@ -123,18 +126,23 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
   }
 }
 
+template <class P>
+__global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
+    k_x_c2r(const XParams prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw) {
+  x_c2r_tile<P, false>(prm, sp, tw, reinterpret_cast<typename P::W*>(p3g_smem), blockIdx.x, blockIdx.y);
+}
+
 // ------------------------------------------------------------- strided Y/Z
 
-template <class P, int DIR>
-__global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
-    k_strided(const SParams prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw) {
+// One tile (M columns x L rows); `bid` enumerates (x tile, o1, o2 = field).
+template <class P, int DIR, bool CG>
+P3G_D void strided_tile(const SParams& prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw,
+                        typename P::W* sm, long long bid) {
   using W = typename P::W;
   using C = typename P::C;
-  W* sm = reinterpret_cast<W*>(p3g_smem);
   const int M = prm.M;
   const int N = prm.N;
   const int L = prm.L;
-  long long bid = blockIdx.x;
   const int xt = (int)(bid % prm.xtiles);
   bid /= prm.xtiles;
   const int o1 = (int)(bid % prm.O1);
@@ -163,7 +171,7 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
     const int src = j >= prm.lmap_a1 ? j - prm.lmap_d : (j < prm.lmap_a0 ? j : -1);
     C v = P::zero();
     if (x0 + m < prm.X && src >= 0)
-      v = load_elem<P>(prm.in, prm.in_user, ibase + m * prm.in_xs + src * prm.in_axis);
+      v = load_elem<P, CG>(prm.in, prm.in_user, ibase + m * prm.in_xs + src * prm.in_axis);
     if (prm.pre == 0) {
       sm[j * M + m] = P::to_w(v);
     } else if (prm.pre == 1) {
@@ -195,6 +203,12 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
     else v = P::from_w(sm[k * M + m]);
     store_elem<P>(prm.out, prm.out_user, obase + m * prm.out_xs + jo * prm.out_axis, v);
   }
+}
+
+template <class P, int DIR>
+__global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
+    k_strided(const SParams prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw) {
+  strided_tile<P, DIR, false>(prm, sp, tw, reinterpret_cast<typename P::W*>(p3g_smem), blockIdx.x);
 }
 
 // ------------------------------------------------------------- Chebyshev

@@ -44,9 +44,10 @@ int fail(int code, const std::string& msg) {
 
 // ------------------------------------------------------------ factorisation
 // Stage radices for length n, ordered by family (16, 8, 4, 2, 3, 5, other
-// primes) as cta_fft expects.  Powers of two use radix 8 (and 16 on the F32
-// path) with a 4 or 2 remainder.
-static bool factor(int n, bool allow16, std::vector<int>& radices) {
+// primes) as cta_fft expects.  Powers of two use the largest radix allowed
+// (max_pow2: 16 only on the F32 path, 8 by default on F64, 4 or 2 when a
+// tuner asks) with a smaller remainder.
+static bool factor(int n, int max_pow2, std::vector<int>& radices) {
   radices.clear();
   int a = 0;
   while (n % 2 == 0) {
@@ -54,7 +55,17 @@ static bool factor(int n, bool allow16, std::vector<int>& radices) {
     ++a;
   }
   std::vector<int> pow2;
-  if (allow16) {
+  if (max_pow2 <= 4) {
+    while (a >= 2 && max_pow2 == 4) {
+      pow2.push_back(4);
+      a -= 2;
+    }
+    while (a >= 1) {
+      pow2.push_back(2);
+      a -= 1;
+    }
+  }
+  if (max_pow2 >= 16) {
     while (a >= 4 && a != 5) {  // 2^5 = 8*4 beats 16*2
       pow2.push_back(16);
       a -= 4;
@@ -113,12 +124,12 @@ struct HostTw {
 
 
 
-static bool build_stages(int n, bool allow16, HostTw& tw, StagePlan& sp) {
+static bool build_stages(int n, int max_pow2, HostTw& tw, StagePlan& sp) {
   std::memset(&sp, 0, sizeof(sp));
   tw.mark = (int)tw.v.size();
   sp.n = n;
   std::vector<int> rad;
-  if (n > 1 && !factor(n, allow16, rad)) return false;
+  if (n > 1 && !factor(n, max_pow2, rad)) return false;
   sp.nstages = (int)rad.size();
   int ns = 1;
   for (int s = 0; s < sp.nstages; ++s) {
@@ -460,6 +471,183 @@ int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st) {
   return P3G_OK;
 }
 
+}  // namespace
+
+namespace p3g {
+
+// Pass parameters of a forward transform: X r2c user real -> wa, Y wa ->
+// ybuf (wa, or wb when nyc < ny) keeping y modes 0..nycph-1 and the top
+// nyc-nycph (seg_copy_y, ftran.F90:736-738), Z ybuf -> user complex with the
+// Z op and z pruning (seg_copy_z, ftran.F90:705-706).
+void make_forward_params(p3g_plan p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
+                         long long dim_out, XParams& x, SParams& y, SParams& z) {
+  const long long P_ = p->pitch;
+  const long long wa_field = (long long)p->nz * p->ny * P_;
+  const long long wb_field = (long long)p->nz * p->nyc * P_;
+  void* ybuf = p->nyc < p->ny ? wb : wa;
+  const long long y_field = p->nyc < p->ny ? wb_field : wa_field;
+  x = XParams{};
+  x.in = in;
+  x.out = wa;
+  x.in_field = dim_in;
+  x.out_field = wa_field;
+  x.in_line = p->nx;
+  x.out_line = P_;
+  x.nlines = p->ny * p->nz;
+  x.nx = p->nx;
+  x.nkeep = p->nxhpc;
+  x.M = p->ax_x.M;
+  x.log2m = p->ax_x.log2m;
+  x.LS = p->ax_x.ls;
+  x.ps = p->ax_x.ps;
+  x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
+
+  y = SParams{};
+  y.in_xs = y.out_xs = 1;
+  y.in = wa;
+  y.out = ybuf;
+  y.in_axis = P_;
+  y.in_o1 = (long long)p->ny * P_;
+  y.in_o2 = wa_field;
+  y.out_axis = P_;
+  y.out_o1 = (long long)p->nyc * P_;
+  y.out_o2 = y_field;
+  y.X = p->nxhpc;
+  y.O1 = p->nz;
+  y.L = p->ny;
+  y.Lout = p->nyc;
+  y.lmap_a0 = p->ny;
+  y.lmap_a1 = p->ny;
+  y.smap_s0 = p->nycph;
+  y.smap_d = p->ny - p->nyc;
+  y.M = p->ax_y.M;
+  y.log2m = p->ax_y.log2m;
+  y.N = p->ax_y.n;
+  y.xtiles = (y.X + y.M - 1) / y.M;
+
+  const AxisPlan& az = p->ax_z[zi];
+  z = SParams{};
+  z.in_xs = z.out_xs = 1;
+  z.in = ybuf;
+  z.out = out;
+  z.out_user = 1;
+  z.in_axis = (long long)p->nyc * P_;
+  z.in_o1 = P_;
+  z.in_o2 = y_field;
+  if (p->layout == P3G_LAYOUT_STRIDE1) {  // (nzc, nyc, nxhpc), z fastest (module.F90:245-254)
+    z.out_axis = 1;
+    z.out_o1 = p->nzc;
+    z.out_xs = (long long)p->nyc * p->nzc;
+  } else {
+    z.out_axis = (long long)p->nxhpc * p->nyc;
+    z.out_o1 = p->nxhpc;
+  }
+  z.out_o2 = dim_out;
+  z.X = p->nxhpc;
+  z.O1 = p->nyc;
+  z.L = p->nz;
+  z.Lout = p->nzc;
+  z.pre = zi == 1 ? 1 : (zi == 2 ? 2 : 0);
+  z.post = zi == 2 ? 1 : 0;
+  z.lmap_a0 = p->nz;
+  z.lmap_a1 = p->nz;
+  z.smap_s0 = p->nzcph;
+  z.smap_d = p->nz - p->nzc;
+  z.M = az.M;
+  z.log2m = az.log2m;
+  z.N = az.n;
+  z.xtiles = (z.X + z.M - 1) / z.M;
+}
+
+// Pass parameters of a backward transform: Z user complex -> zbuf with the
+// z zero fill (seg_copy_z + seg_zero_z, btran.F90:553-555), Y zbuf -> wa with
+// the y zero fill (seg_copy_y + seg_zero_y, btran.F90:585-588), X c2r wa ->
+// user real with x modes beyond nxhpc read as zero (seg_zero_x,
+// btran.F90:662-663).
+void make_backward_params(p3g_plan p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
+                          long long dim_out, SParams& z, SParams& y, XParams& x) {
+  const long long P_ = p->pitch;
+  const long long wa_field = (long long)p->nz * p->ny * P_;
+  const long long wb_field = (long long)p->nz * p->nyc * P_;
+  void* zbuf = p->nyc < p->ny ? wb : wa;
+  const long long z_field = p->nyc < p->ny ? wb_field : wa_field;
+  const AxisPlan& az = p->ax_z[zi];
+  z = SParams{};
+  z.in_xs = z.out_xs = 1;
+  z.in = in;
+  z.out = zbuf;
+  z.in_user = 1;
+  if (p->layout == P3G_LAYOUT_STRIDE1) {
+    z.in_axis = 1;
+    z.in_o1 = p->nzc;
+    z.in_xs = (long long)p->nyc * p->nzc;
+  } else {
+    z.in_axis = (long long)p->nxhpc * p->nyc;
+    z.in_o1 = p->nxhpc;
+  }
+  z.in_o2 = dim_in;
+  z.out_axis = (long long)p->nyc * P_;
+  z.out_o1 = P_;
+  z.out_o2 = z_field;
+  z.X = p->nxhpc;
+  z.O1 = p->nyc;
+  z.L = p->nz;
+  z.Lout = p->nz;
+  z.pre = zi == 1 ? 1 : (zi == 2 ? 2 : 0);
+  z.post = zi == 2 ? 1 : 0;
+  z.lmap_a0 = p->nzcph;
+  z.lmap_a1 = p->nz - p->nzcph;
+  z.lmap_d = p->nz - p->nzc;
+  z.smap_s0 = p->nz;
+  z.M = az.M;
+  z.log2m = az.log2m;
+  z.N = az.n;
+  z.xtiles = (z.X + z.M - 1) / z.M;
+
+  y = SParams{};
+  y.in_xs = y.out_xs = 1;
+  y.in = zbuf;
+  y.out = wa;
+  y.in_axis = P_;
+  y.in_o1 = (long long)p->nyc * P_;
+  y.in_o2 = z_field;
+  y.out_axis = P_;
+  y.out_o1 = (long long)p->ny * P_;
+  y.out_o2 = wa_field;
+  y.X = p->nxhpc;
+  y.O1 = p->nz;
+  y.L = p->ny;
+  y.Lout = p->ny;
+  y.lmap_a0 = p->nycph;
+  y.lmap_a1 = p->ny - p->nycph;
+  y.lmap_d = p->ny - p->nyc;
+  y.smap_s0 = p->ny;
+  y.M = p->ax_y.M;
+  y.log2m = p->ax_y.log2m;
+  y.N = p->ax_y.n;
+  y.xtiles = (y.X + y.M - 1) / y.M;
+
+  x = XParams{};
+  x.in = wa;
+  x.out = out;
+  x.in_field = wa_field;
+  x.out_field = dim_out;
+  x.in_line = P_;
+  x.out_line = p->nx;
+  x.nlines = p->ny * p->nz;
+  x.nx = p->nx;
+  x.nkeep = p->nxhpc;
+  x.M = p->ax_x.M;
+  x.log2m = p->ax_x.log2m;
+  x.LS = p->ax_x.ls;
+  x.ps = p->ax_x.ps;
+  x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
+}
+
+}  // namespace p3g
+
+namespace {
+
 template <class P>
 int do_ftran(p3g_plan p, const void* in, void* out, const char* op, int nv, long long dim_in, long long dim_out,
              cudaStream_t st) {
@@ -469,97 +657,22 @@ int do_ftran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   if (!p->z_ok[zi]) return fail(P3G_E_UNSUPPORTED, std::string("Z transform '") + op[2] + "' unsupported for nz");
   int rc = ensure_workspace(p, nv);
   if (rc) return rc;
-  const long long P_ = p->pitch;
-  const long long wa_field = (long long)p->nz * p->ny * P_;
-  const long long wb_field = (long long)p->nz * p->nyc * P_;
-  void* ybuf = p->nyc < p->ny ? p->wb : p->wa;
-  const long long y_field = p->nyc < p->ny ? wb_field : wa_field;
-  // X r2c: user real -> wa
+  XParams x;
+  SParams y, z;
+  make_forward_params(p, in, out, p->wa, p->wb, zi, dim_in, dim_out, x, y, z);
   {
     PassTimer tm(p, 4, st);
-    XParams x{};
-    x.in = in;
-    x.out = p->wa;
-    x.in_field = dim_in;
-    x.out_field = wa_field;
-    x.in_line = p->nx;
-    x.out_line = P_;
-    x.nlines = p->ny * p->nz;
-    x.nx = p->nx;
-    x.nkeep = p->nxhpc;
-    x.M = p->ax_x.M;
-    x.log2m = p->ax_x.log2m;
-    x.LS = p->ax_x.ls;
-    x.ps = p->ax_x.ps;
-    x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
-    rc = run_x_r2c<P>(p, x, nv, st);
-    if (rc) return rc;
+    if ((rc = run_x_r2c<P>(p, x, nv, st))) return rc;
     tm.done();
   }
-  // Y c2c: wa -> ybuf, keeping y modes 0..nycph-1 and the top nyc-nycph (seg_copy_y, ftran.F90:736-738)
   {
     PassTimer tm(p, 6, st);
-    SParams s{};
-    s.in_xs = s.out_xs = 1;
-    s.in = p->wa;
-    s.out = ybuf;
-    s.in_user = 0;
-    s.out_user = 0;
-    s.in_axis = P_;
-    s.in_o1 = (long long)p->ny * P_;
-    s.in_o2 = wa_field;
-    s.out_axis = P_;
-    s.out_o1 = (long long)p->nyc * P_;
-    s.out_o2 = y_field;
-    s.X = p->nxhpc;
-    s.O1 = p->nz;
-    s.L = p->ny;
-    s.Lout = p->nyc;
-    s.pre = 0;
-    s.post = 0;
-    s.lmap_a0 = p->ny;
-    s.lmap_a1 = p->ny;
-    s.lmap_d = 0;
-    s.smap_s0 = p->nycph;
-    s.smap_d = p->ny - p->nyc;
-    rc = run_strided<P>(p, s, p->ax_y, true, nv, st);
-    if (rc) return rc;
+    if ((rc = run_strided<P>(p, y, p->ax_y, true, nv, st))) return rc;
     tm.done();
   }
-  // Z op: ybuf -> user complex, keeping z modes 0..nzcph-1 and the top nzc-nzcph (seg_copy_z, ftran.F90:705-706)
   {
     PassTimer tm(p, 7, st);
-    SParams s{};
-    s.in_xs = s.out_xs = 1;
-    s.in = ybuf;
-    s.out = out;
-    s.in_user = 0;
-    s.out_user = 1;
-    s.in_axis = (long long)p->nyc * P_;
-    s.in_o1 = P_;
-    s.in_o2 = y_field;
-    if (p->layout == P3G_LAYOUT_STRIDE1) {  // (nzc, nyc, nxhpc), z fastest (module.F90:245-254)
-      s.out_axis = 1;
-      s.out_o1 = p->nzc;
-      s.out_xs = (long long)p->nyc * p->nzc;
-    } else {
-      s.out_axis = (long long)p->nxhpc * p->nyc;
-      s.out_o1 = p->nxhpc;
-    }
-    s.out_o2 = dim_out;
-    s.X = p->nxhpc;
-    s.O1 = p->nyc;
-    s.L = p->nz;
-    s.Lout = p->nzc;
-    s.pre = zi == 1 ? 1 : (zi == 2 ? 2 : 0);
-    s.post = zi == 2 ? 1 : 0;
-    s.lmap_a0 = p->nz;
-    s.lmap_a1 = p->nz;
-    s.lmap_d = 0;
-    s.smap_s0 = p->nzcph;
-    s.smap_d = p->nz - p->nzc;
-    rc = run_strided<P>(p, s, p->ax_z[zi], fsign, nv, st);
-    if (rc) return rc;
+    if ((rc = run_strided<P>(p, z, p->ax_z[zi], fsign, nv, st))) return rc;
     tm.done();
   }
   return P3G_OK;
@@ -574,95 +687,22 @@ int do_btran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   if (!p->z_ok[zi]) return fail(P3G_E_UNSUPPORTED, std::string("Z transform '") + op[0] + "' unsupported for nz");
   int rc = ensure_workspace(p, nv);
   if (rc) return rc;
-  const long long P_ = p->pitch;
-  const long long wa_field = (long long)p->nz * p->ny * P_;
-  const long long wb_field = (long long)p->nz * p->nyc * P_;
-  void* zbuf = p->nyc < p->ny ? p->wb : p->wa;
-  const long long z_field = p->nyc < p->ny ? wb_field : wa_field;
-  // Z op: user complex -> zbuf with z zero-fill (seg_copy_z + seg_zero_z, btran.F90:553-555)
+  SParams z, y;
+  XParams x;
+  make_backward_params(p, in, out, p->wa, p->wb, zi, dim_in, dim_out, z, y, x);
   {
     PassTimer tm(p, 8, st);
-    SParams s{};
-    s.in_xs = s.out_xs = 1;
-    s.in = in;
-    s.out = zbuf;
-    s.in_user = 1;
-    s.out_user = 0;
-    if (p->layout == P3G_LAYOUT_STRIDE1) {
-      s.in_axis = 1;
-      s.in_o1 = p->nzc;
-      s.in_xs = (long long)p->nyc * p->nzc;
-    } else {
-      s.in_axis = (long long)p->nxhpc * p->nyc;
-      s.in_o1 = p->nxhpc;
-    }
-    s.in_o2 = dim_in;
-    s.out_axis = (long long)p->nyc * P_;
-    s.out_o1 = P_;
-    s.out_o2 = z_field;
-    s.X = p->nxhpc;
-    s.O1 = p->nyc;
-    s.L = p->nz;
-    s.Lout = p->nz;
-    s.pre = zi == 1 ? 1 : (zi == 2 ? 2 : 0);
-    s.post = zi == 2 ? 1 : 0;
-    s.lmap_a0 = p->nzcph;
-    s.lmap_a1 = p->nz - p->nzcph;
-    s.lmap_d = p->nz - p->nzc;
-    s.smap_s0 = p->nz;
-    s.smap_d = 0;
-    rc = run_strided<P>(p, s, p->ax_z[zi], fsign, nv, st);
-    if (rc) return rc;
+    if ((rc = run_strided<P>(p, z, p->ax_z[zi], fsign, nv, st))) return rc;
     tm.done();
   }
-  // Y c2c backward: zbuf -> wa with y zero-fill (seg_copy_y + seg_zero_y, btran.F90:585-588)
   {
     PassTimer tm(p, 9, st);
-    SParams s{};
-    s.in_xs = s.out_xs = 1;
-    s.in = zbuf;
-    s.out = p->wa;
-    s.in_user = 0;
-    s.out_user = 0;
-    s.in_axis = P_;
-    s.in_o1 = (long long)p->nyc * P_;
-    s.in_o2 = z_field;
-    s.out_axis = P_;
-    s.out_o1 = (long long)p->ny * P_;
-    s.out_o2 = wa_field;
-    s.X = p->nxhpc;
-    s.O1 = p->nz;
-    s.L = p->ny;
-    s.Lout = p->ny;
-    s.lmap_a0 = p->nycph;
-    s.lmap_a1 = p->ny - p->nycph;
-    s.lmap_d = p->ny - p->nyc;
-    s.smap_s0 = p->ny;
-    s.smap_d = 0;
-    rc = run_strided<P>(p, s, p->ax_y, false, nv, st);
-    if (rc) return rc;
+    if ((rc = run_strided<P>(p, y, p->ax_y, false, nv, st))) return rc;
     tm.done();
   }
-  // X c2r: wa -> user real, x modes beyond nxhpc read as zero (seg_zero_x, btran.F90:662-663)
   {
     PassTimer tm(p, 11, st);
-    XParams x{};
-    x.in = p->wa;
-    x.out = out;
-    x.in_field = wa_field;
-    x.out_field = dim_out;
-    x.in_line = P_;
-    x.out_line = p->nx;
-    x.nlines = p->ny * p->nz;
-    x.nx = p->nx;
-    x.nkeep = p->nxhpc;
-    x.M = p->ax_x.M;
-    x.log2m = p->ax_x.log2m;
-    x.LS = p->ax_x.ls;
-    x.ps = p->ax_x.ps;
-    x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
-    rc = run_x_c2r<P>(p, x, nv, st);
-    if (rc) return rc;
+    if ((rc = run_x_c2r<P>(p, x, nv, st))) return rc;
     tm.done();
   }
   return P3G_OK;
@@ -685,7 +725,17 @@ const char* p3g_last_error(void) { return g_last_error.c_str(); }
 
 int p3g_plan_create(p3g_plan* out, int nx, int ny, int nz, int nxc, int nyc, int nzc, int precision, int layout,
                     int flags) {
+  return p3g_plan_create_tuned(out, nx, ny, nz, nxc, nyc, nzc, precision, layout, flags, 0, 0);
+}
+
+int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int nyc, int nzc, int precision,
+                          int layout, int flags, int max_radix, int max_lines) {
   if (!out) return fail(P3G_E_ARG, "plan pointer is NULL");
+  if (max_radix != 0 && max_radix != 2 && max_radix != 4 && max_radix != 8 &&
+      !(max_radix == 16 && precision == P3G_F32))
+    return fail(P3G_E_ARG, "max_radix must be 0, 2, 4, 8 (or 16 on the F32 path)");
+  if (max_lines < 0 || (max_lines & (max_lines - 1)) != 0)
+    return fail(P3G_E_ARG, "max_lines must be 0 or a power of two");
   *out = nullptr;
   if (nx <= 0 || ny <= 0 || nz <= 0)
     return fail(P3G_E_ARG, "Invalid dimensions : " + std::to_string(nx) + " " + std::to_string(ny) + " " +
@@ -719,12 +769,15 @@ int p3g_plan_create(p3g_plan* out, int nx, int ny, int nz, int nxc, int nyc, int
 
   HostTw tw;
   std::vector<StagePlan> sps;
-  const int strided_max_m = f64 ? 64 : 128;  // 256 words per TMA box row
+  int strided_max_m = f64 ? 64 : 128;  // 256 words per TMA box row
+  const int x_max_m = max_lines > 0 ? max_lines : (1 << 30);
+  if (max_lines > 0 && max_lines < strided_max_m) strided_max_m = max_lines;
+  const int max_pow2 = max_radix > 0 ? max_radix : (f64 ? 8 : 16);
   auto add_axis = [&](AxisPlan& ap, int n, int lines) -> bool {
-    if (!build_stages(n, !f64, tw, ap.sp)) return false;
+    if (!build_stages(n, max_pow2, tw, ap.sp)) return false;
     ap.tw_lo = tw.mark;
     ap.tw_cnt = (int)tw.v.size() - tw.mark;
-    if (!size_tile(ap, n, lines, f64, &ap == &p->ax_x ? (1 << 30) : strided_max_m)) return false;
+    if (!size_tile(ap, n, lines, f64, &ap == &p->ax_x ? x_max_m : strided_max_m)) return false;
     ap.sp_index = (int)sps.size();
     sps.push_back(ap.sp);
     return true;

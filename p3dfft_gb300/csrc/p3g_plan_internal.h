@@ -37,6 +37,18 @@ struct TimerRec {
 
 }  // namespace p3g
 
+struct p3g_plan_s;
+
+namespace p3g {
+// Pass parameters of one field's forward (X, Y, Z) and backward (Z, Y, X)
+// transform with workspaces wa/wb; zi = Z op index (0 fft, 1 dct, 2 dst,
+// 3 none).  Defined in p3g_plan.cu.
+void make_forward_params(p3g_plan_s* p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
+                         long long dim_out, XParams& x, SParams& y, SParams& z);
+void make_backward_params(p3g_plan_s* p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
+                          long long dim_out, SParams& z, SParams& y, XParams& x);
+}  // namespace p3g
+
 struct p3g_plan_s {
   using AxisPlan = p3g::AxisPlan;
   using TimerRec = p3g::TimerRec;

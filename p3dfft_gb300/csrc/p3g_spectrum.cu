@@ -25,122 +25,24 @@
 #include <string>
 
 #include "p3g_plan_internal.h"
+#include "p3g_spectrum.cuh"
 
 namespace p3g {
 namespace {
 
-struct SpecParams {
-  const void* in;
-  double* E;           // nv * (kmax + 1) bins
-  long long field;     // element spacing between fields
-  int rows, len;       // rows of the fast axis and their length
-  int nyc;             // rows decode as (outer, y) with y fastest
-  int nx, ny, nz;
-  int stride1;         // fast axis is z (1) or x (0)
-  int kmax;
-  int flags;
-  double s2;           // scale^2
-};
-
-// ik = floor(sqrt(k2) + 0.5) exactly: the largest m with k2 > m (m - 1).
-P3G_D int shell_index(uint32_t k2) {
-  int m = (int)(sqrtf((float)k2) + 0.5f);
-  while (m > 0 && (unsigned long long)m * (unsigned long long)(m - 1) >= k2) --m;
-  while ((unsigned long long)(m + 1) * (unsigned long long)m < k2) ++m;
-  return m;
-}
-
-// |frequency| of 0-based index i of an axis of n points (driver_spec.F90:294-298)
-P3G_D int fold(int i, int n) { return i + 1 > n / 2 ? n - i : i; }
-
-P3G_D df sq(df a) {
-  df r;
-  r.hi = fmul_rn(a.hi, a.hi);
-  float e = ffma(a.hi, a.hi, -r.hi);
-  r.lo = ffma(2.0f * a.hi, a.lo, e);
-  return r;
-}
-
-template <class P>
-P3G_D void load_mode(const typename P::UC* p, df& re, df& im);
-template <>
-P3G_D void load_mode<PathF64>(const double2* p, df& re, df& im) {
-  const double2 v = *p;
-  re = d2df(v.x);
-  im = d2df(v.y);
-}
-template <>
-P3G_D void load_mode<PathF32>(const float2* p, df& re, df& im) {
-  const float2 v = *p;
-  re = df{v.x, 0.0f};
-  im = df{v.y, 0.0f};
-}
-
 template <class P>
 __global__ void __launch_bounds__(256) k_spectrum(const SpecParams prm) {
   extern __shared__ double p3g_spec_hist[];
-  using UC = typename P::UC;
-  const int nbins = prm.kmax + 1;
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
-  double* hist = p3g_spec_hist + (size_t)warp * nbins;
-  for (int i = threadIdx.x; i < nwarps * nbins; i += blockDim.x) p3g_spec_hist[i] = 0.0;
+  for (int i = threadIdx.x; i < nwarps * (prm.kmax + 1); i += blockDim.x) p3g_spec_hist[i] = 0.0;
   __syncthreads();
-  const UC* in = static_cast<const UC*>(prm.in) + (long long)blockIdx.y * prm.field;
-  const bool k2w = (prm.flags & P3G_SPEC_K2) != 0;
-  const bool herm = (prm.flags & P3G_SPEC_HERMITIAN) != 0;
-  const uint32_t le_mask = 0xFFFFFFFFu >> (31 - lane);
-  for (int r = blockIdx.x * nwarps + warp; r < prm.rows; r += gridDim.x * nwarps) {
-    const int y = r % prm.nyc;
-    const int outer = r / prm.nyc;
-    const int ky = fold(y, prm.ny);
-    const UC* row = in + (long long)r * prm.len;
-    for (int base = 0; base < prm.len; base += 32) {
-      const int i = base + lane;
-      int bin = -1 - lane;  // lanes past the row end: a segment of their own
-      df w{0.0f, 0.0f};
-      if (i < prm.len) {
-        const int kx = prm.stride1 ? outer : i;
-        const int kz = fold(prm.stride1 ? i : outer, prm.nz);
-        const uint32_t k2 = (uint32_t)kx * kx + (uint32_t)ky * ky + (uint32_t)kz * kz;
-        bin = shell_index(k2);
-        df re, im;
-        load_mode<P>(row + i, re, im);
-        w = dadd(sq(re), sq(im));
-        if (k2w) {
-          const float khi = __uint2float_rn(k2);
-          const float klo = (float)((long long)k2 - (long long)khi);
-          w = dmulc(w, khi, klo);
-        }
-        if (herm && kx > 0 && 2 * kx != prm.nx) w = dscale2(w, 2.0f);
-      }
-      const int prev = __shfl_up_sync(0xFFFFFFFFu, bin, 1);
-      const bool head = lane == 0 || prev != bin;
-      const uint32_t heads = __ballot_sync(0xFFFFFFFFu, head);
-      const int seg = __popc(heads & le_mask);
-#pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const float oh = __shfl_down_sync(0xFFFFFFFFu, w.hi, d);
-        const float ol = __shfl_down_sync(0xFFFFFFFFu, w.lo, d);
-        const int os = __shfl_down_sync(0xFFFFFFFFu, seg, d);
-        if (lane + d < 32 && os == seg) w = dadd(w, df{oh, ol});
-      }
-      // modes beyond kmax are dropped (the sample would write past E)
-      if (head && bin >= 0 && bin <= prm.kmax) atomicAdd(hist + bin, (double)w.hi + (double)w.lo);
-    }
-  }
+  spectrum_rows<P, false>(prm, p3g_spec_hist, blockIdx.x * nwarps + (threadIdx.x >> 5), prm.rows, gridDim.x * nwarps,
+                          blockIdx.y);
   __syncthreads();
-  double* E = prm.E + (long long)blockIdx.y * nbins;
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
-    double s = 0.0;
-    for (int k = 0; k < nwarps; ++k) s += p3g_spec_hist[(size_t)k * nbins + b];
-    if (s != 0.0) atomicAdd(E + b, s * prm.s2);
-  }
+  spectrum_flush(prm, p3g_spec_hist, nwarps, blockIdx.y);
 }
 
 constexpr int kSpecThreads = 256;
-constexpr size_t kSpecMaxSmem = 200 * 1024;
 
 template <class P>
 cudaError_t launch_spectrum(const SpecParams& prm, int nv, int sm_count, cudaStream_t st) {
@@ -165,12 +67,10 @@ cudaError_t launch_spectrum(const SpecParams& prm, int nv, int sm_count, cudaStr
 }  // namespace
 }  // namespace p3g
 
-extern "C" int p3g_spectrum(p3g_plan p, const void* in, double* E, int kmax, double scale, int flags, int nv,
-                            long long dim_in, void* stream) {
-  using namespace p3g;
-  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
-  if (!in || !E) return fail(P3G_E_ARG, "NULL array");
-  if (nv <= 0 || nv > 65535) return fail(P3G_E_ARG, "nv out of range");
+namespace p3g {
+
+int make_spectrum_params(p3g_plan p, const void* in, double* E, int kmax, double scale, int flags,
+                         long long dim_in, SpecParams& prm) {
   if (flags & ~(P3G_SPEC_K2 | P3G_SPEC_HERMITIAN)) return fail(P3G_E_ARG, "unknown spectrum flags");
   if (kmax <= 0)  // driver_spec.F90:198
     kmax = (int)(std::sqrt((double)p->nx * p->nx + (double)p->ny * p->ny + (double)p->nz * p->nz) * 0.5 + 0.5);
@@ -187,7 +87,7 @@ extern "C" int p3g_spectrum(p3g_plan p, const void* in, double* E, int kmax, dou
   const long long csize = (long long)p->nxhpc * p->nyc * p->nzc;
   if (dim_in <= 0) dim_in = csize;
   if (dim_in < csize) return fail(P3G_E_ARG, "spectrum error: input array dimensions are too low");
-  SpecParams prm{};
+  prm = SpecParams{};
   prm.in = in;
   prm.E = E;
   prm.field = dim_in;
@@ -201,6 +101,21 @@ extern "C" int p3g_spectrum(p3g_plan p, const void* in, double* E, int kmax, dou
   prm.kmax = kmax;
   prm.flags = flags;
   prm.s2 = scale * scale;
+  return P3G_OK;
+}
+
+}  // namespace p3g
+
+extern "C" int p3g_spectrum(p3g_plan p, const void* in, double* E, int kmax, double scale, int flags, int nv,
+                            long long dim_in, void* stream) {
+  using namespace p3g;
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  if (!in || !E) return fail(P3G_E_ARG, "NULL array");
+  if (nv <= 0 || nv > 65535) return fail(P3G_E_ARG, "nv out of range");
+  SpecParams prm;
+  int rc = make_spectrum_params(p, in, E, kmax, scale, flags, dim_in, prm);
+  if (rc) return rc;
+  const size_t nbins = (size_t)prm.kmax + 1;
   std::lock_guard<std::mutex> lk(p->mu);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemsetAsync(E, 0, nbins * nv * sizeof(double), st);
