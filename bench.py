@@ -267,6 +267,10 @@ def run_ours(args):
         e2e = run_e2e(torch, pg, grid, ops, x, max(1, args.steps // 2), dev)
     del x, b
     torch.cuda.empty_cache()
+    batched = serving = None
+    if not args.skip_forms:
+        batched = run_batched(torch, pg, dev, args.steps, args.warmup, npts / (ms64 * 1e-3) / 1e9)
+        serving = run_serving(torch, pg, args.serve_requests, npts / (ms64 * 1e-3) / 1e9)
 
     value = world * npts / (ms64 * 1e-3) / 1e9
     line = {
@@ -297,6 +301,10 @@ def run_ours(args):
     }
     if e2e:
         line["e2e"] = e2e
+    if batched:
+        line["batched"] = batched
+    if serving:
+        line["serving"] = serving
     ctx.__exit__(None, None, None)
     if rank == 0 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
@@ -305,6 +313,129 @@ def run_ours(args):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+BATCH_SIDES = (48, 64, 96, 120, 128, 160, 192, 256)
+
+
+def run_batched(torch, pg, dev, steps, warmup, plain_f64_gpts):
+    """Batching form: 64 independent r2c+c2r round trips, each side drawn
+    from BATCH_SIDES with a fixed seed, inputs U[-1,1), in one persistent
+    launch replayed from a captured CUDA graph; per-shape radix/tile knobs and
+    the queue window from the autotuner.  Also times the same 64 round trips
+    issued one plan call after another (the plain API) for comparison."""
+    from p3dfft_gb300 import autotune
+    rng = np.random.default_rng(4)
+    shapes = [tuple(int(v) for v in rng.choice(BATCH_SIDES, size=3)) for _ in range(64)]
+    npts = sum(a * b * c for a, b, c in shapes)
+    out = {"grids": 64, "sides": list(BATCH_SIDES), "points_per_step": npts, "seed": 4}
+    results = {}
+    t_tune = time.time()
+    for prec, name in ((pg.F64, "f64"), (pg.F32, "f32")):
+        rdt = torch.float64 if prec == pg.F64 else torch.float32
+        plans = {}
+        for sh in sorted(set(shapes)):
+            t = autotune.tune_shape(sh, prec, reps=3, min_points=1 << 23, cands=autotune.candidates(prec)[:3])
+            plans[sh] = pg.Plan(*sh, precision=prec, max_radix=t["max_radix"], max_lines=t["max_lines"])
+        g = torch.Generator(device=dev)
+        g.manual_seed(44)
+        jobs = []
+        for sh in shapes:
+            nx, ny, nz = sh
+            x = torch.rand((nz, ny, nx), generator=g, device=dev, dtype=torch.float64).mul_(2).sub_(1).to(rdt)
+            jobs.append({"plan": plans[sh], "kind": pg.JOB_ROUNDTRIP, "in": x,
+                         "out": torch.empty_like(x)})
+        window, wtimes = autotune.tune_window(jobs, prec, windows=(1, 4, 16, 0), reps=3)
+        b = pg.Batch(prec).set_jobs(jobs, window=window)
+        b.capture()
+        stream = torch.cuda.current_stream()
+        for _ in range(warmup):
+            b.replay(stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            b.replay(stream)
+        e1.record(stream)
+        b.check(stream)
+        ms = e0.elapsed_time(e1) / steps
+        info = b.info()
+        # round-trip error of every grid (unnormalised transform: divide by N)
+        worst = 0.0
+        for j in jobs:
+            p = j["plan"]
+            r = j["out"].double() / (p.nx * p.ny * p.nz)
+            xin = j["in"].double()
+            worst = max(worst, float(torch.linalg.vector_norm(r - xin) / torch.linalg.vector_norm(xin)))
+        # the same round trips through the plain per-plan API, one after another
+        for p in plans.values():
+            p.set_options(True, True)
+        for _ in range(2):
+            for j in jobs:
+                j["plan"].btran_c2r(j["plan"].ftran_r2c(j["in"]), j["out"])
+        e0.record(stream)
+        for _ in range(max(1, steps // 2)):
+            for j in jobs:
+                j["plan"].btran_c2r(j["plan"].ftran_r2c(j["in"]), j["out"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_plain = e0.elapsed_time(e1) / max(1, steps // 2)
+        results[name] = {"value": round(npts / (ms * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_step": round(ms, 4),
+                         "window": window, "window_ms": {str(k): round(v, 4) for k, v in wtimes.items()},
+                         "work_items": info["items"], "persistent_ctas": info["ctas"],
+                         "kernel_launches_per_step": 1, "roundtrip_rel_l2_max": worst,
+                         "plain_api_ms_per_step": round(ms_plain, 4),
+                         "speedup_vs_plain_api": round(ms_plain / ms, 3)}
+        b.close()
+        for p in plans.values():
+            p.close()
+        del jobs
+        torch.cuda.empty_cache()
+    out.update(results)
+    out["tuning_s"] = round(time.time() - t_tune, 1)
+    if plain_f64_gpts:
+        out["f32_vs_plain_f64_1024cubed"] = round(results["f32"]["value"] / plain_f64_gpts, 3)
+    return out
+
+
+def run_serving(torch, pg, n_requests, plain_f64_gpts):
+    """Serving form: requests (forward : backward : spectrum = 4:4:2, cubic or
+    box grids with sides log-uniform over the 2^a 3^b 5^c values in [32,512],
+    10 % asking for FP64 accuracy) through the continuous-batching server with
+    a 150 GB device-memory budget.  Capacity is measured first with a closed
+    loop (all requests queued at once); the timed stream then arrives as a
+    Poisson process at 70 % of that capacity."""
+    from p3dfft_gb300 import serve
+    cap_reqs = serve.make_requests(min(600, n_requests), seed=50)
+    reqs = serve.poisson_arrivals(serve.make_requests(n_requests, seed=5), rate=1.0)  # rate set below
+    srv = serve.Server(budget_bytes=150e9, slots=3, max_jobs=64, window=4, keep_outputs=False)
+    t = time.time()
+    for r in cap_reqs + reqs:  # plans (tables) resident before the clock starts
+        srv.plan(r.shape, pg.F64 if r.tol < serve.F32_TOL else pg.F32)
+    plan_s = time.time() - t
+    srv.run(serve.make_requests(64, seed=51))  # warm-up
+    t = time.perf_counter()
+    srv.run(cap_reqs)
+    cap_wall = time.perf_counter() - t
+    capacity = len(cap_reqs) / cap_wall
+    rate = 0.7 * capacity
+    serve.poisson_arrivals(reqs, rate=rate, seed=6)
+    launches0 = srv.launches
+    t = time.perf_counter()
+    srv.run(reqs)
+    wall = time.perf_counter() - t
+    out = serve.summarize(reqs, wall)
+    out.update({"arrival_rate_req_s": round(rate, 1), "capacity_req_s": round(capacity, 1),
+                "capacity_gpts_s": round(sum(r.points for r in cap_reqs) / cap_wall / 1e9, 3),
+                "budget_gb": 150, "peak_in_flight_gb": round(srv.peak_in_flight / 1e9, 2),
+                "launches": srv.launches - launches0,
+                "mean_jobs_per_launch": round(float(np.mean(srv.batch_sizes[-(srv.launches - launches0):]
+                                                            or [0])), 2),
+                "slots": len(srv.slots), "plans_resident": len(srv.plans), "plan_setup_s": round(plan_s, 1),
+                "mix": "forward:backward:spectrum 4:4:2, 10% FP64"})
+    if plain_f64_gpts:
+        out["capacity_vs_plain_f64_1024cubed"] = round(out["capacity_gpts_s"] / plain_f64_gpts, 3)
+    srv.close()
+    return out
 
 
 def run_e2e(torch, pg, grid, ops, x_dev, steps, dev):
@@ -406,6 +537,8 @@ def main():
     ap.add_argument("--mode", default="pipe_tma", choices=sorted(MODES),
                     help="kernel family: persistent pipelined with TMA or cp.async copies, or single-tile")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-forms", action="store_true", help="skip the batched and serving forms")
+    ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()

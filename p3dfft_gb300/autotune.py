@@ -92,9 +92,11 @@ def _roundtrip_jobs(plans, x, rdt):
     return jobs
 
 
-def tune_shape(shape, precision, reps: int = 5, min_points: int = 1 << 24, use_cache: bool = True) -> dict:
-    """Best (max_radix, max_lines) for round trips of `shape`; times several
-    copies of the grid in one batch so that the GPU is filled."""
+def tune_shape(shape, precision, reps: int = 5, min_points: int = 1 << 24, use_cache: bool = True,
+               cands=None) -> dict:
+    """Best (max_radix, max_lines) for round trips of `shape` among `cands`
+    (default: candidates(precision)); times several copies of the grid in one
+    batch so that the GPU is filled."""
     import torch
     key = _key(shape, precision)
     if use_cache:
@@ -108,7 +110,7 @@ def tune_shape(shape, precision, reps: int = 5, min_points: int = 1 << 24, use_c
     rdt = torch.float64 if precision == F64 else torch.float32
     x = torch.rand((nz, ny, nx), dtype=rdt, device="cuda") * 2 - 1
     results = []
-    for mr, ml in candidates(precision):
+    for mr, ml in (cands or candidates(precision)):
         try:
             plans = [Plan(nx, ny, nz, precision=precision, max_radix=mr, max_lines=ml)] * copies
         except Exception:  # a knob outside what this shape supports

@@ -55,6 +55,33 @@ struct BatchPass {
 
 constexpr int kBatchSpinLimit = 1 << 22;  // polls of ~1 us: about 4 s
 
+// 256 threads and two CTAs per SM on both paths (128 registers per thread):
+// while one CTA waits on its loads the other computes.  Tiles hold at most
+// kElemsPerThread x 256 = 4096 points.
+constexpr int kBatchThreads = 256;
+constexpr int kBatchTile = kElemsPerThread * kBatchThreads;
+
+// Halve the plan's tile width until one tile fits the batch CTA; returns the
+// tile's shared-memory bytes (0 when even one line is too long).
+size_t fit_x(XParams& x, const AxisPlan& ap, size_t esize) {
+  while (x.M > 1 && (long long)x.M * x.nx > kBatchTile) {
+    x.M >>= 1;
+    x.log2m--;
+  }
+  if ((long long)x.M * x.nx > kBatchTile) return 0;
+  x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
+  return (size_t)x.M * x.LS * esize * (ap.sp.has_generic ? 2 : 1);
+}
+size_t fit_s(SParams& s, const AxisPlan& ap, size_t esize) {
+  while (s.M > 1 && (long long)s.M * s.N > kBatchTile) {
+    s.M >>= 1;
+    s.log2m--;
+  }
+  if ((long long)s.M * s.N > kBatchTile) return 0;
+  s.xtiles = (s.X + s.M - 1) / s.M;
+  return (size_t)s.M * s.N * esize * (ap.sp.has_generic ? 2 : 1);
+}
+
 P3G_D int ld_acquire(const int* p) {
   int v;
   asm volatile("ld.acquire.gpu.global.b32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
@@ -85,7 +112,7 @@ P3G_D bool wait_count(const int* cnt, int need, int* err) {
 
 // ctl[0] = next queue item, ctl[1] = error, ctl[2 + d] = finished tiles of pass d
 template <class P>
-__global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
+__global__ void __launch_bounds__(kBatchThreads, 2)
     k_batch(const BatchPass* __restrict__ passes, int npass, int nitems, int* __restrict__ ctl) {
   using W = typename P::W;
   __shared__ int s_item, s_pass;
@@ -146,7 +173,7 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
 // occupancy for this batch's tile size.
 template <class P>
 cudaError_t batch_config(size_t smem, int& threads, int& per_sm, size_t& max_dyn) {
-  threads = PathLimits<P>::kMaxThreads;
+  threads = kBatchThreads;
   static size_t s_max_dyn = 0;
   cudaError_t e = cudaSuccess;
   if (!s_max_dyn) {
@@ -268,7 +295,7 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
   if (window <= 0) window = njobs;
   std::lock_guard<std::mutex> lk(b->mu);
   const bool f64 = b->prec == P3G_F64;
-  const int threads = f64 ? PathLimits<PathF64>::kMaxThreads : PathLimits<PathF32>::kMaxThreads;
+  const int threads = kBatchThreads;
   const int nwarps = threads / 32;
   // per job: its chain of passes
   std::vector<std::vector<BatchPass>> chains(njobs);
@@ -288,24 +315,29 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
     void* wb = L.wb ? w + L.wa : nullptr;
     void* cplx = L.cplx ? w + L.wa + L.wb : nullptr;
     const StagePlan* dsp = p->d_sp;
+    bool fits = true;
     auto x_pass = [&](int kind, const XParams& x) {
       BatchPass q{};
       q.kind = kind;
       q.x = x;
-      q.tiles = x.tiles;
+      const size_t need = fit_x(q.x, p->ax_x, p->esize());
+      fits = fits && need > 0;
+      q.tiles = q.x.tiles;
       q.sp = dsp + p->ax_x.sp_index;
       q.tw = p->d_tw;
-      smem = std::max(smem, p->ax_x.smem);
+      smem = std::max(smem, need);
       chains[j].push_back(q);
     };
     auto s_pass = [&](int kind, const SParams& s, const AxisPlan& ap) {
       BatchPass q{};
       q.kind = kind;
       q.s = s;
-      q.tiles = s.xtiles * s.O1;
+      const size_t need = fit_s(q.s, ap, p->esize());
+      fits = fits && need > 0;
+      q.tiles = q.s.xtiles * q.s.O1;
       q.sp = dsp + ap.sp_index;
       q.tw = p->d_tw;
-      smem = std::max(smem, ap.smem);
+      smem = std::max(smem, need);
       chains[j].push_back(q);
     };
     const long long rsize = (long long)p->nx * p->ny * p->nz;
@@ -338,6 +370,7 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
       s_pass(kBBwd, y, p->ax_y);
       x_pass(kBXc2r, x);
     }
+    if (!fits) return fail(P3G_E_UNSUPPORTED, who + "a line is longer than a batch tile (4096 points)");
     if (jb.kind == P3G_JOB_SPECTRUM) {
       BatchPass q = chains[j][0];
       q.kind = kBSpec;

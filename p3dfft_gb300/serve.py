@@ -1,0 +1,369 @@
+"""Serving form: a request loop with continuous batching.
+
+Requests are forward r2c transforms, backward c2r transforms, or power
+spectra (forward transform, then |u_hat|^2 binned into integer spherical
+shells in binary64 with the conjugate half counted), of any grid size.
+Plans (twiddles, stage tables) and each shape's input grid stay resident on
+the device.  The loop keeps ``slots`` launch slots, each a CUDA stream with
+one batch object per precision; whenever a slot is free it admits the oldest
+pending requests (FIFO) that fit the device-memory budget and the per-launch
+job limit, and launches them as one persistent batch (p3g_batch_*) per
+precision.  Requests that arrive while other slots are busy are admitted as
+slots and memory free up, and the slots' launches overlap on the GPU.
+
+Admission: a request holds its input, output and work buffer while in
+flight, and the sum over in-flight requests stays within the device-memory
+budget (a request larger than the whole budget is an error).  Resident
+input grids are kept besides, up to a quarter of the budget, least recently
+used first out.
+
+Precision per request: the FP32 path (compensated twiddles; relative L2
+error ~2e-7 against the FP64 oracle) unless the request asks for a tighter
+tolerance than ``F32_TOL``, then the FP64 path (double-float; ~1e-14).
+
+There is no counterpart in the reference (one blocking transform per call);
+the transforms themselves are the reference's (ftran.F90:489-780,
+btran.F90:396-679) and the spectrum is the spectrum sample's binning
+(driver_spec.F90:263-341).
+"""
+from __future__ import annotations
+
+import collections
+import math
+import time
+from dataclasses import dataclass, field
+
+from . import (F32, F64, JOB_BACKWARD, JOB_FORWARD, JOB_SPECTRUM, SPEC_HERMITIAN, Batch, Plan)
+
+F32_TOL = 1e-6
+KINDS = {"forward": JOB_FORWARD, "backward": JOB_BACKWARD, "spectrum": JOB_SPECTRUM}
+
+
+@dataclass
+class Request:
+    rid: int
+    kind: str                 # forward | backward | spectrum
+    shape: tuple              # (nx, ny, nz)
+    arrival: float = 0.0      # seconds on the server's clock
+    tol: float = F32_TOL      # requested accuracy; < F32_TOL selects FP64
+    precision: int = F32
+    t_admit: float = math.nan
+    t_done: float = math.nan
+    out: object = None        # result tensor
+    inp: object = None        # input tensor (resident per shape unless given)
+    nbytes: int = 0           # device bytes held while in flight
+    slot: int = -1
+
+    @property
+    def latency(self) -> float:
+        return self.t_done - self.arrival
+
+    @property
+    def points(self) -> int:
+        return self.shape[0] * self.shape[1] * self.shape[2]
+
+
+def kmax_of(shape) -> int:
+    nx, ny, nz = shape
+    return int(math.sqrt(float(nx) * nx + ny * ny + nz * nz) * 0.5 + 0.5)
+
+
+@dataclass
+class _Slot:
+    stream: object
+    batches: dict
+    event: object = None
+    reqs: list = field(default_factory=list)
+    busy: bool = False
+
+
+class Server:
+    """Continuous-batching transform server on the current CUDA device."""
+
+    def __init__(self, budget_bytes: float = 150e9, slots: int = 3, max_jobs: int = 64, window: int = 4,
+                 tuned: bool = False, keep_outputs: bool = True):
+        import torch
+        self.torch = torch
+        self.budget = int(budget_bytes)
+        self.max_jobs = max_jobs
+        self.window = window
+        self.tuned = tuned
+        self.keep_outputs = keep_outputs
+        self.plans = {}
+        # resident input grids, least recently used first; bounded by a
+        # quarter of the budget (grids in use by in-flight requests stay)
+        self.resident = collections.OrderedDict()   # (shape, precision, backward) -> tensor
+        self.resident_limit = self.budget // 4
+        self.in_use = collections.Counter()
+        self.resident_bytes = 0
+        self.in_flight_bytes = 0
+        self.peak_bytes = 0
+        self.peak_in_flight = 0
+        self.pending = collections.deque()
+        self.done = []
+        self.launches = 0
+        self.batch_sizes = []
+        self.slots = [_Slot(stream=torch.cuda.Stream(), batches={F32: Batch(F32), F64: Batch(F64)})
+                      for _ in range(slots)]
+        self.t0 = time.perf_counter()
+
+    # ------------------------------------------------------------ resources
+    def now(self) -> float:
+        return time.perf_counter() - self.t0
+
+    def plan(self, shape, precision) -> Plan:
+        key = (tuple(shape), precision)
+        p = self.plans.get(key)
+        if p is None:
+            if self.tuned:
+                from .autotune import tuned_plan
+                p = tuned_plan(tuple(shape), precision)
+            else:
+                p = Plan(*shape, precision=precision)
+            self.plans[key] = p
+        return p
+
+    def _dtypes(self, precision):
+        t = self.torch
+        return (t.float64, t.complex128) if precision == F64 else (t.float32, t.complex64)
+
+    def _input_key(self, req: Request):
+        return (tuple(req.shape), req.precision, req.kind == "backward")
+
+    def resident_input(self, shape, precision, kind, seed=0):
+        """The shape's input grid, created once on the device: U[-1,1) reals,
+        or for backward requests a complex N(0,1) spectrum."""
+        key = (tuple(shape), precision, kind == "backward")
+        x = self.resident.get(key)
+        if x is not None:
+            self.resident.move_to_end(key)
+            return x
+        t = self.torch
+        nx, ny, nz = shape
+        rdt, cdt = self._dtypes(precision)
+        g = t.Generator(device="cuda")
+        g.manual_seed(hash((tuple(shape), seed)) & 0x7FFFFFFF)
+        if kind == "backward":
+            x = t.randn((nz, ny, nx // 2 + 1), generator=g, device="cuda", dtype=cdt)
+        else:
+            x = t.rand((nz, ny, nx), generator=g, device="cuda", dtype=t.float64).mul_(2).sub_(1).to(rdt)
+        self.resident[key] = x
+        self.resident_bytes += x.numel() * x.element_size()
+        for k in list(self.resident):
+            if self.resident_bytes <= self.resident_limit or k == key:
+                break
+            if self.in_use[k] == 0:
+                old = self.resident.pop(k)
+                self.resident_bytes -= old.numel() * old.element_size()
+        return x
+
+    def request_bytes(self, req: Request) -> int:
+        """Device bytes a request holds while in flight: its input grid, its
+        output and its batch work buffer."""
+        p = self.plan(req.shape, req.precision)
+        nx, ny, nz = req.shape
+        rsz = 8 if req.precision == F64 else 4
+        real = nx * ny * nz * rsz
+        cplx = (nx // 2 + 1) * ny * nz * 2 * rsz
+        if req.kind == "forward":
+            io = real + cplx
+        elif req.kind == "backward":
+            io = cplx + real
+        else:
+            io = real + (kmax_of(req.shape) + 1) * 8
+        return io + p.work_bytes(KINDS[req.kind])
+
+    # ------------------------------------------------------------ the loop
+    def submit(self, req: Request) -> None:
+        req.precision = F64 if req.tol < F32_TOL else F32
+        self.pending.append(req)
+
+    def _launch(self, slot: _Slot, reqs) -> None:
+        t = self.torch
+        groups = {F32: [], F64: []}
+        for r in reqs:
+            p = self.plan(r.shape, r.precision)
+            rdt, cdt = self._dtypes(r.precision)
+            nx, ny, nz = r.shape
+            if r.inp is None:
+                r.inp = self.resident_input(r.shape, r.precision, r.kind)
+                self.in_use[self._input_key(r)] += 1
+            work = t.empty(p.work_bytes(KINDS[r.kind]), dtype=t.uint8, device="cuda")
+            if r.kind == "forward":
+                r.out = t.empty(p.complex_shape, dtype=cdt, device="cuda")
+                job = {"plan": p, "kind": JOB_FORWARD, "in": r.inp, "out": r.out, "work": work}
+            elif r.kind == "backward":
+                r.out = t.empty((nz, ny, nx), dtype=rdt, device="cuda")
+                job = {"plan": p, "kind": JOB_BACKWARD, "in": r.inp, "out": r.out, "work": work}
+            else:
+                r.out = t.empty(kmax_of(r.shape) + 1, dtype=t.float64, device="cuda")
+                job = {"plan": p, "kind": JOB_SPECTRUM, "in": r.inp, "out": r.out, "work": work,
+                       "kmax": kmax_of(r.shape), "scale": 1.0 / (nx * ny * nz), "flags": SPEC_HERMITIAN}
+            groups[r.precision].append(job)
+        # the slot's launch follows everything queued on the current stream
+        # (input grids generated there, allocations of the buffers above)
+        slot.stream.wait_stream(t.cuda.current_stream())
+        with t.cuda.stream(slot.stream):
+            for prec, jobs in groups.items():
+                if jobs:
+                    b = slot.batches[prec]
+                    b.set_jobs(jobs, window=self.window)
+                    b.launch(slot.stream)
+                    self.launches += 1
+            slot.event = t.cuda.Event()
+            slot.event.record(slot.stream)
+        slot.reqs = list(reqs)
+        slot.busy = True
+        self.batch_sizes.append(len(reqs))
+
+    def _retire(self, slot: _Slot) -> None:
+        now = self.now()
+        for prec, b in slot.batches.items():
+            if any(r.precision == prec for r in slot.reqs):
+                b.check(slot.stream)
+            b._keep = []  # release the work buffers
+        for r in slot.reqs:
+            r.t_done = now
+            self.in_flight_bytes -= r.nbytes
+            key = self._input_key(r)
+            if self.in_use[key] > 0:
+                self.in_use[key] -= 1
+            if not self.keep_outputs:
+                r.out = None
+                r.inp = None
+            self.done.append(r)
+        slot.reqs = []
+        slot.busy = False
+
+    def poll(self) -> bool:
+        """Retire finished slots, then fill free slots from the queue.
+        Returns True when something happened."""
+        acted = False
+        for s in self.slots:
+            if s.busy and s.event.query():
+                self._retire(s)
+                acted = True
+        for i, s in enumerate(self.slots):
+            if s.busy or not self.pending:
+                continue
+            take = []
+            while self.pending and len(take) < self.max_jobs:
+                r = self.pending[0]
+                nb = self.request_bytes(r)
+                if nb > self.budget:
+                    raise RuntimeError(f"request {r.rid} needs {nb} device bytes, above the device-memory "
+                                       f"budget of {self.budget}")
+                if self.in_flight_bytes + nb > self.budget:
+                    break
+                self.pending.popleft()
+                r.nbytes = nb
+                r.t_admit = self.now()
+                r.slot = i
+                self.in_flight_bytes += nb
+                take.append(r)
+            if not take:
+                break
+            self.peak_in_flight = max(self.peak_in_flight, self.in_flight_bytes)
+            self.peak_bytes = max(self.peak_bytes, self.resident_bytes + self.in_flight_bytes)
+            self._launch(s, take)
+            acted = True
+        return acted
+
+    def drain(self) -> None:
+        while self.pending or any(s.busy for s in self.slots):
+            if not self.poll():
+                time.sleep(20e-6)
+
+    def run(self, requests):
+        """Replays `requests` with their arrival times (seconds from the
+        start of the call) and returns them completed (outputs dropped at
+        completion unless the server keeps them)."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        self.t0 = time.perf_counter()
+        i = 0
+        n = len(reqs)
+        while i < n or self.pending or any(s.busy for s in self.slots):
+            now = self.now()
+            while i < n and reqs[i].arrival <= now:
+                self.submit(reqs[i])
+                i += 1
+            if not self.poll():
+                time.sleep(20e-6)
+        return reqs
+
+    def close(self) -> None:
+        for s in self.slots:
+            for b in s.batches.values():
+                b.close()
+        for p in self.plans.values():
+            p.close()
+        self.plans.clear()
+        self.resident.clear()
+
+
+# ------------------------------------------------------------------ workload
+def smooth_sides(lo: int = 32, hi: int = 512):
+    """All 2^a 3^b 5^c in [lo, hi]."""
+    out = []
+    a = 1
+    while a <= hi:
+        b = a
+        while b <= hi:
+            c = b
+            while c <= hi:
+                if c >= lo:
+                    out.append(c)
+                c *= 5
+            b *= 3
+        a *= 2
+    return sorted(set(out))
+
+
+def make_requests(n: int, seed: int = 5, lo: int = 32, hi: int = 512, mix=(4, 4, 2), f64_fraction: float = 0.1):
+    """n requests: kinds forward:backward:spectrum = mix, cubic or box grids
+    with sides log-uniform over the 2^a 3^b 5^c values in [lo, hi], and a
+    fraction asking for FP64 accuracy.  Arrival times are filled in by
+    poisson_arrivals."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    sides = np.array(smooth_sides(lo, hi))
+    logs = np.log(sides)
+    kinds = np.array(["forward", "backward", "spectrum"])
+    p = np.array(mix, dtype=float) / sum(mix)
+
+    def side():
+        u = rng.uniform(math.log(lo), math.log(hi))
+        return int(sides[np.argmin(np.abs(logs - u))])
+
+    reqs = []
+    for i in range(n):
+        if rng.random() < 0.5:
+            s = side()
+            shape = (s, s, s)
+        else:
+            shape = (side(), side(), side())
+        kind = str(rng.choice(kinds, p=p))
+        tol = 1e-12 if rng.random() < f64_fraction else F32_TOL
+        reqs.append(Request(rid=i, kind=kind, shape=shape, tol=tol))
+    return reqs
+
+
+def poisson_arrivals(reqs, rate: float, seed: int = 6):
+    """Exponential inter-arrival times at `rate` requests per second."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    for r in reqs:
+        t += rng.exponential(1.0 / rate)
+        r.arrival = t
+    return reqs
+
+
+def summarize(reqs, wall_s: float) -> dict:
+    import numpy as np
+    lat = np.array([r.latency for r in reqs]) * 1e3
+    pts = sum(r.points for r in reqs)
+    return {"requests": len(reqs), "p50_ms": round(float(np.percentile(lat, 50)), 3),
+            "p99_ms": round(float(np.percentile(lat, 99)), 3), "mean_ms": round(float(lat.mean()), 3),
+            "throughput_req_s": round(len(reqs) / wall_s, 1), "gpts_per_s": round(pts / wall_s / 1e9, 3),
+            "wall_s": round(wall_s, 3), "f64_requests": sum(1 for r in reqs if r.precision == F64)}
