@@ -18,8 +18,8 @@
 // small grid is still in the 129 MB L2 when its next pass reads it; a large
 // window gives each pass more parallel tiles.  The autotuner picks it.
 //
-// Visibility between CTAs: each thread fences after its stores, then the CTA
-// barrier, then one atomic increment of the pass counter; the waiting CTA's
+// Visibility between CTAs: the CTA barrier after a tile's stores, then thread
+// 0's gpu-scope fence and one atomic increment of the pass counter; the waiting CTA's
 // thread 0 polls the counter with ld.acquire.gpu and fences; the CTA then
 // reads the data through L2 only (ld.global.cg), so no stale L1 line from an
 // earlier pass is seen.
@@ -110,25 +110,43 @@ P3G_D bool wait_count(const int* cnt, int need, int* err) {
   }
 }
 
-// ctl[0] = next queue item, ctl[1] = error, ctl[2 + d] = finished tiles of pass d
+// Pass lookup: the first-item index of up to kFirstCache passes is copied to
+// shared memory at kernel start, so finding an item's pass is a binary
+// search in shared memory instead of a chain of dependent global loads.
+constexpr int kFirstCache = 1024;
+
+P3G_D int find_pass(const BatchPass* __restrict__ passes, const int* s_first, int npass, int it) {
+  int lo = 0, hi = npass - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    const int f = mid < kFirstCache ? s_first[mid] : passes[mid].first;
+    if (f <= it) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ctl[0] = next queue item, ctl[1] = error, ctl[2 + d] = finished tiles of pass d.
+// Thread 0 takes the ticket of the next item while the CTA works on the
+// current one, which hides the atomic's round trip.
 template <class P>
 __global__ void __launch_bounds__(kBatchThreads, 2)
     k_batch(const BatchPass* __restrict__ passes, int npass, int nitems, int* __restrict__ ctl) {
   using W = typename P::W;
   __shared__ int s_item, s_pass;
+  __shared__ int s_first[kFirstCache];
   W* sm = reinterpret_cast<W*>(p3g_smem);
+  for (int i = threadIdx.x; i < npass && i < kFirstCache; i += blockDim.x) s_first[i] = passes[i].first;
+  int ticket = 0;
+  if (threadIdx.x == 0) ticket = atomicAdd(&ctl[0], 1);
+  __syncthreads();
   for (;;) {
     if (threadIdx.x == 0) {
       int d = -1;
-      const int it = atomicAdd(&ctl[0], 1);
+      const int it = ticket;
       if (it < nitems && ld_relaxed(&ctl[1]) == 0) {
-        int lo = 0, hi = npass - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (passes[mid].first <= it) lo = mid;
-          else hi = mid - 1;
-        }
-        d = lo;
+        ticket = atomicAdd(&ctl[0], 1);  // next item, in flight during this one
+        d = find_pass(passes, s_first, npass, it);
         const int dep = passes[d].dep;
         if (dep >= 0 && !wait_count(&ctl[2 + dep], passes[dep].tiles, &ctl[1])) d = -1;
       }
@@ -162,9 +180,13 @@ __global__ void __launch_bounds__(kBatchThreads, 2)
         break;
       default: break;
     }
-    __threadfence();
+    // publish: the barrier orders every thread's stores before thread 0's
+    // gpu-scope fence and counter increment (the grid-barrier pattern)
     __syncthreads();
-    if (threadIdx.x == 0) atomicAdd(&ctl[2 + d], 1);
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(&ctl[2 + d], 1);
+    }
   }
 }
 

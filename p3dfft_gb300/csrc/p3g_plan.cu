@@ -202,8 +202,7 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   const int E = f64 ? PipeLimits<PathF64>::kE : PipeLimits<PathF32>::kE;
   const int n = ap.n;
   const int nh = n / 2 + 1;
-  int M = ap.M;
-  for (;; M /= 2) {
+  auto threads_for = [&](int M) {
     int t = (M * n + E - 1) / E;
     if (kind == 2) {
       const int maxi = E / 2 + 2;
@@ -211,19 +210,40 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
       t = t > t2 ? t : t2;
     }
     t = (t + 31) / 32 * 32;
-    if (t < 32) t = 32;
-    if (t <= max_threads) {
-      ap.pipe_threads = t;
-      break;
-    }
-    if (M == 1) return;
-  }
-  if (M != ap.M) return;  // keep one tile shape per axis
-  // buffer stride rounded to 1 KB so both buffers (TMA destinations) stay aligned
-  const size_t need = (size_t)(kind == 0 ? M * n : M * (ap.ls > 2 * nh ? ap.ls : 2 * nh)) * esize;
-  const size_t buf_bytes = (need + 1023) / 1024 * 1024;
+    return t < 32 ? 32 : t;
+  };
+  auto smem_for = [&](int M, size_t& buf_bytes) {
+    // buffer stride rounded to 1 KB so both buffers (TMA destinations) stay aligned
+    const size_t need = (size_t)(kind == 0 ? M * n : M * (ap.ls > 2 * nh ? ap.ls : 2 * nh)) * esize;
+    buf_bytes = (need + 1023) / 1024 * 1024;
+    return 1024 + 2 * buf_bytes + (size_t)ap.tw_cnt * 16 + 16;
+  };
+  // resident warps per SM for tile width M: 128 registers per thread, 2048
+  // threads and ~228 KB of shared memory per SM
+  auto warps_for = [&](int M) {
+    const int t = threads_for(M);
+    size_t bb;
+    const size_t sm = smem_for(M, bb);
+    int b = 65536 / (128 * t);
+    b = std::min(b, 2048 / t);
+    b = std::min(b, (int)((228 * 1024) / sm));
+    return b * t / 32;
+  };
+  // widest tile whose CTA fits the kernel; a narrower one (down to half of
+  // that, at least 2 lines) only when it keeps 1.5x more warps resident,
+  // e.g. 540-point lines whose 4-line tile needs 288 threads (one CTA of
+  // 9 warps per SM) against 160 threads for 2 lines (three CTAs)
+  int M = ap.M;
+  while (M > 1 && threads_for(M) > max_threads) M /= 2;
+  if (threads_for(M) > max_threads) return;
+  const int w0 = warps_for(M);
+  if (M >= 4 && 2 * warps_for(M / 2) >= 3 * w0) M /= 2;
+  ap.pipe_threads = threads_for(M);
+  ap.pipe_m = M;
+  ap.pipe_log2m = ilog2(M);
+  size_t buf_bytes = 0;
+  ap.pipe_smem = smem_for(M, buf_bytes);
   ap.buf_elems = (int)(buf_bytes / esize);
-  ap.pipe_smem = 1024 + 2 * buf_bytes + (size_t)ap.tw_cnt * 16 + 16;
   ap.pipe_ok = ap.pipe_smem <= 227 * 1024;
 }
 
@@ -377,6 +397,9 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
   s.xtiles = (s.X + ap.M - 1) / ap.M;
   const int esize = (int)sizeof(typename P::W);
   if (p->use_pipe && ap.pipe_ok && aligned_to(s.in, esize)) {
+    s.M = ap.pipe_m;
+    s.log2m = ap.pipe_log2m;
+    s.xtiles = (s.X + s.M - 1) / s.M;
     SPipeParams pp{};
     pp.s = s;
     pp.c.tiles_per_field = s.xtiles * s.O1;
@@ -389,13 +412,13 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
     CUtensorMap map;
     std::memset(&map, 0, sizeof(map));
     if (p->use_tma && s.in_xs == 1 && s.pre <= 1 && s.lmap_a0 >= s.L && s.lmap_a1 >= s.L) {
-      const int brows = pick_box_rows(s.L, ap.n, ap.M, esize);
-      if (brows > 0 && encode_strided_map(&map, s.in, esize, s.X, s.L, s.O1, nv, s.in_axis, s.in_o1, s.in_o2, ap.M,
+      const int brows = pick_box_rows(s.L, ap.n, s.M, esize);
+      if (brows > 0 && encode_strided_map(&map, s.in, esize, s.X, s.L, s.O1, nv, s.in_axis, s.in_o1, s.in_o2, s.M,
                                           brows)) {
         pp.use_tma = 1;
         pp.brows = brows;
         pp.nbox = (s.L + brows - 1) / brows;
-        pp.box_bytes = brows * ap.M * esize;
+        pp.box_bytes = brows * s.M * esize;
       }
     }
     const int slots = p->sm_count * ap.pipe_bps;
@@ -421,6 +444,9 @@ int run_x_r2c(p3g_plan p, XParams& x, int nv, cudaStream_t st) {
     int chunk = (int)us;
     if ((x.nx * us) % 16 == 0 && (x.in_field * us) % 16 == 0 && aligned_to(x.in, 16)) chunk = 16;
     else if ((x.nx * us) % 8 == 0 && (x.in_field * us) % 8 == 0 && aligned_to(x.in, 8)) chunk = 8;
+    x.M = ap.pipe_m;
+    x.log2m = ap.pipe_log2m;
+    x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
     XPipeParams xp{};
     xp.x = x;
     xp.chunk = chunk;
@@ -448,6 +474,9 @@ template <class P>
 int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st) {
   const AxisPlan& ap = p->ax_x;
   if (p->use_pipe && ap.pipe_ok) {
+    x.M = ap.pipe_m;
+    x.log2m = ap.pipe_log2m;
+    x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
     XPipeParams xp{};
     xp.x = x;
     xp.chunk = (int)sizeof(typename P::W);
@@ -827,7 +856,8 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
   {
     AxisPlan c2r = p->ax_x;
     size_pipe(c2r, 2, f64);
-    if (!c2r.pipe_ok || c2r.pipe_threads != p->ax_x.pipe_threads) p->ax_x.pipe_ok = false;
+    if (!c2r.pipe_ok || c2r.pipe_threads != p->ax_x.pipe_threads || c2r.pipe_m != p->ax_x.pipe_m)
+      p->ax_x.pipe_ok = false;
     p->ax_x.buf_elems = c2r.buf_elems;
     p->ax_x.pipe_smem = c2r.pipe_smem;
   }

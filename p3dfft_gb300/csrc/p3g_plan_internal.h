@@ -24,6 +24,7 @@ struct AxisPlan {
   int ls = 0, ps = 0;         // X axis: shared-memory line-pair stride and padding shift
   // pipelined kernels (p3g_pipe.cuh): same tile, double buffered
   bool pipe_ok = false;
+  int pipe_m = 1, pipe_log2m = 0;  // lines (columns) per pipelined tile
   int pipe_threads = 0;
   int buf_elems = 0;
   size_t pipe_smem = 0;
