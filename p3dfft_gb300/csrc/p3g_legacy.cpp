@@ -8,9 +8,11 @@
 // State follows the reference's module-level SAVE variables
 // (build/module.F90:101-176): one global plan set up by p3dfft_setup and torn
 // down by p3dfft_clean, 12 accumulating timers, overwrite flag.  Arrays may
-// be host memory (staged through device buffers, H2D and D2H copies inside the
-// call) or device memory (used in place).  Every call is synchronous like the
-// reference's.
+// be device memory or host memory: the kernels read and write host arrays in
+// place when the GPU can address them (page-locked memory, or any memory on a
+// host whose page tables the GPU uses), else they are staged through device
+// buffers with H2D and D2H copies inside the call.  Every call is synchronous
+// like the reference's.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -73,6 +75,32 @@ bool on_device(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Host arrays the kernels may read and write in place, without staging: page-
+// locked (registered) host memory, or any host memory when the GPU reaches
+// pageable memory through the host's page tables (a Grace host over
+// NVLink-C2C).  P3DFFT_GB_HOST_DIRECT=0 forces staging through device buffers.
+bool host_direct(const void* p) {
+  static int mode = -1;
+  static bool pageable = false;
+  if (mode < 0) {
+    const char* e = std::getenv("P3DFFT_GB_HOST_DIRECT");
+    mode = (e && *e == '0') ? 0 : 1;
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) == cudaSuccess)
+      pageable = v != 0;
+    cudaGetLastError();
+  }
+  if (!mode) return false;
+  if (pageable) return true;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost && a.devicePointer == p;
+}
+
 void* stage(int which, size_t bytes) {
   if (bytes > g_stage_bytes[which]) {
     if (g_stage[which]) cudaFree(g_stage[which]);
@@ -97,10 +125,14 @@ bool ready() {
 }
 
 // Runs one transform call with host or device arrays.  in_bytes/out_bytes
-// cover all nv fields.
+// cover all nv fields.  Host arrays are used in place only on the real-space
+// side (in_real / out_real): the X passes read and write whole contiguous
+// lines there, while the Z passes reach the wavenumber-space array in short
+// strided runs that cross the host link far slower than one bulk copy.
 template <class F>
-void run(const void* in, size_t in_bytes, void* out, size_t out_bytes, F&& call) {
-  const bool din = on_device(in), dout = on_device(out);
+void run(const void* in, size_t in_bytes, bool in_real, void* out, size_t out_bytes, bool out_real, F&& call) {
+  const bool din = on_device(in) || (in_real && host_direct(in));
+  const bool dout = on_device(out) || (out_real && host_direct(out));
   const void* dev_in = in;
   void* dev_out = out;
   if (!din) {
@@ -190,14 +222,14 @@ void p3dfft_get_mpi_info(int* taskid, int* ntasks, int* comm) {
 void p3dfft_ftran_r2c(real_t* A, real_t* B, unsigned char* op) {
   if (!ready()) return;
   const char* o = reinterpret_cast<const char*>(op);
-  run(A, rsize() * sizeof(real_t), B, csize() * 2 * sizeof(real_t),
+  run(A, rsize() * sizeof(real_t), true, B, csize() * 2 * sizeof(real_t), false,
       [&](const void* i, void* out) { return p3g_ftran_r2c(g_plan, i, out, o, 1, 0, 0, g_stream); });
 }
 
 void p3dfft_btran_c2r(real_t* A, real_t* B, unsigned char* op) {
   if (!ready()) return;
   const char* o = reinterpret_cast<const char*>(op);
-  run(A, csize() * 2 * sizeof(real_t), B, rsize() * sizeof(real_t),
+  run(A, csize() * 2 * sizeof(real_t), false, B, rsize() * sizeof(real_t), true,
       [&](const void* i, void* out) { return p3g_btran_c2r(g_plan, i, out, o, 1, 0, 0, g_stream); });
 }
 
@@ -209,7 +241,7 @@ void p3dfft_ftran_r2c_many(real_t* A, int* dim_in, real_t* B, int* dim_out, int*
   const char* o = reinterpret_cast<const char*>(op);
   const long long di = *dim_in, dout = *dim_out;
   const int n = *nv;
-  run(A, (size_t)di * n * sizeof(real_t), B, (size_t)dout * n * 2 * sizeof(real_t),
+  run(A, (size_t)di * n * sizeof(real_t), true, B, (size_t)dout * n * 2 * sizeof(real_t), false,
       [&](const void* i, void* out) { return p3g_ftran_r2c(g_plan, i, out, o, n, di, dout, g_stream); });
 }
 
@@ -221,14 +253,14 @@ void p3dfft_btran_c2r_many(real_t* A, int* dim_in, real_t* B, int* dim_out, int*
   const char* o = reinterpret_cast<const char*>(op);
   const long long di = *dim_in, dout = *dim_out;
   const int n = *nv;
-  run(A, (size_t)di * n * 2 * sizeof(real_t), B, (size_t)dout * n * sizeof(real_t),
+  run(A, (size_t)di * n * 2 * sizeof(real_t), false, B, (size_t)dout * n * sizeof(real_t), true,
       [&](const void* i, void* out) { return p3g_btran_c2r(g_plan, i, out, o, n, di, dout, g_stream); });
 }
 
 void p3dfft_cheby(real_t* A, real_t* B, real_t* Lz) {
   if (!ready()) return;
   const double lz = *Lz;
-  run(A, rsize() * sizeof(real_t), B, csize() * 2 * sizeof(real_t),
+  run(A, rsize() * sizeof(real_t), true, B, csize() * 2 * sizeof(real_t), false,
       [&](const void* i, void* out) { return p3g_cheby(g_plan, i, out, lz, 1, 0, 0, g_stream); });
 }
 
@@ -239,7 +271,7 @@ void p3dfft_cheby_many(real_t* A, int* dim_in, real_t* B, int* dim_out, int* nv,
   const double lz = *Lz;
   const long long di = *dim_in, dout = *dim_out;
   const int n = *nv;
-  run(A, (size_t)di * n * sizeof(real_t), B, (size_t)dout * n * 2 * sizeof(real_t),
+  run(A, (size_t)di * n * sizeof(real_t), true, B, (size_t)dout * n * 2 * sizeof(real_t), false,
       [&](const void* i, void* out) { return p3g_cheby(g_plan, i, out, lz, n, di, dout, g_stream); });
 }
 

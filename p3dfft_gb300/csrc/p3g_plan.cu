@@ -389,6 +389,17 @@ bool encode_strided_map(CUtensorMap* m, const void* base, int esize, long long X
 
 bool aligned_to(const void* ptr, size_t a) { return reinterpret_cast<uintptr_t>(ptr) % a == 0; }
 
+// Tensor maps (TMA) are only built over device memory; user arrays in host
+// memory that the kernels address directly are read with cp.async.
+bool device_memory(const void* ptr) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice;
+}
+
 template <class P>
 int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int nv, cudaStream_t st) {
   s.M = ap.M;
@@ -411,7 +422,8 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
     pp.chunk = esize;
     CUtensorMap map;
     std::memset(&map, 0, sizeof(map));
-    if (p->use_tma && s.in_xs == 1 && s.pre <= 1 && s.lmap_a0 >= s.L && s.lmap_a1 >= s.L) {
+    if (p->use_tma && s.in_xs == 1 && s.pre <= 1 && s.lmap_a0 >= s.L && s.lmap_a1 >= s.L &&
+        (!s.in_user || device_memory(s.in))) {
       const int brows = pick_box_rows(s.L, ap.n, s.M, esize);
       if (brows > 0 && encode_strided_map(&map, s.in, esize, s.X, s.L, s.O1, nv, s.in_axis, s.in_o1, s.in_o2, s.M,
                                           brows)) {

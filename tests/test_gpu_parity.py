@@ -348,3 +348,46 @@ def test_stride1_drop_in(torch_cuda):
     ref = orc.OraclePlan(nx, ny, nz, stride1=True)
     assert orc.normalised_linf(b, ref.ftran_r2c(a, "fft")) <= F64_TOL
     assert np.max(np.abs(r / (nx * ny * nz) - a)) <= orc.roundtrip_tolerance(nx * ny * nz)
+
+
+_HOST_PATH_SCRIPT = r"""
+import sys, numpy as np, torch
+import p3dfft_gb300 as pg
+nx, ny, nz = 48, 40, 36
+a = np.random.default_rng(3).uniform(-1, 1, (nz, ny, nx))
+out = {}
+pg.p3dfft_setup((1, 1), nx, ny, nz)
+b = np.zeros((nz, ny, nx // 2 + 1), dtype=np.complex128)       # pageable host arrays
+pg.p3dfft_ftran_r2c(a, b, "fft")
+r = np.zeros_like(a)
+pg.p3dfft_btran_c2r(b, r, "tff")
+pa = torch.from_numpy(a).pin_memory()                              # page-locked host arrays
+pb = torch.zeros((nz, ny, nx // 2 + 1), dtype=torch.complex128).pin_memory()
+pr = torch.zeros((nz, ny, nx), dtype=torch.float64).pin_memory()
+pg.p3dfft_ftran_r2c(pa, pb, "ffc")
+pg.p3dfft_btran_c2r(pb, pr, "cff")
+pg.p3dfft_clean()
+np.savez(sys.argv[1], b=b, r=r, pb=pb.numpy(), pr=pr.numpy())
+"""
+
+
+@pytest.mark.parametrize("direct", ["1", "0"])
+def test_host_arrays_direct_and_staged(torch_cuda, tmp_path, direct):
+    # host arrays reached by the kernels in place (P3DFFT_GB_HOST_DIRECT=1,
+    # the default where the GPU can address them) or staged through device
+    # buffers (=0): the same results, matching the oracle
+    import os
+    import subprocess
+    import sys
+    f = tmp_path / "out.npz"
+    env = dict(os.environ, P3DFFT_GB_HOST_DIRECT=direct)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.run([sys.executable, "-c", _HOST_PATH_SCRIPT, str(f)], check=True, env=env, cwd=root, timeout=300)
+    d = np.load(f)
+    nx, ny, nz = 48, 40, 36
+    a = np.random.default_rng(3).uniform(-1, 1, (nz, ny, nx))
+    ref = orc.OraclePlan(nx, ny, nz)
+    assert orc.normalised_linf(d["b"], ref.ftran_r2c(a, "fft")) <= F64_TOL
+    assert orc.normalised_linf(d["r"], ref.btran_c2r(ref.ftran_r2c(a, "fft"), "tff")) <= F64_TOL
+    assert orc.normalised_linf(d["pb"], ref.ftran_r2c(a, "ffc")) <= F64_TOL
+    assert orc.normalised_linf(d["pr"], ref.btran_c2r(ref.ftran_r2c(a, "ffc"), "cff")) <= F64_TOL
