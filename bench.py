@@ -459,12 +459,26 @@ def run_e2e(torch, pg, grid, ops, x_dev, steps, dev):
         pg.p3dfft_clean()
     r_bytes = nx * ny * nz * 8
     c_bytes = (nx // 2 + 1) * ny * nz * 16
+    # host-link bandwidth seen by pinned copies of the same arrays (1 GiB each way)
+    link = {}
+    n = min(host_in.numel(), 1 << 27)
+    dbuf = torch.empty(n, dtype=torch.float64, device=dev)
+    hflat = host_in.view(-1)[:n]
+    for name, fn in (("h2d", lambda: dbuf.copy_(hflat, non_blocking=True)),
+                     ("d2h", lambda: hflat.copy_(dbuf, non_blocking=True))):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        link[name] = round(n * 8 / (time.perf_counter() - t) / 1e9, 1)
+    del dbuf
     return {"value": round(nx * ny * nz / dt / 1e9, 3), "unit": UNIT, "ms_per_step": round(dt * 1e3, 3),
             "h2d_bytes_per_step": r_bytes + c_bytes, "d2h_bytes_per_step": c_bytes + r_bytes,
             "path": "libp3dfft.so p3dfft_ftran_r2c + p3dfft_btran_c2r, pinned host arrays: the real arrays "
                     "read/written in place by the X passes over the host link, the complex arrays staged by "
                     "cudaMemcpyAsync",
-            "host_link_gbs": {"h2d": 211.6, "d2h": 193.6, "source": "copy-engine and kernel probe on this GPU"}}
+            "host_link_gbs": link}
 
 
 # ------------------------------------------------------------ CPU arms
