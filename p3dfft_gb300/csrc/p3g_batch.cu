@@ -45,6 +45,8 @@ struct BatchPass {
   int first;   // queue index of its first item
   int dep;     // pass that must be complete first, -1 = none
   int rows_per_item;  // spectrum passes
+  int pipe;    // 1: tiles go through the double-buffered path (cp.async prefetch)
+  int chunk;   // X r2c: bytes per cp.async copy of the real lines
   int pad_;
   const StagePlan* sp;
   const float4* tw;
@@ -60,6 +62,38 @@ constexpr int kBatchSpinLimit = 1 << 22;  // polls of ~1 us: about 4 s
 // kElemsPerThread x 256 = 4096 points.
 constexpr int kBatchThreads = 256;
 constexpr int kBatchTile = kElemsPerThread * kBatchThreads;
+
+// Points per thread of the double-buffered path (as the pipelined pass
+// kernels): 8 on F64, 16 on F32.
+template <bool F64>
+__host__ __device__ constexpr int batch_pipe_elems() { return F64 ? 8 : 16; }
+
+// Double-buffered path: halve the tile width until the tile fits E points per
+// thread (c2r: the Hermitian merge holds E/2 + 2 items per thread); returns
+// the buffer size in elements (0 when it cannot fit).
+size_t pipe_fit_x(XParams& x, bool c2r, int E) {
+  const int nh = x.nx / 2 + 1;
+  auto fits = [&](int M) {
+    return (long long)M * x.nx <= (long long)E * kBatchThreads &&
+           (!c2r || (long long)M * nh <= (long long)(E / 2 + 2) * kBatchThreads);
+  };
+  while (x.M > 1 && !fits(x.M)) {
+    x.M >>= 1;
+    x.log2m--;
+  }
+  if (!fits(x.M)) return 0;
+  x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
+  return (size_t)x.M * (x.LS > 2 * nh ? x.LS : 2 * nh);
+}
+size_t pipe_fit_s(SParams& s, int E) {
+  while (s.M > 1 && (long long)s.M * s.N > (long long)E * kBatchThreads) {
+    s.M >>= 1;
+    s.log2m--;
+  }
+  if ((long long)s.M * s.N > (long long)E * kBatchThreads) return 0;
+  s.xtiles = (s.X + s.M - 1) / s.M;
+  return (size_t)s.M * s.N;
+}
 
 // Halve the plan's tile width until one tile fits the batch CTA; returns the
 // tile's shared-memory bytes (0 when even one line is too long).
@@ -126,68 +160,170 @@ P3G_D int find_pass(const BatchPass* __restrict__ passes, const int* s_first, in
   return lo;
 }
 
+// cp.async copies of a double-buffered item's input tile into buf.
+template <class P>
+P3G_D void batch_issue(const BatchPass& bp, int tile, typename P::W* buf) {
+  switch (bp.kind) {
+    case kBXr2c: xr2c_copy<P>(bp.x, bp.chunk, buf, tile * bp.x.M, 0); break;
+    case kBXc2r: xc2r_copy<P>(bp.x, buf, tile * bp.x.M, 0); break;
+    default: {
+      const int o1 = tile / bp.s.xtiles;
+      strided_copy<P>(bp.s, buf, tile - o1 * bp.s.xtiles, o1, 0);
+      break;
+    }
+  }
+}
+
+// Transform and store a double-buffered item whose tile is in buf.
+template <class P>
+P3G_D void batch_process_pipe(const BatchPass& bp, int tile, typename P::W* buf) {
+  constexpr int E = batch_pipe_elems<P::kF64>();
+  switch (bp.kind) {
+    case kBXr2c: {
+      xr2c_pack<P, E>(bp.x, buf);
+      Tile<P> t{buf, nullptr, bp.x.M, bp.x.log2m, bp.x.LS, 1, bp.x.ps};
+      cta_fft<P, -1, E>(t, bp.sp, bp.tw);
+      xr2c_store<P>(bp.x, buf, tile * bp.x.M, 0);
+      break;
+    }
+    case kBXc2r: {
+      xc2r_merge<P, E / 2 + 2>(bp.x, buf);
+      Tile<P> t{buf, nullptr, bp.x.M, bp.x.log2m, bp.x.LS, 1, bp.x.ps};
+      cta_fft<P, 1, E>(t, bp.sp, bp.tw);
+      xc2r_store<P>(bp.x, buf, tile * bp.x.M, 0);
+      break;
+    }
+    default: {
+      const int o1 = tile / bp.s.xtiles;
+      strided_fix<P>(bp.s, false, buf);
+      Tile<P> t{buf, nullptr, bp.s.M, bp.s.log2m, 1, bp.s.M};
+      if (bp.kind == kBFwd) cta_fft<P, -1, E>(t, bp.sp, bp.tw);
+      else cta_fft<P, 1, E>(t, bp.sp, bp.tw);
+      strided_store<P>(bp.s, buf, tile - o1 * bp.s.xtiles, o1, 0);
+      break;
+    }
+  }
+}
+
+// Single-tile items (plans with generic prime stages, which need a scratch
+// tile), spectrum chunks and histogram clears; sm spans both buffers.  Kept
+// out of line so that its registers do not weigh on the double-buffered path.
+template <class P>
+__device__ __noinline__ void batch_process_single(const BatchPass& bp, int tile, typename P::W* sm) {
+  switch (bp.kind) {
+    case kBXr2c: x_r2c_tile<P, true>(bp.x, bp.sp, bp.tw, sm, tile, 0); break;
+    case kBFwd: strided_tile<P, -1, true>(bp.s, bp.sp, bp.tw, sm, tile); break;
+    case kBBwd: strided_tile<P, 1, true>(bp.s, bp.sp, bp.tw, sm, tile); break;
+    case kBXc2r: x_c2r_tile<P, true>(bp.x, bp.sp, bp.tw, sm, tile, 0); break;
+    case kBSpec: {
+      double* hist = reinterpret_cast<double*>(sm);
+      const int nwarps = blockDim.x >> 5;
+      for (int i = threadIdx.x; i < nwarps * (bp.spec.kmax + 1); i += blockDim.x) hist[i] = 0.0;
+      __syncthreads();
+      const int r0 = tile * bp.rows_per_item;
+      const int r1 = min(r0 + bp.rows_per_item, bp.spec.rows);
+      spectrum_rows<P, true>(bp.spec, hist, r0 + (int)(threadIdx.x >> 5), r1, nwarps, 0);
+      __syncthreads();
+      spectrum_flush(bp.spec, hist, nwarps, 0);
+      break;
+    }
+    case kBZero:
+      for (int i = threadIdx.x; i <= bp.spec.kmax; i += blockDim.x) bp.spec.E[i] = 0.0;
+      break;
+    default: break;
+  }
+}
+
 // ctl[0] = next queue item, ctl[1] = error, ctl[2 + d] = finished tiles of pass d.
-// Thread 0 takes the ticket of the next item while the CTA works on the
-// current one, which hides the atomic's round trip.
+//
+// Each CTA holds a current item and, taken while the current one is worked
+// on, the ticket of the next.  When the next item is double-buffered and its
+// dependency is already complete, its tile is copied into the other buffer
+// (cp.async) while the current tile is transformed; otherwise the CTA waits
+// for the dependency after finishing the current item and loads then.
 template <class P>
 __global__ void __launch_bounds__(kBatchThreads, 2)
-    k_batch(const BatchPass* __restrict__ passes, int npass, int nitems, int* __restrict__ ctl) {
+    k_batch(const BatchPass* __restrict__ passes, int npass, int nitems, int* __restrict__ ctl, int buf_elems) {
   using W = typename P::W;
-  __shared__ int s_item, s_pass;
   __shared__ int s_first[kFirstCache];
-  W* sm = reinterpret_cast<W*>(p3g_smem);
+  __shared__ int s_item, s_pass, s_ready;
+  W* const buf0 = reinterpret_cast<W*>(p3g_smem);
   for (int i = threadIdx.x; i < npass && i < kFirstCache; i += blockDim.x) s_first[i] = passes[i].first;
-  int ticket = 0;
-  if (threadIdx.x == 0) ticket = atomicAdd(&ctl[0], 1);
   __syncthreads();
-  for (;;) {
+  // first item: wait for its dependency, then load
+  if (threadIdx.x == 0) {
+    const int it = atomicAdd(&ctl[0], 1);
+    int d = -1;
+    if (it < nitems && ld_relaxed(&ctl[1]) == 0) {
+      d = find_pass(passes, s_first, npass, it);
+      const int dep = passes[d].dep;
+      if (dep >= 0 && !wait_count(&ctl[2 + dep], passes[dep].tiles, &ctl[1])) d = -1;
+    }
+    s_item = it;
+    s_pass = d;
+  }
+  __syncthreads();
+  int cur = s_item, dc = s_pass, b = 0;
+  if (dc >= 0 && passes[dc].pipe) batch_issue<P>(passes[dc], cur - passes[dc].first, buf0);
+  cp_async_commit();
+#pragma unroll 1
+  while (dc >= 0) {
+    __syncthreads();  // everyone has read s_item / s_pass of the current item
     if (threadIdx.x == 0) {
-      int d = -1;
-      const int it = ticket;
+      const int it = atomicAdd(&ctl[0], 1);
+      int d = -1, ready = 0;
       if (it < nitems && ld_relaxed(&ctl[1]) == 0) {
-        ticket = atomicAdd(&ctl[0], 1);  // next item, in flight during this one
         d = find_pass(passes, s_first, npass, it);
         const int dep = passes[d].dep;
-        if (dep >= 0 && !wait_count(&ctl[2 + dep], passes[dep].tiles, &ctl[1])) d = -1;
+        ready = dep < 0 || ld_acquire(&ctl[2 + dep]) >= passes[dep].tiles;
+        if (ready) __threadfence();
       }
       s_item = it;
       s_pass = d;
+      s_ready = ready;
     }
     __syncthreads();
-    const int d = s_pass;
-    if (d < 0) break;
-    const BatchPass& bp = passes[d];
-    const int tile = s_item - bp.first;
-    switch (bp.kind) {
-      case kBXr2c: x_r2c_tile<P, true>(bp.x, bp.sp, bp.tw, sm, tile, 0); break;
-      case kBFwd: strided_tile<P, -1, true>(bp.s, bp.sp, bp.tw, sm, tile); break;
-      case kBBwd: strided_tile<P, 1, true>(bp.s, bp.sp, bp.tw, sm, tile); break;
-      case kBXc2r: x_c2r_tile<P, true>(bp.x, bp.sp, bp.tw, sm, tile, 0); break;
-      case kBSpec: {
-        double* hist = reinterpret_cast<double*>(p3g_smem);
-        const int nwarps = blockDim.x >> 5;
-        for (int i = threadIdx.x; i < nwarps * (bp.spec.kmax + 1); i += blockDim.x) hist[i] = 0.0;
-        __syncthreads();
-        const int r0 = tile * bp.rows_per_item;
-        const int r1 = min(r0 + bp.rows_per_item, bp.spec.rows);
-        spectrum_rows<P, true>(bp.spec, hist, r0 + (int)(threadIdx.x >> 5), r1, nwarps, 0);
-        __syncthreads();
-        spectrum_flush(bp.spec, hist, nwarps, 0);
-        break;
-      }
-      case kBZero:
-        for (int i = threadIdx.x; i <= bp.spec.kmax; i += blockDim.x) bp.spec.E[i] = 0.0;
-        break;
-      default: break;
+    const int nxt = s_item, dn = s_pass;
+    const bool ready = s_ready != 0;
+    const BatchPass& bc = passes[dc];
+    const bool pipe = bc.pipe != 0;
+    bool prefetched = false;
+    if (pipe && dn >= 0 && ready && passes[dn].pipe) {
+      batch_issue<P>(passes[dn], nxt - passes[dn].first, buf0 + (b ^ 1) * buf_elems);
+      prefetched = true;
+    }
+    cp_async_commit();
+    if (pipe) {
+      cp_async_wait<1>();
+      __syncthreads();
+      batch_process_pipe<P>(bc, cur - bc.first, buf0 + b * buf_elems);
+    } else {
+      batch_process_single<P>(bc, cur - bc.first, buf0);
     }
     // publish: the barrier orders every thread's stores before thread 0's
     // gpu-scope fence and counter increment (the grid-barrier pattern)
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
-      atomicAdd(&ctl[2 + d], 1);
+      atomicAdd(&ctl[2 + dc], 1);
+    }
+    cur = nxt;
+    dc = dn;
+    b ^= 1;
+    if (dc >= 0 && !prefetched) {
+      if (!ready) {
+        if (threadIdx.x == 0) {
+          const int dep = passes[dc].dep;
+          s_ready = wait_count(&ctl[2 + dep], passes[dep].tiles, &ctl[1]) ? 1 : 0;
+        }
+        __syncthreads();
+        if (!s_ready) dc = -1;
+      }
+      if (dc >= 0 && passes[dc].pipe) batch_issue<P>(passes[dc], cur - passes[dc].first, buf0 + b * buf_elems);
+      cp_async_commit();
     }
   }
+  cp_async_wait<0>();
 }
 
 // Opts the kernel in to the largest dynamic shared memory the device allows
@@ -219,9 +355,9 @@ cudaError_t batch_config(size_t smem, int& threads, int& per_sm, size_t& max_dyn
 }
 
 template <class P>
-cudaError_t batch_launch(const BatchPass* d_pass, int npass, int nitems, int* ctl, int grid, int threads,
-                         size_t smem, cudaStream_t st) {
-  k_batch<P><<<grid, threads, smem, st>>>(d_pass, npass, nitems, ctl);
+cudaError_t batch_launch(const BatchPass* d_pass, int npass, int nitems, int* ctl, int buf_elems, int grid,
+                         int threads, size_t smem, cudaStream_t st) {
+  k_batch<P><<<grid, threads, smem, st>>>(d_pass, npass, nitems, ctl, buf_elems);
   return cudaGetLastError();
 }
 
@@ -259,6 +395,7 @@ struct p3g_batch_s {
   size_t ctl_cap = 0;
   int npass = 0, nitems = 0;
   size_t smem = 0;
+  int buf_elems = 0;
   int threads = 0, grid = 0;
   cudaStream_t upload = nullptr;
   cudaGraph_t graph = nullptr;
@@ -321,7 +458,9 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
   const int nwarps = threads / 32;
   // per job: its chain of passes
   std::vector<std::vector<BatchPass>> chains(njobs);
-  size_t smem = 0;
+  size_t smem = 0;        // single-tile and spectrum items (bytes)
+  size_t buf_elems = 0;   // one buffer of the double-buffered items (elements)
+  const int pipe_e = f64 ? batch_pipe_elems<true>() : batch_pipe_elems<false>();
   for (int j = 0; j < njobs; ++j) {
     const p3g_job& jb = jobs[j];
     p3g_plan p = jb.plan;
@@ -338,28 +477,59 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
     void* cplx = L.cplx ? w + L.wa + L.wb : nullptr;
     const StagePlan* dsp = p->d_sp;
     bool fits = true;
+    const size_t es = p->esize();
+    // double-buffered when the axis has no generic prime stage and its tile
+    // fits the pipelined CTA; else single-tile (scratch tile, no prefetch)
     auto x_pass = [&](int kind, const XParams& x) {
       BatchPass q{};
       q.kind = kind;
       q.x = x;
-      const size_t need = fit_x(q.x, p->ax_x, p->esize());
-      fits = fits && need > 0;
+      const AxisPlan& ap = p->ax_x;
+      size_t pe = 0;
+      if (!ap.sp.has_generic && ap.sp.nstages > 0 && x.nx >= 2) {
+        XParams t = x;
+        pe = pipe_fit_x(t, kind == kBXc2r, pipe_e);
+        if (pe) q.x = t;
+      }
+      if (pe) {
+        q.pipe = 1;
+        buf_elems = std::max(buf_elems, pe);
+        const size_t ur = f64 ? 8 : 4;
+        q.chunk = (int)ur;
+        const uintptr_t a = reinterpret_cast<uintptr_t>(x.in);
+        if ((x.nx * ur) % 16 == 0 && a % 16 == 0) q.chunk = 16;
+        else if ((x.nx * ur) % 8 == 0 && a % 8 == 0) q.chunk = 8;
+      } else {
+        const size_t need = fit_x(q.x, ap, es);
+        fits = fits && need > 0;
+        smem = std::max(smem, need);
+      }
       q.tiles = q.x.tiles;
-      q.sp = dsp + p->ax_x.sp_index;
+      q.sp = dsp + ap.sp_index;
       q.tw = p->d_tw;
-      smem = std::max(smem, need);
       chains[j].push_back(q);
     };
     auto s_pass = [&](int kind, const SParams& s, const AxisPlan& ap) {
       BatchPass q{};
       q.kind = kind;
       q.s = s;
-      const size_t need = fit_s(q.s, ap, p->esize());
-      fits = fits && need > 0;
+      size_t pe = 0;
+      if (!ap.sp.has_generic && ap.sp.nstages > 0 && s.N >= 2) {
+        SParams t = s;
+        pe = pipe_fit_s(t, pipe_e);
+        if (pe) q.s = t;
+      }
+      if (pe) {
+        q.pipe = 1;
+        buf_elems = std::max(buf_elems, pe);
+      } else {
+        const size_t need = fit_s(q.s, ap, es);
+        fits = fits && need > 0;
+        smem = std::max(smem, need);
+      }
       q.tiles = q.s.xtiles * q.s.O1;
       q.sp = dsp + ap.sp_index;
       q.tw = p->d_tw;
-      smem = std::max(smem, need);
       chains[j].push_back(q);
     };
     const long long rsize = (long long)p->nx * p->ny * p->nz;
@@ -401,6 +571,11 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
       smem = std::max(smem, (size_t)nwarps * (q.spec.kmax + 1) * sizeof(double));
       chains[j].push_back(q);
     }
+  }
+  {
+    const size_t es = f64 ? 16 : 8;
+    buf_elems = (buf_elems + 1) / 2 * 2;  // keeps the second buffer 16-byte aligned
+    smem = std::max(smem, 2 * buf_elems * es);
   }
   if (smem > 227 * 1024) return fail(P3G_E_UNSUPPORTED, "a job's tile exceeds shared memory");
   // queue: windows of jobs, pass-major inside a window
@@ -462,6 +637,7 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
   b->npass = (int)b->host.size();
   b->nitems = (int)items;
   b->smem = smem;
+  b->buf_elems = (int)buf_elems;
   b->threads = thr;
   const long long slots = (long long)b->sm_count * per_sm;
   b->grid = (int)std::max(1LL, std::min(slots, items));
@@ -473,8 +649,10 @@ static int batch_enqueue(p3g_batch b, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(b->d_ctl, 0, ctl_bytes, st);
   if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch clear: ") + cudaGetErrorString(e));
   e = b->prec == P3G_F64
-          ? batch_launch<PathF64>(b->d_pass, b->npass, b->nitems, b->d_ctl, b->grid, b->threads, b->smem, st)
-          : batch_launch<PathF32>(b->d_pass, b->npass, b->nitems, b->d_ctl, b->grid, b->threads, b->smem, st);
+          ? batch_launch<PathF64>(b->d_pass, b->npass, b->nitems, b->d_ctl, b->buf_elems, b->grid, b->threads,
+                                  b->smem, st)
+          : batch_launch<PathF32>(b->d_pass, b->npass, b->nitems, b->d_ctl, b->buf_elems, b->grid, b->threads,
+                                  b->smem, st);
   if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
   return P3G_OK;
 }

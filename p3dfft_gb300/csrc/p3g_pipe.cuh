@@ -89,29 +89,14 @@ P3G_D void strided_decode(const SPipeParams& q, int tile, int& xt, int& o1, int&
   xt = r - o1 * q.s.xtiles;
 }
 
-// Copies of one tile into buffer b.  TMA: thread 0 arms the barrier and
-// issues the boxes.  cp.async: every thread, one commit group per call; the
-// DCT-I/DST-I extension rows are extra copies of the same elements (the
-// DST-I negation happens in the fix-up step).
+// cp.async copies of one strided tile (columns xt*M.., row block o1, field
+// o2) into dst, without a commit; the DCT-I/DST-I extension rows are extra
+// copies of the same elements (the DST-I negation happens in the fix-up
+// step).
 template <class P>
-P3G_D void strided_issue(const SPipeParams& q, const CUtensorMap* tin, int tile, int b) {
+P3G_D void strided_copy(const SParams& s, typename P::W* dst, int xt, int o1, int o2) {
   using W = typename P::W;
-  const StridedSmem<P> sm = strided_smem<P>(q.c);
-  W* dst = sm.buf0 + b * q.c.buf_elems;
-  const SParams& s = q.s;
   const int M = s.M, L = s.L;
-  int xt, o1, o2;
-  strided_decode(q, tile, xt, o1, o2);
-  if (q.use_tma) {
-    if (threadIdx.x == 0) {
-      constexpr int kWords = sizeof(W) / 4;
-      fence_proxy_async_smem();
-      mbar_arrive_expect_tx(&sm.mbar[b], (uint32_t)(q.nbox * q.box_bytes));
-      for (int i = 0; i < q.nbox; ++i)
-        tma_load_4d(dst + i * q.brows * M, tin, &sm.mbar[b], xt * M * kWords, i * q.brows, o1, o2);
-    }
-    return;
-  }
   const long long ib = (long long)o1 * s.in_o1 + (long long)o2 * s.in_o2 + (long long)xt * M * s.in_xs;
   const char* in = static_cast<const char*>(s.in);
   constexpr int esz = (int)sizeof(W);
@@ -156,15 +141,93 @@ P3G_D void strided_issue(const SPipeParams& q, const CUtensorMap* tin, int tile,
   } else {
     for (int e = threadIdx.x; e < M * L; e += T) one(e & (M - 1), e >> s.log2m);
   }
+}
+
+// Copies of one tile into buffer b.  TMA: thread 0 arms the barrier and
+// issues the boxes.  cp.async: every thread, one commit group per call.
+template <class P>
+P3G_D void strided_issue(const SPipeParams& q, const CUtensorMap* tin, int tile, int b) {
+  using W = typename P::W;
+  const StridedSmem<P> sm = strided_smem<P>(q.c);
+  W* dst = sm.buf0 + b * q.c.buf_elems;
+  int xt, o1, o2;
+  strided_decode(q, tile, xt, o1, o2);
+  if (q.use_tma) {
+    if (threadIdx.x == 0) {
+      constexpr int kWords = sizeof(W) / 4;
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&sm.mbar[b], (uint32_t)(q.nbox * q.box_bytes));
+      for (int i = 0; i < q.nbox; ++i)
+        tma_load_4d(dst + i * q.brows * q.s.M, tin, &sm.mbar[b], xt * q.s.M * kWords, i * q.brows, o1, o2);
+    }
+    return;
+  }
+  strided_copy<P>(q.s, dst, xt, o1, o2);
   cp_async_commit();
+}
+
+// Fix-up of a loaded strided tile, element-wise in place: user format ->
+// working format, DST-I negation, DCT-I mirror after a TMA load (tma).
+// Ends with a barrier when it changed anything.
+template <class P>
+P3G_D void strided_fix(const SParams& s, bool tma, typename P::W* sm) {
+  using W = typename P::W;
+  using C = typename P::C;
+  const bool raw_user = s.in_user != 0;
+  if (raw_user || s.pre == 2 || (tma && s.pre == 1)) {
+    const int M = s.M, L = s.L;
+    const int rows = tma ? L : s.N;
+    for (int e = threadIdx.x; e < M * rows; e += blockDim.x) {
+      const int m = e & (M - 1);
+      const int j = e >> s.log2m;
+      C v = raw_user ? P::from_uc(reinterpret_cast<const typename P::UC*>(sm)[j * M + m]) : P::from_w(sm[j * M + m]);
+      if (s.pre == 2 && j >= L + 2) v = cneg(v);
+      const W w = P::to_w(v);
+      sm[j * M + m] = w;
+      if (tma && s.pre == 1 && j >= 1 && j <= L - 2) sm[(2 * (L - 1) - j) * M + m] = w;
+    }
+    __syncthreads();
+  }
+}
+
+// Store of a transformed strided tile with the pruning map and the output
+// format (DST-I output rows k+1 times i).
+template <class P>
+P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int o1, int o2) {
+  using C = typename P::C;
+  const int M = s.M;
+  const int x0 = xt * M;
+  const long long obase = (long long)o1 * s.out_o1 + (long long)o2 * s.out_o2 + (long long)x0 * s.out_xs;
+  auto one = [&](int m, int jo) {
+    const int k = jo < s.smap_s0 ? jo : jo + s.smap_d;
+    C v;
+    if (s.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
+    else v = P::from_w(sm[k * M + m]);
+    store_elem<P>(s.out, s.out_user, obase + (long long)m * s.out_xs + (long long)jo * s.out_axis, v);
+  };
+  const int T = blockDim.x;
+  if (s.out_xs != 1) {  // rows adjacent in memory (STRIDE1 user layout): rows fastest
+    const FastDiv div_lo(s.Lout);
+    for (int e = threadIdx.x; e < M * s.Lout; e += T) {
+      const int m = (int)div_lo.div(e);
+      if (x0 + m < s.X) one(m, e - m * s.Lout);
+    }
+  } else if ((T & (M - 1)) == 0) {
+    const int m = threadIdx.x & (M - 1);
+    if (x0 + m < s.X)
+      for (int jo = threadIdx.x >> s.log2m; jo < s.Lout; jo += T >> s.log2m) one(m, jo);
+  } else {
+    for (int e = threadIdx.x; e < M * s.Lout; e += T) {
+      const int m = e & (M - 1);
+      if (x0 + m < s.X) one(m, e >> s.log2m);
+    }
+  }
 }
 
 template <class P, int DIR>
 __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMinBlocks)
     k_strided_pipe(const __grid_constant__ CUtensorMap tin, const __grid_constant__ SPipeParams pp,
                    const StagePlan* __restrict__ sp, const float4* __restrict__ tw_g) {
-  using W = typename P::W;
-  using C = typename P::C;
   {
     const StridedSmem<P> sm = strided_smem<P>(pp.c);
     for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) sm.tw[i] = __ldg(tw_g + pp.c.tw_base + i);
@@ -193,28 +256,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       else cp_async_wait<1>();
     }
     if (__syncthreads_or(!ok)) break;
-    {
-      // fix-up, element-wise in place: user format -> working format, DST-I
-      // negation, DCT-I mirror after a TMA load
-      const SPipeParams& q = pp;
-      const SParams& s = q.s;
-      const bool raw_user = s.in_user != 0;
-      if (raw_user || s.pre == 2 || (q.use_tma && s.pre == 1)) {
-        W* sm = strided_smem<P>(q.c).buf0 + b * q.c.buf_elems;
-        const int M = s.M, L = s.L;
-        const int rows = q.use_tma ? L : s.N;
-        for (int e = threadIdx.x; e < M * rows; e += blockDim.x) {
-          const int m = e & (M - 1);
-          const int j = e >> s.log2m;
-          C v = raw_user ? P::from_uc(reinterpret_cast<const typename P::UC*>(sm)[j * M + m]) : P::from_w(sm[j * M + m]);
-          if (s.pre == 2 && j >= L + 2) v = cneg(v);
-          const W w = P::to_w(v);
-          sm[j * M + m] = w;
-          if (q.use_tma && s.pre == 1 && j >= 1 && j <= L - 2) sm[(2 * (L - 1) - j) * M + m] = w;
-        }
-        __syncthreads();
-      }
-    }
+    strided_fix<P>(pp.s, pp.use_tma != 0, strided_smem<P>(pp.c).buf0 + b * pp.c.buf_elems);
     {
       const SPipeParams& q = pp;
       const StridedSmem<P> sm = strided_smem<P>(q.c);
@@ -222,38 +264,9 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       cta_fft<P, DIR, PipeLimits<P>::kE>(t, sp, sm.tw, q.c.tw_base);
     }
     {
-      const SPipeParams& q = pp;
-      const SParams& s = q.s;
-      const W* sm = strided_smem<P>(q.c).buf0 + b * q.c.buf_elems;
-      const int M = s.M;
       int xt, o1, o2;
-      strided_decode(q, tile, xt, o1, o2);
-      const int x0 = xt * M;
-      const long long obase = (long long)o1 * s.out_o1 + (long long)o2 * s.out_o2 + (long long)x0 * s.out_xs;
-      auto one = [&](int m, int jo) {
-        const int k = jo < s.smap_s0 ? jo : jo + s.smap_d;
-        C v;
-        if (s.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
-        else v = P::from_w(sm[k * M + m]);
-        store_elem<P>(s.out, s.out_user, obase + (long long)m * s.out_xs + (long long)jo * s.out_axis, v);
-      };
-      const int T = blockDim.x;
-      if (s.out_xs != 1) {  // rows adjacent in memory (STRIDE1 user layout): rows fastest
-        const FastDiv div_lo(s.Lout);
-        for (int e = threadIdx.x; e < M * s.Lout; e += T) {
-          const int m = (int)div_lo.div(e);
-          if (x0 + m < s.X) one(m, e - m * s.Lout);
-        }
-      } else if ((T & (M - 1)) == 0) {
-        const int m = threadIdx.x & (M - 1);
-        if (x0 + m < s.X)
-          for (int jo = threadIdx.x >> s.log2m; jo < s.Lout; jo += T >> s.log2m) one(m, jo);
-      } else {
-        for (int e = threadIdx.x; e < M * s.Lout; e += T) {
-          const int m = e & (M - 1);
-          if (x0 + m < s.X) one(m, e >> s.log2m);
-        }
-      }
+      strided_decode(pp, tile, xt, o1, o2);
+      strided_store<P>(pp.s, strided_smem<P>(pp.c).buf0 + b * pp.c.buf_elems, xt, o1, o2);
     }
     __syncthreads();
   }
@@ -280,132 +293,136 @@ P3G_D float4* xpipe_tw(const PipeCommon& pc) {
   return reinterpret_cast<float4*>(xpipe_buf<P>(pc, 2));
 }
 
-// r2c: real lines 2p, 2p+1 of the tile copied raw ([line][x])
+// r2c: real lines 2p, 2p+1 of the tile (first pair p0 of field `field`)
+// copied raw ([line][x]) into dst, `chunk` bytes per copy, without a commit.
 template <class P>
-P3G_D void xr2c_issue(const XPipeParams& q, int tile, int b) {
+P3G_D void xr2c_copy(const XParams& x, int chunk, typename P::W* dst_w, int p0, int field) {
   using UR = typename P::UR;
-  const XParams& x = q.x;
   const int M = x.M, N = x.nx;
-  const int field = tile / q.c.tiles_per_field;
-  const int p0 = (tile - field * q.c.tiles_per_field) * M;
   const char* in = reinterpret_cast<const char*>(static_cast<const UR*>(x.in) + field * x.in_field);
-  char* dst = reinterpret_cast<char*>(xpipe_buf<P>(q.c, b));
-  const int cpl = N * (int)sizeof(UR) / q.chunk;  // copies per line
+  char* dst = reinterpret_cast<char*>(dst_w);
+  const int cpl = N * (int)sizeof(UR) / chunk;  // copies per line
   const FastDiv fcpl((uint32_t)cpl);
   for (int e = threadIdx.x; e < 2 * M * cpl; e += blockDim.x) {
     const int lt = (int)fcpl.div((uint32_t)e);
     const int c = e - lt * cpl;
     const int line = 2 * p0 + lt;
     const bool ok = line < x.nlines;
-    const char* g = ok ? in + (long long)line * x.in_line * (long long)sizeof(UR) + (long long)c * q.chunk : in;
-    char* d = dst + ((long long)lt * N * (long long)sizeof(UR) + (long long)c * q.chunk);
-    const uint32_t nb = ok ? (uint32_t)q.chunk : 0u;
-    if (q.chunk == 16) cp_async16(d, g, nb);
-    else if (q.chunk == 8) cp_async8(d, g, nb);
+    const char* g = ok ? in + (long long)line * x.in_line * (long long)sizeof(UR) + (long long)c * chunk : in;
+    char* d = dst + ((long long)lt * N * (long long)sizeof(UR) + (long long)c * chunk);
+    const uint32_t nb = ok ? (uint32_t)chunk : 0u;
+    if (chunk == 16) cp_async16(d, g, nb);
+    else if (chunk == 8) cp_async8(d, g, nb);
     else cp_async4(d, g, nb);
   }
+}
+
+template <class P>
+P3G_D void xr2c_issue(const XPipeParams& q, int tile, int b) {
+  const int field = tile / q.c.tiles_per_field;
+  const int p0 = (tile - field * q.c.tiles_per_field) * q.x.M;
+  xr2c_copy<P>(q.x, q.chunk, xpipe_buf<P>(q.c, b), p0, field);
   cp_async_commit();
+}
+
+// Real lines 2p, 2p+1 -> complex line p (z = x1 + i x2) in the padded
+// working layout, in place: every thread reads its items, a barrier, then
+// writes them.  MAXI >= M N / blockDim.x.  Ends with a barrier.
+template <class P, int MAXI>
+P3G_D void xr2c_pack(const XParams& x, typename P::W* sm) {
+  using C = typename P::C;
+  using UR = typename P::UR;
+  const UR* raw = reinterpret_cast<const UR*>(sm);
+  const int MN = x.M * x.nx, N = x.nx;
+  const FastDiv fN((uint32_t)N);
+  C v[MAXI];
+#pragma unroll
+  for (int i = 0; i < MAXI; ++i) v[i] = P::zero();  // see stage_reg
+#pragma unroll
+  for (int i = 0; i < MAXI; ++i) {
+    const int e = threadIdx.x + i * blockDim.x;
+    if (e < MN) {
+      const int pr = (int)fN.div((uint32_t)e);
+      const int xi = e - pr * N;
+      v[i] = P::make(P::from_ur(raw[(2 * pr) * N + xi]), P::from_ur(raw[(2 * pr + 1) * N + xi]));
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < MAXI; ++i) {
+    const int e = threadIdx.x + i * blockDim.x;
+    if (e < MN) {
+      const int pr = (int)fN.div((uint32_t)e);
+      sm[pr * x.LS + pad_index(e - pr * N, x.ps)] = P::to_w(v[i]);
+    }
+  }
+  __syncthreads();
+}
+
+// X1[k] = (Z[k] + conj Z[N-k]) / 2, X2[k] = -i (Z[k] - conj Z[N-k]) / 2,
+// modes k < nkeep stored to the working layout.
+template <class P>
+P3G_D void xr2c_store(const XParams& x, const typename P::W* sm, int p0, int field) {
+  using W = typename P::W;
+  using C = typename P::C;
+  const int N = x.nx, nk = x.nkeep;
+  W* out = static_cast<W*>(x.out) + field * x.out_field;
+  const FastDiv fnk((uint32_t)nk);
+  for (int e = threadIdx.x; e < x.M * nk; e += blockDim.x) {
+    const int pr = (int)fnk.div((uint32_t)e);
+    const int k = e - pr * nk;
+    const int line = 2 * (p0 + pr);
+    if (line >= x.nlines) continue;
+    const C a = P::from_w(sm[pr * x.LS + pad_index(k, x.ps)]);
+    const C bb = cconj(P::from_w(sm[pr * x.LS + pad_index(k == 0 ? 0 : N - k, x.ps)]));
+    out[(long long)line * x.out_line + k] = P::to_w(cscale2(a + bb, 0.5f));
+    if (line + 1 < x.nlines)
+      out[(long long)(line + 1) * x.out_line + k] = P::to_w(cscale2(rot<-1>(a - bb), 0.5f));
+  }
 }
 
 template <class P>
 __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMinBlocks)
     k_xr2c_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
                 const float4* __restrict__ tw_g) {
-  using W = typename P::W;
-  using C = typename P::C;
-  using UR = typename P::UR;
   {
     float4* tw_s = xpipe_tw<P>(pp.c);
     for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) tw_s[i] = __ldg(tw_g + pp.c.tw_base + i);
   }
   __syncthreads();
-  constexpr int MAXI = PipeLimits<P>::kE;  // (pair, x) items per thread: M N / T <= E
   int it = 0;
   int tile = blockIdx.x;
   if (tile < pp.c.ntiles) xr2c_issue<P>(pp, tile, 0);
 #pragma unroll 1
   for (; tile < pp.c.ntiles; tile += gridDim.x, ++it) {
     const int b = it & 1;
-    {
-      const XPipeParams& q = pp;
-      const int next = tile + gridDim.x;
-      if (next < q.c.ntiles) xr2c_issue<P>(q, next, b ^ 1);
-      else cp_async_commit();
-      cp_async_wait<1>();
-    }
+    const int next = tile + gridDim.x;
+    if (next < pp.c.ntiles) xr2c_issue<P>(pp, next, b ^ 1);
+    else cp_async_commit();
+    cp_async_wait<1>();
     __syncthreads();
+    xr2c_pack<P, PipeLimits<P>::kE>(pp.x, xpipe_buf<P>(pp.c, b));
     {
-      // real lines 2p, 2p+1 -> complex line p (z = x1 + i x2): read all, then write
-      const XPipeParams& q = pp;
-      W* sm = xpipe_buf<P>(q.c, b);
-      const UR* raw = reinterpret_cast<const UR*>(sm);
-      const int MN = q.x.M * q.x.nx, N = q.x.nx;
-      const FastDiv fN((uint32_t)N);
-      C v[MAXI];
-#pragma unroll
-      for (int i = 0; i < MAXI; ++i) v[i] = P::zero();  // see stage_reg
-#pragma unroll
-      for (int i = 0; i < MAXI; ++i) {
-        const int e = threadIdx.x + i * blockDim.x;
-        if (e < MN) {
-          const int pr = (int)fN.div((uint32_t)e);
-          const int xi = e - pr * N;
-          v[i] = P::make(P::from_ur(raw[(2 * pr) * N + xi]), P::from_ur(raw[(2 * pr + 1) * N + xi]));
-        }
-      }
-      __syncthreads();
-#pragma unroll
-      for (int i = 0; i < MAXI; ++i) {
-        const int e = threadIdx.x + i * blockDim.x;
-        if (e < MN) {
-          const int pr = (int)fN.div((uint32_t)e);
-          sm[pr * q.x.LS + pad_index(e - pr * N, q.x.ps)] = P::to_w(v[i]);
-        }
-      }
-    }
-    __syncthreads();
-    {
-      const XPipeParams& q = pp;
-      Tile<P> t{xpipe_buf<P>(q.c, b), nullptr, q.x.M, q.x.log2m, q.x.LS, 1, q.x.ps};
-      cta_fft<P, -1, PipeLimits<P>::kE>(t, sp, xpipe_tw<P>(q.c), q.c.tw_base);
+      Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
+      cta_fft<P, -1, PipeLimits<P>::kE>(t, sp, xpipe_tw<P>(pp.c), pp.c.tw_base);
     }
     {
-      // X1[k] = (Z[k] + conj Z[N-k]) / 2, X2[k] = -i (Z[k] - conj Z[N-k]) / 2
-      const XPipeParams& q = pp;
-      const XParams& x = q.x;
-      const W* sm = xpipe_buf<P>(q.c, b);
-      const int M = x.M, N = x.nx, nk = x.nkeep;
-      const int field = tile / q.c.tiles_per_field;
-      const int p0 = (tile - field * q.c.tiles_per_field) * M;
-      W* out = static_cast<W*>(x.out) + field * x.out_field;
-      const FastDiv fnk((uint32_t)nk);
-      for (int e = threadIdx.x; e < M * nk; e += blockDim.x) {
-        const int pr = (int)fnk.div((uint32_t)e);
-        const int k = e - pr * nk;
-        const int line = 2 * (p0 + pr);
-        if (line >= x.nlines) continue;
-        const C a = P::from_w(sm[pr * x.LS + pad_index(k, x.ps)]);
-        const C bb = cconj(P::from_w(sm[pr * x.LS + pad_index(k == 0 ? 0 : N - k, x.ps)]));
-        out[(long long)line * x.out_line + k] = P::to_w(cscale2(a + bb, 0.5f));
-        if (line + 1 < x.nlines)
-          out[(long long)(line + 1) * x.out_line + k] = P::to_w(cscale2(rot<-1>(a - bb), 0.5f));
-      }
+      const int field = tile / pp.c.tiles_per_field;
+      const int p0 = (tile - field * pp.c.tiles_per_field) * pp.x.M;
+      xr2c_store<P>(pp.x, xpipe_buf<P>(pp.c, b), p0, field);
     }
     __syncthreads();
   }
   cp_async_wait<0>();
 }
 
-// c2r: complex lines 2p, 2p+1 of nh = N/2+1 modes copied raw (pair stride 2 nh)
+// c2r: complex lines 2p, 2p+1 of nh = N/2+1 modes copied raw (pair stride
+// 2 nh) into dst, modes beyond nkeep as zeros, without a commit.
 template <class P>
-P3G_D void xc2r_issue(const XPipeParams& q, int tile, int b) {
+P3G_D void xc2r_copy(const XParams& x, typename P::W* dst, int p0, int field) {
   using W = typename P::W;
-  const XParams& x = q.x;
   const int M = x.M, nh = x.nx / 2 + 1;
-  const int field = tile / q.c.tiles_per_field;
-  const int p0 = (tile - field * q.c.tiles_per_field) * M;
   const W* in = static_cast<const W*>(x.in) + field * x.in_field;
-  W* dst = xpipe_buf<P>(q.c, b);
   const FastDiv fnh((uint32_t)nh);
   for (int e = threadIdx.x; e < 2 * M * nh; e += blockDim.x) {
     const int lt = (int)fnh.div((uint32_t)e);
@@ -416,106 +433,114 @@ P3G_D void xc2r_issue(const XPipeParams& q, int tile, int b) {
     if constexpr (sizeof(W) == 16) cp_async16(dst + lt * nh + k, g, ok ? 16u : 0u);
     else cp_async8(dst + lt * nh + k, g, ok ? 8u : 0u);
   }
+}
+
+template <class P>
+P3G_D void xc2r_issue(const XPipeParams& q, int tile, int b) {
+  const int field = tile / q.c.tiles_per_field;
+  const int p0 = (tile - field * q.c.tiles_per_field) * q.x.M;
+  xc2r_copy<P>(q.x, xpipe_buf<P>(q.c, b), p0, field);
   cp_async_commit();
+}
+
+// Hermitian extension of the raw pair lines into Z = X1 + i X2 (padded
+// working layout), in place: read all, barrier, write.  MAXI >= M nh /
+// blockDim.x.  Ends with a barrier.
+template <class P, int MAXI>
+P3G_D void xc2r_merge(const XParams& x, typename P::W* sm) {
+  using C = typename P::C;
+  const int N = x.nx, nh = N / 2 + 1, NP = 2 * nh, Mnh = x.M * nh;
+  const FastDiv fnh((uint32_t)nh);
+  C z0[MAXI], z1[MAXI];
+  int ip[MAXI], ik[MAXI];
+#pragma unroll
+  for (int i = 0; i < MAXI; ++i) {  // see stage_reg
+    z0[i] = P::zero();
+    z1[i] = P::zero();
+    ik[i] = 0;
+  }
+#pragma unroll
+  for (int i = 0; i < MAXI; ++i) {
+    const int e = threadIdx.x + i * blockDim.x;
+    ip[i] = -1;
+    if (e < Mnh) {
+      const int pr = (int)fnh.div((uint32_t)e);
+      const int k = e - pr * nh;
+      C x1 = P::from_w(sm[pr * NP + k]);
+      C x2 = P::from_w(sm[pr * NP + nh + k]);
+      if (k == 0 || 2 * k == N) {
+        x1 = P::make(P::re(x1), P::re(P::zero()));
+        x2 = P::make(P::re(x2), P::re(P::zero()));
+      }
+      z0[i] = x1 + rot<1>(x2);
+      z1[i] = cconj(x1) + rot<1>(cconj(x2));
+      ip[i] = pr;
+      ik[i] = k;
+    }
+  }
+  __syncthreads();
+  const int LS = x.LS, ps = x.ps;  // Z layout (padded), raw lines used NP = 2 nh
+#pragma unroll
+  for (int i = 0; i < MAXI; ++i) {
+    if (ip[i] >= 0) {
+      sm[ip[i] * LS + pad_index(ik[i], ps)] = P::to_w(z0[i]);
+      if (ik[i] > 0 && 2 * ik[i] < N) sm[ip[i] * LS + pad_index(N - ik[i], ps)] = P::to_w(z1[i]);
+    }
+  }
+  __syncthreads();
+}
+
+// x1 = Re z, x2 = Im z to the user's real lines (format conversion fused).
+template <class P>
+P3G_D void xc2r_store(const XParams& x, const typename P::W* sm, int p0, int field) {
+  using W = typename P::W;
+  using UR = typename P::UR;
+  const int M = x.M, N = x.nx, LS = x.LS, ps = x.ps;
+  UR* out = static_cast<UR*>(x.out) + field * x.out_field;
+  const float* smf = reinterpret_cast<const float*>(sm);
+  constexpr int kW = sizeof(W) / sizeof(float);
+  const FastDiv fN((uint32_t)N);
+  for (int e = threadIdx.x; e < 2 * M * N; e += blockDim.x) {
+    const int lt = (int)fN.div((uint32_t)e);
+    const int n = e - lt * N;
+    const int line = 2 * p0 + lt;
+    if (line >= x.nlines) continue;
+    const int c = lt & 1;
+    const float* f = smf + ((lt >> 1) * LS + pad_index(n, ps)) * kW;
+    if constexpr (P::kF64) out[(long long)line * x.out_line + n] = P::to_ur(df{f[c], f[2 + c]});
+    else out[(long long)line * x.out_line + n] = f[c];
+  }
 }
 
 template <class P>
 __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMinBlocks)
     k_xc2r_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
                 const float4* __restrict__ tw_g) {
-  using W = typename P::W;
-  using C = typename P::C;
-  using UR = typename P::UR;
   {
     float4* tw_s = xpipe_tw<P>(pp.c);
     for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) tw_s[i] = __ldg(tw_g + pp.c.tw_base + i);
   }
   __syncthreads();
-  constexpr int MAXI = PipeLimits<P>::kE / 2 + 2;  // host guarantees T * MAXI >= M nh
   int it = 0;
   int tile = blockIdx.x;
   if (tile < pp.c.ntiles) xc2r_issue<P>(pp, tile, 0);
 #pragma unroll 1
   for (; tile < pp.c.ntiles; tile += gridDim.x, ++it) {
     const int b = it & 1;
-    {
-      const XPipeParams& q = pp;
-      const int next = tile + gridDim.x;
-      if (next < q.c.ntiles) xc2r_issue<P>(q, next, b ^ 1);
-      else cp_async_commit();
-      cp_async_wait<1>();
-    }
+    const int next = tile + gridDim.x;
+    if (next < pp.c.ntiles) xc2r_issue<P>(pp, next, b ^ 1);
+    else cp_async_commit();
+    cp_async_wait<1>();
     __syncthreads();
+    xc2r_merge<P, PipeLimits<P>::kE / 2 + 2>(pp.x, xpipe_buf<P>(pp.c, b));  // host: T * MAXI >= M nh
     {
-      // Hermitian extension into Z (in place, pair stride NP = 2 nh): read all, then write
-      const XPipeParams& q = pp;
-      W* sm = xpipe_buf<P>(q.c, b);
-      const int N = q.x.nx, nh = N / 2 + 1, NP = 2 * nh, Mnh = q.x.M * nh;
-      const FastDiv fnh((uint32_t)nh);
-      C z0[MAXI], z1[MAXI];
-      int ip[MAXI], ik[MAXI];
-#pragma unroll
-      for (int i = 0; i < MAXI; ++i) {  // see stage_reg
-        z0[i] = P::zero();
-        z1[i] = P::zero();
-        ik[i] = 0;
-      }
-#pragma unroll
-      for (int i = 0; i < MAXI; ++i) {
-        const int e = threadIdx.x + i * blockDim.x;
-        ip[i] = -1;
-        if (e < Mnh) {
-          const int pr = (int)fnh.div((uint32_t)e);
-          const int k = e - pr * nh;
-          C x1 = P::from_w(sm[pr * NP + k]);
-          C x2 = P::from_w(sm[pr * NP + nh + k]);
-          if (k == 0 || 2 * k == N) {
-            x1 = P::make(P::re(x1), P::re(P::zero()));
-            x2 = P::make(P::re(x2), P::re(P::zero()));
-          }
-          z0[i] = x1 + rot<1>(x2);
-          z1[i] = cconj(x1) + rot<1>(cconj(x2));
-          ip[i] = pr;
-          ik[i] = k;
-        }
-      }
-      __syncthreads();
-      const int LS = q.x.LS, ps = q.x.ps;  // Z layout (padded), raw lines used NP = 2 nh
-#pragma unroll
-      for (int i = 0; i < MAXI; ++i) {
-        if (ip[i] >= 0) {
-          sm[ip[i] * LS + pad_index(ik[i], ps)] = P::to_w(z0[i]);
-          if (ik[i] > 0 && 2 * ik[i] < N) sm[ip[i] * LS + pad_index(N - ik[i], ps)] = P::to_w(z1[i]);
-        }
-      }
-    }
-    __syncthreads();
-    {
-      const XPipeParams& q = pp;
-      Tile<P> t{xpipe_buf<P>(q.c, b), nullptr, q.x.M, q.x.log2m, q.x.LS, 1, q.x.ps};
-      cta_fft<P, 1, PipeLimits<P>::kE>(t, sp, xpipe_tw<P>(q.c), q.c.tw_base);
+      Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
+      cta_fft<P, 1, PipeLimits<P>::kE>(t, sp, xpipe_tw<P>(pp.c), pp.c.tw_base);
     }
     {
-      const XPipeParams& q = pp;
-      const XParams& x = q.x;
-      const W* sm = xpipe_buf<P>(q.c, b);
-      const int M = x.M, N = x.nx, LS = x.LS, ps = x.ps;
-      const int field = tile / q.c.tiles_per_field;
-      const int p0 = (tile - field * q.c.tiles_per_field) * M;
-      UR* out = static_cast<UR*>(x.out) + field * x.out_field;
-      const float* smf = reinterpret_cast<const float*>(sm);
-      constexpr int kW = sizeof(W) / sizeof(float);
-      const FastDiv fN((uint32_t)N);
-      for (int e = threadIdx.x; e < 2 * M * N; e += blockDim.x) {
-        const int lt = (int)fN.div((uint32_t)e);
-        const int n = e - lt * N;
-        const int line = 2 * p0 + lt;
-        if (line >= x.nlines) continue;
-        const int c = lt & 1;
-        const float* f = smf + ((lt >> 1) * LS + pad_index(n, ps)) * kW;
-        if constexpr (P::kF64) out[(long long)line * x.out_line + n] = P::to_ur(df{f[c], f[2 + c]});
-        else out[(long long)line * x.out_line + n] = f[c];
-      }
+      const int field = tile / pp.c.tiles_per_field;
+      const int p0 = (tile - field * pp.c.tiles_per_field) * pp.x.M;
+      xc2r_store<P>(pp.x, xpipe_buf<P>(pp.c, b), p0, field);
     }
     __syncthreads();
   }
