@@ -169,13 +169,33 @@ def time_device(torch, plan, x, b, r, ops, steps, warmup, stream):
     return ms, plan.launches - launches0
 
 
+# ------------------------------------------------------------ replicas
+def replica_env():
+    """(world, rank, local rank) from the torchrun environment."""
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def max_over_ranks(torch, dist, value: float, device) -> float:
+    """The slowest rank's time: every rank runs a full replica, so the job's
+    time is the maximum over ranks (no data-path collective)."""
+    if dist is None:
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_gpts(world: int, points_per_replica: int, ms: float) -> float:
+    """Whole-job throughput: the points of all replicas over the max time."""
+    return world * points_per_replica / (ms * 1e-3) / 1e9
+
+
 def run_ours(args):
     import torch
     import p3dfft_gb300 as pg
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world, rank, local = replica_env()
     dist = None
     if world > 1:
         import torch.distributed as dist_mod
@@ -206,10 +226,7 @@ def run_ours(args):
         dist.barrier()
     with ClockSampler(local) as clk:
         ms64, launches = time_device(torch, plan, x, b, r, ops, args.steps, args.warmup, stream)
-    if dist:
-        t = torch.tensor([ms64], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms64 = float(t.item())
+    ms64 = max_over_ranks(torch, dist, ms64, dev)
     timers = plan.timers()
     # per-pass kernel times over the timed steps (plan timers: slots 5,7,8,9,10,12)
     bm = bytes_model(grid, 8)
@@ -256,10 +273,7 @@ def run_ours(args):
     err32 = float(torch.linalg.vector_norm(diff) / torch.linalg.vector_norm(fwd64))
     del b32, r32, x32, diff, fwd64
     plan32.close()
-    if dist:
-        t = torch.tensor([ms32], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms32 = float(t.item())
+    ms32 = max_over_ranks(torch, dist, ms32, dev)
 
     # ---- end to end through the drop-in C-ABI with pinned host buffers
     e2e = None
@@ -272,7 +286,7 @@ def run_ours(args):
         batched = run_batched(torch, pg, dev, args.steps, args.warmup, npts / (ms64 * 1e-3) / 1e9)
         serving = run_serving(torch, pg, args.serve_requests, npts / (ms64 * 1e-3) / 1e9)
 
-    value = world * npts / (ms64 * 1e-3) / 1e9
+    value = aggregate_gpts(world, npts, ms64)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms64, 4), "higher_is_better": True, "scaling": "weak",
@@ -283,7 +297,7 @@ def run_ours(args):
                    "parallelism": f"replicas x{world}"},
         "error": {"f64_roundtrip_normalised_linf": rt_err,
                   "f32_forward_rel_l2_vs_f64": err32},
-        "f32": {"value": round(world * npts / (ms32 * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_step": round(ms32, 4),
+        "f32": {"value": round(aggregate_gpts(world, npts, ms32), 3), "unit": UNIT, "ms_per_step": round(ms32, 4),
                 "rel_l2_vs_f64": err32, "speedup_vs_f64": round(ms64 / ms32, 3)},
         "passes_ms": {k: round(v, 4) for k, v in pass_ms.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "launches_per_step": nl,
