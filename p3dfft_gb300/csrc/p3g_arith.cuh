@@ -15,6 +15,7 @@
 // __host__ __device__ so the CPU tests can check them bit for bit.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -162,10 +163,24 @@ P3G_HD df d2df(double x) {
   return r;
 }
 
-// df2d: hi + lo rounded to binary64 (error <= 1 ulp of the result).  The pair
-// is first made canonical with TwoSum (s + t == hi + lo, |t| <= ulp32(s)/2), s
-// is widened exactly, and t is added as an integer number of binary64 ulps of
-// s directly on the bit pattern.  Subnormal binary32 parts are flushed.
+// Nearest integer of a binary32 value below 2^30.
+P3G_HD int32_t f32_to_i32_rn(float v) {
+#if defined(__CUDA_ARCH__)
+  return __float2int_rn(v);
+#else
+  return (int32_t)std::nearbyint(v);
+#endif
+}
+
+// df2d: hi + lo rounded to binary64 (error <= 1/2 ulp of the result for
+// |hi + lo| >= 2^-75, below that the lo part is dropped).  The pair is made
+// canonical with TwoSum (s + t == hi + lo, |t| <= ulp32(s)/2), s is widened
+// exactly, and t, scaled to binary64 ulps of s (|k| <= 2^29) and rounded to an
+// integer with one F2I, is added to the bit pattern.  A step that lowers |s|
+// from an exact power of two counts in the half-size ulps of the binade below.
+// No step crosses a binade otherwise: the widened s has at least 2^29 ulps of
+// mantissa above its binade and at least 2^29 below the next.  Subnormal
+// binary32 parts are flushed.
 P3G_HD double df2d(float hi, float lo) {
   float s, t;
   two_sum(hi, lo, s, t);
@@ -175,27 +190,15 @@ P3G_HD double df2d(float hi, float lo) {
   const uint32_t ms = sb & 0x7FFFFFu;
   if (es == 0) return u2d((uint64_t)sign << 32);
   if (es == 255) return u2d(((uint64_t)(sign | 0x7FF00000u | (ms ? 0x80000u : 0u))) << 32);
-  uint64_t d = ((uint64_t)(sign | ((uint32_t)(es + 896) << 20) | (ms >> 3)) << 32) |
-               ((uint64_t)(ms & 7u) << 29);
+  const uint64_t d = ((uint64_t)(sign | ((uint32_t)(es + 896) << 20) | (ms >> 3)) << 32) |
+                     ((uint64_t)(ms & 7u) << 29);
   const uint32_t tb = f2u(t);
-  const int et = (int)((tb >> 23) & 0xFFu);
-  if (et != 0 && et != 255) {
-    const uint32_t mt = (tb & 0x7FFFFFu) | 0x800000u;  // 24-bit significand of t
-    const bool shrink = ((tb ^ sb) & 0x80000000u) != 0u;  // t lowers |s|
-    // t = mt * 2^(et-150); one binary64 ulp of s is 2^(es-179) (2^(es-180)
-    // just below a power of two when |s| shrinks).
-    int sh = et - es + 29 + ((shrink && ms == 0u) ? 1 : 0);
-    uint64_t k;
-    if (sh >= 0) {
-      k = (uint64_t)mt << sh;  // sh <= 6 because |t| <= ulp32(s)/2
-    } else if (sh > -25) {
-      k = ((uint64_t)mt + (1ull << (-sh - 1))) >> (-sh);
-    } else {
-      k = 0;
-    }
-    d = shrink ? d - k : d + k;
-  }
-  return u2d(d);
+  const bool down = ((tb ^ sb) & 0x80000000u) != 0u;  // t lowers |s|
+  // one binary64 ulp of s is 2^(es-179); 2^(179-es) has biased exponent 306-es
+  const int scale_e = 306 - es + ((down && ms == 0u) ? 1 : 0);
+  if ((tb & 0x7FFFFFFFu) == 0u || scale_e > 254) return u2d(d);
+  const int64_t k = f32_to_i32_rn(u2f(tb & 0x7FFFFFFFu) * u2f((uint32_t)scale_e << 23));
+  return u2d(down ? d - (uint64_t)k : d + (uint64_t)k);
 }
 
 // ------------------------------------------------------- double-float ops
