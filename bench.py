@@ -490,8 +490,8 @@ def run_e2e(torch, pg, grid, ops, x_dev, steps, dev):
     return {"value": round(nx * ny * nz / dt / 1e9, 3), "unit": UNIT, "ms_per_step": round(dt * 1e3, 3),
             "h2d_bytes_per_step": r_bytes + c_bytes, "d2h_bytes_per_step": c_bytes + r_bytes,
             "path": "libp3dfft.so p3dfft_ftran_r2c + p3dfft_btran_c2r, pinned host arrays: the real arrays "
-                    "read/written in place by the X passes over the host link, the complex arrays staged by "
-                    "cudaMemcpyAsync",
+                    "read/written in place by the X passes over the host link, the complex arrays copied in "
+                    "row blocks overlapped with the Z pass",
             "host_link_gbs": link}
 
 

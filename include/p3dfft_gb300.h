@@ -75,6 +75,19 @@ int p3g_ftran_r2c(p3g_plan plan, const void* in, void* out, const char* op, int 
 int p3g_btran_c2r(p3g_plan plan, const void* in, void* out, const char* op, int nv, long long dim_in,
                   long long dim_out, void* stream);
 
+/* Single-field transforms between a device (or GPU-addressable host) real
+ * array and a HOST complex array, with the host copies overlapped with the Z
+ * pass (no counterpart in the reference, whose arrays are host memory
+ * throughout): ftran runs X and Y, then the Z pass in `chunks` row blocks,
+ * copying each block's output to out_host on copy_stream while the next block
+ * computes; btran copies the input in row blocks and starts each block's Z pass
+ * when its copy has landed.  stage is a device buffer of the complex array's
+ * size.  XYZ layout.  The caller synchronises both streams. */
+int p3g_ftran_r2c_to_host(p3g_plan plan, const void* in, void* out_host, void* stage, const char* op, int chunks,
+                          void* stream, void* copy_stream);
+int p3g_btran_c2r_from_host(p3g_plan plan, const void* in_host, void* stage, void* out, const char* op, int chunks,
+                            void* stream, void* copy_stream);
+
 /* p3dfft_cheby (reference build/ftran.F90:321-464): 'ffc' transform, scaling
  * by 1/(nx*ny*(nzc-1)) and the Chebyshev-derivative recurrence along z with
  * factor 4/lz. */

@@ -147,6 +147,29 @@ class Plan:
         _check(_core().p3g_cheby(self._h, _ptr(x), _ptr(out), float(lz), nv, dim_in, dim_out, _stream_ptr(stream)))
         return out
 
+    def ftran_r2c_to_host(self, x, out_host, op="fft", chunks=8, stream=None, copy_stream=None):
+        """Forward transform into a host (pinned) complex tensor, the host
+        copies overlapped with the Z pass in row blocks (p3g_ftran_r2c_to_host)."""
+        import torch
+        stage = torch.empty(self.complex_shape, dtype=self._dtypes()[1], device=x.device)
+        cs = copy_stream or torch.cuda.Stream(device=x.device)
+        st = _stream_ptr(stream)
+        _check(_core().p3g_ftran_r2c_to_host(self._h, _ptr(x), _ptr(out_host), _ptr(stage), op.encode(), chunks, st,
+                                             _stream_ptr(cs)))
+        torch.cuda.synchronize(x.device)
+        return out_host
+
+    def btran_c2r_from_host(self, c_host, out, op="tff", chunks=8, stream=None, copy_stream=None):
+        """Backward transform of a host (pinned) complex tensor, the host copies
+        overlapped with the Z pass in row blocks (p3g_btran_c2r_from_host)."""
+        import torch
+        stage = torch.empty(self.complex_shape, dtype=self._dtypes()[1], device=out.device)
+        cs = copy_stream or torch.cuda.Stream(device=out.device)
+        _check(_core().p3g_btran_c2r_from_host(self._h, _ptr(c_host), _ptr(stage), _ptr(out), op.encode(), chunks,
+                                               _stream_ptr(stream), _stream_ptr(cs)))
+        torch.cuda.synchronize(out.device)
+        return out
+
     def spectrum(self, b, kmax=0, scale=1.0, flags=None, nv=1, dim_in=0, out=None, stream=None):
         """Shell spectrum of the forward output b (see p3g_spectrum); returns a
         float64 CUDA tensor of kmax + 1 bins (nv rows when nv > 1).  flags

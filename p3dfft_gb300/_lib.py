@@ -40,6 +40,10 @@ CORE_SIGNATURES = {
                                              ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "p3g_job_work_bytes": (ctypes.c_longlong, [ctypes.c_void_p, ctypes.c_int]),
+    "p3g_ftran_r2c_to_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    "p3g_btran_c2r_from_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     "p3g_batch_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
     "p3g_batch_set_jobs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Job), ctypes.c_int]),
     "p3g_batch_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),

@@ -43,6 +43,8 @@ int g_layout = P3G_LAYOUT_XYZ;
 #endif
 std::string g_msg;
 cudaStream_t g_stream = nullptr;
+cudaStream_t g_copy = nullptr;  // host copies overlapped with the Z pass
+constexpr int kRowBlocks = 8;
 void* g_stage[2] = {nullptr, nullptr};
 size_t g_stage_bytes[2] = {0, 0};
 int g_nx, g_ny, g_nz, g_nxhpc, g_nyc, g_nzc;
@@ -191,6 +193,7 @@ void p3dfft_setup(int* dims, int* nx, int* ny, int* nz, int* comm, int* nxc, int
   const int cx = nxc ? *nxc : *nx, cy = nyc ? *nyc : *ny, cz = nzc ? *nzc : *nz;
   if (!check(p3g_plan_create(&g_plan, *nx, *ny, *nz, cx, cy, cz, kPrec, g_layout, P3G_FLAG_TIMERS))) return;
   if (!g_stream) cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+  if (!g_copy) cudaStreamCreateWithFlags(&g_copy, cudaStreamNonBlocking);
   std::memset(g_timers, 0, sizeof(g_timers));
   g_comm = comm ? *comm : 0;
   g_nx = *nx;
@@ -219,9 +222,24 @@ void p3dfft_get_mpi_info(int* taskid, int* ntasks, int* comm) {
   g_status = 0;
 }
 
+// Waits for both streams of an overlapped call and records the outcome.
+void finish_overlapped(int rc) {
+  const cudaError_t a = cudaStreamSynchronize(g_stream), b = cudaStreamSynchronize(g_copy);
+  if (!check(rc)) return;
+  if (a != cudaSuccess || b != cudaSuccess) return error(P3G_E_CUDA, "P3DFFT error: transform failed");
+  g_status = 0;
+}
+
 void p3dfft_ftran_r2c(real_t* A, real_t* B, unsigned char* op) {
   if (!ready()) return;
   const char* o = reinterpret_cast<const char*>(op);
+  // host output (staged) with a GPU-readable input: copy the Z pass's output
+  // to the host in row blocks while later blocks compute
+  if (g_layout == P3G_LAYOUT_XYZ && !on_device(B) && (on_device(A) || host_direct(A))) {
+    void* st = stage(1, csize() * 2 * sizeof(real_t));
+    if (!st) return error(P3G_E_NOMEM, "P3DFFT error: staging allocation failed");
+    return finish_overlapped(p3g_ftran_r2c_to_host(g_plan, A, B, st, o, kRowBlocks, g_stream, g_copy));
+  }
   run(A, rsize() * sizeof(real_t), true, B, csize() * 2 * sizeof(real_t), false,
       [&](const void* i, void* out) { return p3g_ftran_r2c(g_plan, i, out, o, 1, 0, 0, g_stream); });
 }
@@ -229,6 +247,13 @@ void p3dfft_ftran_r2c(real_t* A, real_t* B, unsigned char* op) {
 void p3dfft_btran_c2r(real_t* A, real_t* B, unsigned char* op) {
   if (!ready()) return;
   const char* o = reinterpret_cast<const char*>(op);
+  // host input (staged) with a GPU-writable output: row-block copies feed the
+  // Z pass as they land
+  if (g_layout == P3G_LAYOUT_XYZ && !on_device(A) && (on_device(B) || host_direct(B))) {
+    void* st = stage(0, csize() * 2 * sizeof(real_t));
+    if (!st) return error(P3G_E_NOMEM, "P3DFFT error: staging allocation failed");
+    return finish_overlapped(p3g_btran_c2r_from_host(g_plan, A, st, B, o, kRowBlocks, g_stream, g_copy));
+  }
   run(A, csize() * 2 * sizeof(real_t), false, B, rsize() * sizeof(real_t), true,
       [&](const void* i, void* out) { return p3g_btran_c2r(g_plan, i, out, o, 1, 0, 0, g_stream); });
 }

@@ -749,6 +749,142 @@ int do_btran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   return P3G_OK;
 }
 
+// Row blocks of the Z pass: block c covers y in [c*nyc/K, (c+1)*nyc/K).
+struct RowBlock {
+  int y0, y1;
+};
+std::vector<RowBlock> row_blocks(int nyc, int chunks) {
+  std::vector<RowBlock> r;
+  if (chunks < 1) chunks = 1;
+  if (chunks > nyc) chunks = nyc;
+  for (int c = 0; c < chunks; ++c) r.push_back({(int)((long long)c * nyc / chunks), (int)((long long)(c + 1) * nyc / chunks)});
+  return r;
+}
+
+// The Z pass of rows [y0, y1): the same parameters with shifted bases.
+SParams z_rows(const SParams& z, int y0, int y1, size_t esize) {
+  SParams c = z;
+  c.O1 = y1 - y0;
+  c.in = static_cast<const unsigned char*>(z.in) + (size_t)y0 * z.in_o1 * esize;
+  c.out = static_cast<unsigned char*>(z.out) + (size_t)y0 * z.out_o1 * esize;
+  return c;
+}
+
+struct EventSet {
+  std::vector<cudaEvent_t> ev;
+  explicit EventSet(size_t n) : ev(n, nullptr) {
+    for (auto& e : ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  }
+  ~EventSet() {
+    for (auto e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+};
+
+// Forward transform into a host array: X and Y passes, then the Z pass in row
+// blocks, each block's output copied to the host on cs while the next block
+// computes.
+template <class P>
+int do_ftran_to_host(p3g_plan p, const void* in, void* out_host, void* stage, const char* op, int chunks,
+                     cudaStream_t st, cudaStream_t cs) {
+  bool fsign = true;
+  const int zi = op_index(op[2], fsign, true);
+  if (zi < 0) return fail(P3G_E_ARG, std::string("Unknown transform type: ") + op[2]);
+  if (!p->z_ok[zi]) return fail(P3G_E_UNSUPPORTED, std::string("Z transform '") + op[2] + "' unsupported for nz");
+  int rc = ensure_workspace(p, 1);
+  if (rc) return rc;
+  const long long rsize = (long long)p->nx * p->ny * p->nz;
+  const long long csize = (long long)p->nxhpc * p->nyc * p->nzc;
+  XParams x;
+  SParams y, z;
+  make_forward_params(p, in, stage, p->wa, p->wb, zi, rsize, csize, x, y, z);
+  {
+    PassTimer tm(p, 4, st);
+    if ((rc = run_x_r2c<P>(p, x, 1, st))) return rc;
+    tm.done();
+  }
+  {
+    PassTimer tm(p, 6, st);
+    if ((rc = run_strided<P>(p, y, p->ax_y, true, 1, st))) return rc;
+    tm.done();
+  }
+  const size_t es = p->esize();
+  const auto blocks = row_blocks(p->nyc, chunks);
+  EventSet evs(blocks.size());
+  const size_t pitch = (size_t)p->nyc * p->nxhpc * es;
+  for (size_t c = 0; c < blocks.size(); ++c) {
+    const int y0 = blocks[c].y0, y1 = blocks[c].y1;
+    SParams zc = z_rows(z, y0, y1, es);
+    {
+      PassTimer tm(p, 7, st);
+      if ((rc = run_strided<P>(p, zc, p->ax_z[zi], fsign, 1, st))) return rc;
+      tm.done();
+    }
+    cudaError_t e = cudaEventRecord(evs.ev[c], st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, evs.ev[c], 0);
+    const size_t off = (size_t)y0 * p->nxhpc * es;
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(static_cast<unsigned char*>(out_host) + off, pitch,
+                            static_cast<const unsigned char*>(stage) + off, pitch, (size_t)(y1 - y0) * p->nxhpc * es,
+                            p->nzc, cudaMemcpyDeviceToHost, cs);
+    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("device to host copy: ") + cudaGetErrorString(e));
+  }
+  return P3G_OK;
+}
+
+// Backward transform from a host array: the input is copied in row blocks on
+// cs and the Z pass of each block starts as soon as its copy has landed; then
+// the Y and X passes.
+template <class P>
+int do_btran_from_host(p3g_plan p, const void* in_host, void* stage, void* out, const char* op, int chunks,
+                       cudaStream_t st, cudaStream_t cs) {
+  bool fsign = false;
+  const int zi = op_index(op[0], fsign, false);
+  if (zi < 0) return fail(P3G_E_ARG, std::string("Unknown transform type: ") + op[0]);
+  if (!p->z_ok[zi]) return fail(P3G_E_UNSUPPORTED, std::string("Z transform '") + op[0] + "' unsupported for nz");
+  int rc = ensure_workspace(p, 1);
+  if (rc) return rc;
+  const long long rsize = (long long)p->nx * p->ny * p->nz;
+  const long long csize = (long long)p->nxhpc * p->nyc * p->nzc;
+  SParams z, y;
+  XParams x;
+  make_backward_params(p, stage, out, p->wa, p->wb, zi, csize, rsize, z, y, x);
+  const size_t es = p->esize();
+  const auto blocks = row_blocks(p->nyc, chunks);
+  EventSet evs(blocks.size());
+  const size_t pitch = (size_t)p->nyc * p->nxhpc * es;
+  // the copies must not overwrite the stage while earlier work on st reads it
+  EventSet start(1);
+  cudaError_t e = cudaEventRecord(start.ev[0], st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, start.ev[0], 0);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("stream order: ") + cudaGetErrorString(e));
+  for (size_t c = 0; c < blocks.size(); ++c) {
+    const int y0 = blocks[c].y0, y1 = blocks[c].y1;
+    const size_t off = (size_t)y0 * p->nxhpc * es;
+    e = cudaMemcpy2DAsync(static_cast<unsigned char*>(stage) + off, pitch,
+                          static_cast<const unsigned char*>(in_host) + off, pitch, (size_t)(y1 - y0) * p->nxhpc * es,
+                          p->nzc, cudaMemcpyHostToDevice, cs);
+    if (e == cudaSuccess) e = cudaEventRecord(evs.ev[c], cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, evs.ev[c], 0);
+    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("host to device copy: ") + cudaGetErrorString(e));
+    SParams zc = z_rows(z, y0, y1, es);
+    PassTimer tm(p, 8, st);
+    if ((rc = run_strided<P>(p, zc, p->ax_z[zi], fsign, 1, st))) return rc;
+    tm.done();
+  }
+  {
+    PassTimer tm(p, 9, st);
+    if ((rc = run_strided<P>(p, y, p->ax_y, false, 1, st))) return rc;
+    tm.done();
+  }
+  {
+    PassTimer tm(p, 11, st);
+    if ((rc = run_x_c2r<P>(p, x, 1, st))) return rc;
+    tm.done();
+  }
+  return P3G_OK;
+}
+
 bool valid_op(const char* op) { return op && op[0] && op[1] && op[2]; }
 
 void split_df(long double v, float& hi, float& lo) {
@@ -973,6 +1109,30 @@ int p3g_get_dims(p3g_plan p, int conf, int start[3], int end[3], int size[3]) {
     return fail(P3G_E_ARG, "conf must be 1, 2 or 3");
   }
   return P3G_OK;
+}
+
+int p3g_ftran_r2c_to_host(p3g_plan p, const void* in, void* out_host, void* stage, const char* op, int chunks,
+                          void* stream, void* copy_stream) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  if (!valid_op(op)) return fail(P3G_E_ARG, "op must have 3 letters");
+  if (!in || !out_host || !stage) return fail(P3G_E_ARG, "NULL array");
+  if (p->layout != P3G_LAYOUT_XYZ) return fail(P3G_E_UNSUPPORTED, "row-block copies need the XYZ layout");
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = static_cast<cudaStream_t>(stream), cs = static_cast<cudaStream_t>(copy_stream);
+  return p->prec == P3G_F64 ? do_ftran_to_host<PathF64>(p, in, out_host, stage, op, chunks, st, cs)
+                            : do_ftran_to_host<PathF32>(p, in, out_host, stage, op, chunks, st, cs);
+}
+
+int p3g_btran_c2r_from_host(p3g_plan p, const void* in_host, void* stage, void* out, const char* op, int chunks,
+                            void* stream, void* copy_stream) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  if (!valid_op(op)) return fail(P3G_E_ARG, "op must have 3 letters");
+  if (!in_host || !out || !stage) return fail(P3G_E_ARG, "NULL array");
+  if (p->layout != P3G_LAYOUT_XYZ) return fail(P3G_E_UNSUPPORTED, "row-block copies need the XYZ layout");
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = static_cast<cudaStream_t>(stream), cs = static_cast<cudaStream_t>(copy_stream);
+  return p->prec == P3G_F64 ? do_btran_from_host<PathF64>(p, in_host, stage, out, op, chunks, st, cs)
+                            : do_btran_from_host<PathF32>(p, in_host, stage, out, op, chunks, st, cs);
 }
 
 int p3g_ftran_r2c(p3g_plan p, const void* in, void* out, const char* op, int nv, long long dim_in, long long dim_out,
