@@ -491,12 +491,38 @@ P3G_D void xc2r_merge(const XParams& x, typename P::W* sm) {
 }
 
 // x1 = Re z, x2 = Im z to the user's real lines (format conversion fused).
+// Even N: each thread takes positions n, n+1 of a line pair, reads the two
+// complex values once and writes two-element vectors to both lines.
 template <class P>
 P3G_D void xc2r_store(const XParams& x, const typename P::W* sm, int p0, int field) {
   using W = typename P::W;
   using UR = typename P::UR;
   const int M = x.M, N = x.nx, LS = x.LS, ps = x.ps;
   UR* out = static_cast<UR*>(x.out) + field * x.out_field;
+  const bool vec = (N & 1) == 0 && (x.out_line & 1) == 0 &&
+                   (reinterpret_cast<uintptr_t>(out) & (2 * sizeof(UR) - 1)) == 0;
+  if (vec) {
+    const int NH = N >> 1;
+    const FastDiv fNH((uint32_t)NH);
+    for (int e = threadIdx.x; e < M * NH; e += blockDim.x) {
+      const int pr = (int)fNH.div((uint32_t)e);
+      const int n = 2 * (e - pr * NH);
+      const int line = 2 * (p0 + pr);
+      if (line >= x.nlines) continue;
+      const W a = sm[pr * LS + pad_index(n, ps)];  // n even: n and n+1 never straddle a pad
+      const W b = sm[pr * LS + pad_index(n, ps) + 1];
+      UR* o = out + (long long)line * x.out_line + n;
+      if constexpr (P::kF64) {
+        *reinterpret_cast<double2*>(o) = make_double2(P::to_ur(df{a.x, a.z}), P::to_ur(df{b.x, b.z}));
+        if (line + 1 < x.nlines)
+          *reinterpret_cast<double2*>(o + x.out_line) = make_double2(P::to_ur(df{a.y, a.w}), P::to_ur(df{b.y, b.w}));
+      } else {
+        *reinterpret_cast<float2*>(o) = make_float2(a.x, b.x);
+        if (line + 1 < x.nlines) *reinterpret_cast<float2*>(o + x.out_line) = make_float2(a.y, b.y);
+      }
+    }
+    return;
+  }
   const float* smf = reinterpret_cast<const float*>(sm);
   constexpr int kW = sizeof(W) / sizeof(float);
   const FastDiv fN((uint32_t)N);
