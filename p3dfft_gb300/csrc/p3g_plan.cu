@@ -422,8 +422,11 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
     pp.chunk = esize;
     CUtensorMap map;
     std::memset(&map, 0, sizeof(map));
-    if (p->use_tma && s.in_xs == 1 && s.pre <= 1 && s.lmap_a0 >= s.L && s.lmap_a1 >= s.L &&
-        (!s.in_user || device_memory(s.in))) {
+    // TMA boxes copy rows one to one: the load map must be the identity
+    // (no zero band and no shift; the backward passes of an unpruned grid
+    // have a0 == a1 and d == 0)
+    const bool identity_rows = (s.lmap_a0 >= s.L && s.lmap_a1 >= s.L) || (s.lmap_d == 0 && s.lmap_a0 >= s.lmap_a1);
+    if (p->use_tma && s.in_xs == 1 && s.pre <= 1 && identity_rows && (!s.in_user || device_memory(s.in))) {
       const int brows = pick_box_rows(s.L, ap.n, s.M, esize);
       if (brows > 0 && encode_strided_map(&map, s.in, esize, s.X, s.L, s.O1, nv, s.in_axis, s.in_o1, s.in_o2, s.M,
                                           brows)) {
