@@ -151,23 +151,25 @@ class Plan:
         """Forward transform into a host (pinned) complex tensor, the host
         copies overlapped with the Z pass in row blocks (p3g_ftran_r2c_to_host)."""
         import torch
-        stage = torch.empty(self.complex_shape, dtype=self._dtypes()[1], device=x.device)
-        cs = copy_stream or torch.cuda.Stream(device=x.device)
+        dev = x.device if x.is_cuda else torch.device("cuda", torch.cuda.current_device())
+        stage = torch.empty(self.complex_shape, dtype=self._dtypes()[1], device=dev)
+        cs = copy_stream or torch.cuda.Stream(device=dev)
         st = _stream_ptr(stream)
         _check(_core().p3g_ftran_r2c_to_host(self._h, _ptr(x), _ptr(out_host), _ptr(stage), op.encode(), chunks, st,
                                              _stream_ptr(cs)))
-        torch.cuda.synchronize(x.device)
+        torch.cuda.synchronize(dev)
         return out_host
 
     def btran_c2r_from_host(self, c_host, out, op="tff", chunks=8, stream=None, copy_stream=None):
         """Backward transform of a host (pinned) complex tensor, the host copies
         overlapped with the Z pass in row blocks (p3g_btran_c2r_from_host)."""
         import torch
-        stage = torch.empty(self.complex_shape, dtype=self._dtypes()[1], device=out.device)
-        cs = copy_stream or torch.cuda.Stream(device=out.device)
+        dev = out.device if out.is_cuda else torch.device("cuda", torch.cuda.current_device())
+        stage = torch.empty(self.complex_shape, dtype=self._dtypes()[1], device=dev)
+        cs = copy_stream or torch.cuda.Stream(device=dev)
         _check(_core().p3g_btran_c2r_from_host(self._h, _ptr(c_host), _ptr(stage), _ptr(out), op.encode(), chunks,
                                                _stream_ptr(stream), _stream_ptr(cs)))
-        torch.cuda.synchronize(out.device)
+        torch.cuda.synchronize(dev)
         return out
 
     def spectrum(self, b, kmax=0, scale=1.0, flags=None, nv=1, dim_in=0, out=None, stream=None):

@@ -401,7 +401,8 @@ bool device_memory(const void* ptr) {
 }
 
 template <class P>
-int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int nv, cudaStream_t st) {
+int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int nv, cudaStream_t st,
+                int max_sms = 0) {
   s.M = ap.M;
   s.log2m = ap.log2m;
   s.N = ap.n;
@@ -436,7 +437,7 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
         pp.box_bytes = brows * s.M * esize;
       }
     }
-    const int slots = p->sm_count * ap.pipe_bps;
+    const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
     const int grid = pp.c.ntiles < slots ? pp.c.ntiles : slots;
     cudaError_t e = launch_strided_pipe<P>(&map, pp, p->d_sp + ap.sp_index, p->d_tw, fwd_sign, kElemsPerThread,
                                            ap.pipe_threads, ap.pipe_smem, grid, st);
@@ -451,7 +452,7 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
 }
 
 template <class P>
-int run_x_r2c(p3g_plan p, XParams& x, int nv, cudaStream_t st) {
+int run_x_r2c(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) {
   const AxisPlan& ap = p->ax_x;
   using UR = typename P::UR;
   if (p->use_pipe && ap.pipe_ok) {
@@ -471,7 +472,7 @@ int run_x_r2c(p3g_plan p, XParams& x, int nv, cudaStream_t st) {
     xp.c.tw_count = ap.tw_cnt;
     xp.c.buf_elems = ap.buf_elems;
     xp.c.err = p->d_err;
-    const int slots = p->sm_count * ap.pipe_bps;
+    const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
     const int grid = xp.c.ntiles < slots ? xp.c.ntiles : slots;
     cudaError_t e = launch_xr2c_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, kElemsPerThread, ap.pipe_threads,
                                         ap.pipe_smem, grid, st);
@@ -486,7 +487,7 @@ int run_x_r2c(p3g_plan p, XParams& x, int nv, cudaStream_t st) {
 }
 
 template <class P>
-int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st) {
+int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) {
   const AxisPlan& ap = p->ax_x;
   if (p->use_pipe && ap.pipe_ok) {
     x.M = ap.pipe_m;
@@ -501,7 +502,7 @@ int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st) {
     xp.c.tw_count = ap.tw_cnt;
     xp.c.buf_elems = ap.buf_elems;
     xp.c.err = p->d_err;
-    const int slots = p->sm_count * ap.pipe_bps;
+    const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
     const int grid = xp.c.ntiles < slots ? xp.c.ntiles : slots;
     cudaError_t e = launch_xc2r_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, kElemsPerThread, ap.pipe_threads,
                                         ap.pipe_smem, grid, st);
@@ -784,6 +785,39 @@ struct EventSet {
   }
 };
 
+// z-slabs of the X and Y passes: slab c covers planes [c*nz/K, (c+1)*nz/K).
+XParams x_planes(const XParams& x, int ny, int z0, int z1, size_t in_es, size_t out_es) {
+  XParams s = x;
+  s.in = static_cast<const unsigned char*>(x.in) + (size_t)z0 * ny * x.in_line * in_es;
+  s.out = static_cast<unsigned char*>(x.out) + (size_t)z0 * ny * x.out_line * out_es;
+  s.nlines = ny * (z1 - z0);
+  s.tiles = ((s.nlines + 1) / 2 + s.M - 1) / s.M;
+  return s;
+}
+SParams y_planes(const SParams& y, int z0, int z1, size_t es) {
+  SParams s = y;
+  s.O1 = z1 - z0;
+  s.in = static_cast<const unsigned char*>(y.in) + (size_t)z0 * y.in_o1 * es;
+  s.out = static_cast<unsigned char*>(y.out) + (size_t)z0 * y.out_o1 * es;
+  return s;
+}
+
+int aux_stream(p3g_plan p, cudaStream_t& aux) {
+  if (!p->aux && cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    p->aux = nullptr;
+    return fail(P3G_E_CUDA, "stream creation failed");
+  }
+  aux = p->aux;
+  return P3G_OK;
+}
+
+// When the real array lives in host memory the X pass is bound by the host
+// link, not by the SMs: the X and Y passes then run in z-slabs on two
+// streams, the X pass of slab k+1 (on a third of the SMs) reading the host
+// while the Y pass of slab k computes on the rest.
+constexpr int kZSlabs = 8;
+
 // Forward transform into a host array: X and Y passes, then the Z pass in row
 // blocks, each block's output copied to the host on cs while the next block
 // computes.
@@ -801,17 +835,45 @@ int do_ftran_to_host(p3g_plan p, const void* in, void* out_host, void* stage, co
   XParams x;
   SParams y, z;
   make_forward_params(p, in, stage, p->wa, p->wb, zi, rsize, csize, x, y, z);
-  {
-    PassTimer tm(p, 4, st);
-    if ((rc = run_x_r2c<P>(p, x, 1, st))) return rc;
-    tm.done();
-  }
-  {
-    PassTimer tm(p, 6, st);
-    if ((rc = run_strided<P>(p, y, p->ax_y, true, 1, st))) return rc;
-    tm.done();
-  }
   const size_t es = p->esize();
+  if (!device_memory(in) && p->nz >= 2) {
+    cudaStream_t aux;
+    if ((rc = aux_stream(p, aux))) return rc;
+    const int x_sms = std::max(1, p->sm_count / 3), y_sms = p->sm_count - x_sms;
+    const auto slabs = row_blocks(p->nz, kZSlabs);
+    EventSet ev(slabs.size() + 2);
+    cudaError_t e = cudaEventRecord(ev.ev[0], st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, ev.ev[0], 0);
+    for (size_t k = 0; k < slabs.size() && e == cudaSuccess; ++k) {
+      XParams xs = x_planes(x, p->ny, slabs[k].y0, slabs[k].y1, sizeof(typename P::UR), es);
+      {
+        PassTimer tm(p, 4, st);
+        if ((rc = run_x_r2c<P>(p, xs, 1, st, x_sms))) return rc;
+        tm.done();
+      }
+      e = cudaEventRecord(ev.ev[k + 1], st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, ev.ev[k + 1], 0);
+      if (e != cudaSuccess) break;
+      SParams ys = y_planes(y, slabs[k].y0, slabs[k].y1, es);
+      PassTimer tm(p, 6, aux);
+      if ((rc = run_strided<P>(p, ys, p->ax_y, true, 1, aux, y_sms))) return rc;
+      tm.done();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(ev.ev[slabs.size() + 1], aux);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev.ev[slabs.size() + 1], 0);
+    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("stream order: ") + cudaGetErrorString(e));
+  } else {
+    {
+      PassTimer tm(p, 4, st);
+      if ((rc = run_x_r2c<P>(p, x, 1, st))) return rc;
+      tm.done();
+    }
+    {
+      PassTimer tm(p, 6, st);
+      if ((rc = run_strided<P>(p, y, p->ax_y, true, 1, st))) return rc;
+      tm.done();
+    }
+  }
   const auto blocks = row_blocks(p->nyc, chunks);
   EventSet evs(blocks.size());
   const size_t pitch = (size_t)p->nyc * p->nxhpc * es;
@@ -874,6 +936,34 @@ int do_btran_from_host(p3g_plan p, const void* in_host, void* stage, void* out, 
     PassTimer tm(p, 8, st);
     if ((rc = run_strided<P>(p, zc, p->ax_z[zi], fsign, 1, st))) return rc;
     tm.done();
+  }
+  if (!device_memory(out) && p->nz >= 2) {
+    // host output: the Y pass of slab k+1 computes while the X pass of slab k
+    // writes its lines over the host link
+    cudaStream_t aux;
+    if ((rc = aux_stream(p, aux))) return rc;
+    const int x_sms = std::max(1, p->sm_count / 3), y_sms = p->sm_count - x_sms;
+    const auto slabs = row_blocks(p->nz, kZSlabs);
+    EventSet ev(slabs.size() + 1);
+    for (size_t k = 0; k < slabs.size() && e == cudaSuccess; ++k) {
+      SParams ys = y_planes(y, slabs[k].y0, slabs[k].y1, es);
+      {
+        PassTimer tm(p, 9, st);
+        if ((rc = run_strided<P>(p, ys, p->ax_y, false, 1, st, y_sms))) return rc;
+        tm.done();
+      }
+      e = cudaEventRecord(ev.ev[k], st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, ev.ev[k], 0);
+      if (e != cudaSuccess) break;
+      XParams xs = x_planes(x, p->ny, slabs[k].y0, slabs[k].y1, es, sizeof(typename P::UR));
+      PassTimer tm(p, 11, aux);
+      if ((rc = run_x_c2r<P>(p, xs, 1, aux, x_sms))) return rc;
+      tm.done();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(ev.ev[slabs.size()], aux);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev.ev[slabs.size()], 0);
+    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("stream order: ") + cudaGetErrorString(e));
+    return P3G_OK;
   }
   {
     PassTimer tm(p, 9, st);
@@ -1069,6 +1159,7 @@ int p3g_plan_destroy(p3g_plan p) {
     cudaEventDestroy(r.b);
   }
   for (auto e : p->free_events) cudaEventDestroy(e);
+  if (p->aux) cudaStreamDestroy(p->aux);
   if (p->wa) cudaFree(p->wa);
   if (p->wb) cudaFree(p->wb);
   if (p->d_tw) cudaFree(p->d_tw);

@@ -69,6 +69,7 @@ struct p3g_plan_s {
   std::vector<TimerRec> pending;
   std::vector<cudaEvent_t> free_events;
   long long launches = 0;
+  cudaStream_t aux = nullptr;  // second compute stream of the host-array transforms
   std::mutex mu;
   int sm_count = 0;
   int* d_err = nullptr;  // set by a kernel whose bounded wait timed out

@@ -393,23 +393,27 @@ def test_host_arrays_direct_and_staged(torch_cuda, tmp_path, direct):
     assert orc.normalised_linf(d["pr"], ref.btran_c2r(ref.ftran_r2c(a, "ffc"), "cff")) <= F64_TOL
 
 
+@pytest.mark.parametrize("real_on_host", [False, True])
 @pytest.mark.parametrize("chunks", [1, 3, 8, 100])
-@pytest.mark.parametrize("args", [(48, 40, 36), (33, 20, 16, 20, 9, 10)])
-def test_host_row_block_transforms(torch_cuda, args, chunks):
+@pytest.mark.parametrize("args", [(48, 40, 36), (33, 20, 16, 20, 9, 10), (16, 12, 3)])
+def test_host_row_block_transforms(torch_cuda, args, chunks, real_on_host):
     # p3g_ftran_r2c_to_host / p3g_btran_c2r_from_host: the Z pass in row
-    # blocks with the host copies overlapped; bit-identical to the plain calls
+    # blocks with the host copies overlapped (and, with the real array in host
+    # memory, the X and Y passes in z-slabs on two streams); bit-identical to
+    # the plain calls
     import p3dfft_gb300 as pg
     torch = torch_cuda
     nx, ny, nz = args[:3]
     plan = pg.Plan(*args, precision=pg.F64)
     x = torch.from_numpy(_rand((nz, ny, nx), 41)).cuda()
     want_b = plan.ftran_r2c(x)
-    hb = torch.zeros(plan.complex_shape, dtype=torch.complex128).pin_memory()
-    plan.ftran_r2c_to_host(x, hb, chunks=chunks)
-    assert torch.equal(hb, want_b.cpu())
     want_r = plan.btran_c2r(want_b)
-    r = torch.zeros_like(x)
+    xin = x.cpu().pin_memory() if real_on_host else x
+    hb = torch.zeros(plan.complex_shape, dtype=torch.complex128).pin_memory()
+    plan.ftran_r2c_to_host(xin, hb, chunks=chunks)
+    assert torch.equal(hb, want_b.cpu())
+    r = torch.zeros((nz, ny, nx), dtype=torch.float64).pin_memory() if real_on_host else torch.zeros_like(x)
     plan.btran_c2r_from_host(hb, r, chunks=chunks)
-    assert torch.equal(r, want_r)
+    assert torch.equal(r.cpu(), want_r.cpu())
     plan.check()
     plan.close()
