@@ -1,6 +1,6 @@
 // Pipelined (persistent, double-buffered) pass kernels.
 //
-// One CTA per SM walks a strided list of tiles.  While it transforms tile i
+// Each CTA walks a strided list of tiles (grid = SMs x resident CTAs).  While it transforms tile i
 // in shared buffer b, the copy of tile i+1 into buffer b^1 is already in
 // flight (TMA tensor tiles or cp.async), so HBM traffic overlaps the
 // double-float butterflies.  Each tile goes through: a fix-up step in shared
@@ -38,16 +38,6 @@ struct XPipeParams {
   PipeCommon c;
   int chunk;                // r2c: cp.async bytes per copy (4, 8 or 16)
 };
-
-// Hides a pointer's value from the optimiser.  The persistent loops below
-// re-derive their parameter block through it in every phase: otherwise the
-// compiler hoists the loads of all pass parameters out of the tile loop and
-// keeps them live across the FFT, which spills.
-template <class T>
-P3G_D T* opaque(T* p) {
-  asm volatile("" : "+l"(p));
-  return p;
-}
 
 P3G_D unsigned char* align1k(unsigned char* p) {
   return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
