@@ -55,6 +55,20 @@ struct PipeLimits {
   static constexpr int kMinBlocks = 65536 / 128 / kMaxThreads;
 };
 
+// X passes on the F64 path: 256-thread CTAs, three per SM (85 registers),
+// with the twiddles read from the global table through L1 instead of a
+// shared-memory copy, which leaves room for three double-buffered tiles per
+// SM.  The X passes gain from the extra resident warps; the strided passes,
+// whose tiles must stay 4 columns wide for their long-stride DRAM rows, keep
+// PipeLimits.
+template <class P>
+struct XPipeLimits {
+  static constexpr int kE = PipeLimits<P>::kE;
+  static constexpr int kMaxThreads = P::kF64 ? 256 : PipeLimits<P>::kMaxThreads;
+  static constexpr int kMinBlocks = P::kF64 ? 3 : PipeLimits<P>::kMinBlocks;
+  static constexpr bool kSharedTwiddles = !P::kF64;
+};
+
 // ------------------------------------------------------------ strided Y/Z
 template <class P>
 struct StridedSmem {
@@ -416,10 +430,11 @@ P3G_D void xr2c_store(const XParams& x, const typename P::W* sm, int p0, int fie
 }
 
 template <class P>
-__global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMinBlocks)
+__global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::kMinBlocks)
     k_xr2c_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
                 const float4* __restrict__ tw_g) {
-  {
+  constexpr bool kTwS = XPipeLimits<P>::kSharedTwiddles;
+  if constexpr (kTwS) {
     float4* tw_s = xpipe_tw<P>(pp.c);
     for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) tw_s[i] = __ldg(tw_g + pp.c.tw_base + i);
   }
@@ -435,10 +450,11 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
     else cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
-    xr2c_pack<P, PipeLimits<P>::kE>(pp.x, xpipe_buf<P>(pp.c, b));
+    xr2c_pack<P, XPipeLimits<P>::kE>(pp.x, xpipe_buf<P>(pp.c, b));
     {
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
-      cta_fft<P, -1, PipeLimits<P>::kE>(t, sp, xpipe_tw<P>(pp.c), pp.c.tw_base);
+      if constexpr (kTwS) cta_fft<P, -1, XPipeLimits<P>::kE>(t, sp, xpipe_tw<P>(pp.c), pp.c.tw_base);
+      else cta_fft<P, -1, XPipeLimits<P>::kE>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;
@@ -573,10 +589,11 @@ P3G_D void xc2r_store(const XParams& x, const typename P::W* sm, int p0, int fie
 }
 
 template <class P>
-__global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMinBlocks)
+__global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::kMinBlocks)
     k_xc2r_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
                 const float4* __restrict__ tw_g) {
-  {
+  constexpr bool kTwS = XPipeLimits<P>::kSharedTwiddles;
+  if constexpr (kTwS) {
     float4* tw_s = xpipe_tw<P>(pp.c);
     for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) tw_s[i] = __ldg(tw_g + pp.c.tw_base + i);
   }
@@ -592,10 +609,11 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
     else cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
-    xc2r_merge<P, PipeLimits<P>::kE / 2 + 2>(pp.x, xpipe_buf<P>(pp.c, b));  // host: T * MAXI >= M nh
+    xc2r_merge<P, XPipeLimits<P>::kE / 2 + 2>(pp.x, xpipe_buf<P>(pp.c, b));  // host: T * MAXI >= M nh
     {
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
-      cta_fft<P, 1, PipeLimits<P>::kE>(t, sp, xpipe_tw<P>(pp.c), pp.c.tw_base);
+      if constexpr (kTwS) cta_fft<P, 1, XPipeLimits<P>::kE>(t, sp, xpipe_tw<P>(pp.c), pp.c.tw_base);
+      else cta_fft<P, 1, XPipeLimits<P>::kE>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;

@@ -198,8 +198,11 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   ap.pipe_ok = false;
   if (ap.sp.nstages < 1 || ap.sp.has_generic || ap.n < 2) return;
   const size_t esize = f64 ? 16 : 8;
-  const int max_threads = f64 ? PipeLimits<PathF64>::kMaxThreads : PipeLimits<PathF32>::kMaxThreads;
+  const bool xk = kind != 0;  // X kernels have their own launch shape (XPipeLimits)
+  const int max_threads = f64 ? (xk ? XPipeLimits<PathF64>::kMaxThreads : PipeLimits<PathF64>::kMaxThreads)
+                              : (xk ? XPipeLimits<PathF32>::kMaxThreads : PipeLimits<PathF32>::kMaxThreads);
   const int E = f64 ? PipeLimits<PathF64>::kE : PipeLimits<PathF32>::kE;
+  const bool tw_shared = !xk || (f64 ? XPipeLimits<PathF64>::kSharedTwiddles : XPipeLimits<PathF32>::kSharedTwiddles);
   const int n = ap.n;
   const int nh = n / 2 + 1;
   auto threads_for = [&](int M) {
@@ -216,15 +219,16 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
     // buffer stride rounded to 1 KB so both buffers (TMA destinations) stay aligned
     const size_t need = (size_t)(kind == 0 ? M * n : M * (ap.ls > 2 * nh ? ap.ls : 2 * nh)) * esize;
     buf_bytes = (need + 1023) / 1024 * 1024;
-    return 1024 + 2 * buf_bytes + (size_t)ap.tw_cnt * 16 + 16;
+    return 1024 + 2 * buf_bytes + (tw_shared ? (size_t)ap.tw_cnt * 16 : 0) + 16;
   };
-  // resident warps per SM for tile width M: 128 registers per thread, 2048
-  // threads and ~228 KB of shared memory per SM
+  // resident warps per SM for tile width M: registers per thread from the
+  // kernel's launch bounds, 2048 threads and ~228 KB of shared memory per SM
   auto warps_for = [&](int M) {
     const int t = threads_for(M);
     size_t bb;
     const size_t sm = smem_for(M, bb);
-    int b = 65536 / (128 * t);
+    const int regs = (xk && f64) ? 65536 / (256 * XPipeLimits<PathF64>::kMinBlocks) : 128;
+    int b = 65536 / (regs * t);
     b = std::min(b, 2048 / t);
     b = std::min(b, (int)((228 * 1024) / sm));
     return b * t / 32;
