@@ -55,18 +55,16 @@ struct PipeLimits {
   static constexpr int kMinBlocks = 65536 / 128 / kMaxThreads;
 };
 
-// X passes on the F64 path: 256-thread CTAs, three per SM (85 registers),
-// with the twiddles read from the global table through L1 instead of a
-// shared-memory copy, which leaves room for three double-buffered tiles per
-// SM.  The X passes gain from the extra resident warps; the strided passes,
-// whose tiles must stay 4 columns wide for their long-stride DRAM rows, keep
-// PipeLimits.
+// X passes: 256-thread CTAs, three per SM (85 registers), with the twiddles
+// read from the global table through L1 instead of a shared-memory copy, which
+// leaves room for three double-buffered tiles per SM.  The X passes gain from
+// the extra resident warps; the strided passes, whose tiles must stay wide for
+// their long-stride DRAM rows, keep PipeLimits.
 template <class P>
 struct XPipeLimits {
   static constexpr int kE = PipeLimits<P>::kE;
-  static constexpr int kMaxThreads = P::kF64 ? 256 : PipeLimits<P>::kMaxThreads;
-  static constexpr int kMinBlocks = P::kF64 ? 3 : PipeLimits<P>::kMinBlocks;
-  static constexpr bool kSharedTwiddles = !P::kF64;
+  static constexpr int kMaxThreads = 256;
+  static constexpr int kMinBlocks = 3;
 };
 
 // ------------------------------------------------------------ strided Y/Z
@@ -292,10 +290,6 @@ P3G_D typename P::W* xpipe_buf(const PipeCommon& pc, int b) {
   extern __shared__ unsigned char p3g_pipe_smem[];
   return reinterpret_cast<typename P::W*>(align1k(p3g_pipe_smem)) + b * pc.buf_elems;
 }
-template <class P>
-P3G_D float4* xpipe_tw(const PipeCommon& pc) {
-  return reinterpret_cast<float4*>(xpipe_buf<P>(pc, 2));
-}
 
 // r2c: real lines 2p, 2p+1 of the tile (first pair p0 of field `field`)
 // copied raw ([line][x]) into dst, `chunk` bytes per copy, without a commit.
@@ -433,12 +427,6 @@ template <class P>
 __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::kMinBlocks)
     k_xr2c_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
                 const float4* __restrict__ tw_g) {
-  constexpr bool kTwS = XPipeLimits<P>::kSharedTwiddles;
-  if constexpr (kTwS) {
-    float4* tw_s = xpipe_tw<P>(pp.c);
-    for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) tw_s[i] = __ldg(tw_g + pp.c.tw_base + i);
-  }
-  __syncthreads();
   int it = 0;
   int tile = blockIdx.x;
   if (tile < pp.c.ntiles) xr2c_issue<P>(pp, tile, 0);
@@ -453,8 +441,7 @@ __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::k
     xr2c_pack<P, XPipeLimits<P>::kE>(pp.x, xpipe_buf<P>(pp.c, b));
     {
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
-      if constexpr (kTwS) cta_fft<P, -1, XPipeLimits<P>::kE>(t, sp, xpipe_tw<P>(pp.c), pp.c.tw_base);
-      else cta_fft<P, -1, XPipeLimits<P>::kE>(t, sp, tw_g, 0);
+      cta_fft<P, -1, XPipeLimits<P>::kE>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;
@@ -592,12 +579,6 @@ template <class P>
 __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::kMinBlocks)
     k_xc2r_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
                 const float4* __restrict__ tw_g) {
-  constexpr bool kTwS = XPipeLimits<P>::kSharedTwiddles;
-  if constexpr (kTwS) {
-    float4* tw_s = xpipe_tw<P>(pp.c);
-    for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) tw_s[i] = __ldg(tw_g + pp.c.tw_base + i);
-  }
-  __syncthreads();
   int it = 0;
   int tile = blockIdx.x;
   if (tile < pp.c.ntiles) xc2r_issue<P>(pp, tile, 0);
@@ -612,8 +593,7 @@ __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::k
     xc2r_merge<P, XPipeLimits<P>::kE / 2 + 2>(pp.x, xpipe_buf<P>(pp.c, b));  // host: T * MAXI >= M nh
     {
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
-      if constexpr (kTwS) cta_fft<P, 1, XPipeLimits<P>::kE>(t, sp, xpipe_tw<P>(pp.c), pp.c.tw_base);
-      else cta_fft<P, 1, XPipeLimits<P>::kE>(t, sp, tw_g, 0);
+      cta_fft<P, 1, XPipeLimits<P>::kE>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;

@@ -202,7 +202,7 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   const int max_threads = f64 ? (xk ? XPipeLimits<PathF64>::kMaxThreads : PipeLimits<PathF64>::kMaxThreads)
                               : (xk ? XPipeLimits<PathF32>::kMaxThreads : PipeLimits<PathF32>::kMaxThreads);
   const int E = f64 ? PipeLimits<PathF64>::kE : PipeLimits<PathF32>::kE;
-  const bool tw_shared = !xk || (f64 ? XPipeLimits<PathF64>::kSharedTwiddles : XPipeLimits<PathF32>::kSharedTwiddles);
+  const bool tw_shared = !xk;  // the X kernels read the global table
   const int n = ap.n;
   const int nh = n / 2 + 1;
   auto threads_for = [&](int M) {
@@ -227,7 +227,7 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
     const int t = threads_for(M);
     size_t bb;
     const size_t sm = smem_for(M, bb);
-    const int regs = (xk && f64) ? 65536 / (256 * XPipeLimits<PathF64>::kMinBlocks) : 128;
+    const int regs = xk ? 65536 / (XPipeLimits<PathF64>::kMaxThreads * XPipeLimits<PathF64>::kMinBlocks) : 128;
     int b = 65536 / (regs * t);
     b = std::min(b, 2048 / t);
     b = std::min(b, (int)((228 * 1024) / sm));
