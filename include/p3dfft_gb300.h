@@ -151,6 +151,12 @@ int p3g_batch_replay(p3g_batch batch, void* stream);
 int p3g_batch_status(p3g_batch batch, void* stream);
 /* info = {passes, work items, persistent CTAs, launches so far} */
 int p3g_batch_info(p3g_batch batch, long long info[4]);
+/* Test hook for the bounded dependency waits: makes the passes that depend
+ * on pass `pass` (queue order, as numbered by set_jobs) wait for a tile that
+ * never completes, so their waits run out (about 4 s) and the next
+ * p3g_batch_status reports the time-out; the launch ends and the context stays
+ * usable.  The next p3g_batch_set_jobs clears it. */
+int p3g_batch_block_pass(p3g_batch batch, int pass);
 int p3g_batch_destroy(p3g_batch batch);
 
 /* The reference's 12 accumulating stage timers (build/module.F90:106,709-744),

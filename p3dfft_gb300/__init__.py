@@ -275,6 +275,10 @@ class Batch:
     def check(self, stream=None):
         _check(_core().p3g_batch_status(self._h, _stream_ptr(stream)))
 
+    def block_pass(self, index):
+        """Test hook: the waits on pass `index` run out (p3g_batch_block_pass)."""
+        _check(_core().p3g_batch_block_pass(self._h, int(index)))
+
     def info(self):
         a = (ctypes.c_longlong * 4)()
         _check(_core().p3g_batch_info(self._h, a))

@@ -52,6 +52,7 @@ CORE_SIGNATURES = {
     "p3g_batch_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "p3g_batch_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "p3g_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "p3g_batch_block_pass": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "p3g_spectrum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
                                     ctypes.c_int, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p]),
     "p3g_plan_set_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),

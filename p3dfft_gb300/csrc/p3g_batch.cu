@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -712,6 +713,19 @@ int p3g_batch_status(p3g_batch b, void* stream) {
   e = cudaMemcpy(&err, b->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch status: ") + cudaGetErrorString(e));
   if (err) return fail(P3G_E_CUDA, "batch kernel: a dependency wait timed out");
+  return P3G_OK;
+}
+
+int p3g_batch_block_pass(p3g_batch b, int pass) {
+  if (!b || b->nitems == 0) return fail(P3G_E_STATE, "batch has no jobs");
+  if (pass < 0 || pass >= b->npass) return fail(P3G_E_ARG, "pass index out of range");
+  std::lock_guard<std::mutex> lk(b->mu);
+  // waiters compare the pass's done-counter with this device copy of its tile
+  // count; one more than the pass has makes every dependent wait run out
+  const int blocked = b->host[pass].tiles + 1;
+  cudaError_t e = cudaMemcpy(reinterpret_cast<unsigned char*>(b->d_pass + pass) + offsetof(BatchPass, tiles), &blocked,
+                             sizeof(int), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("block pass: ") + cudaGetErrorString(e));
   return P3G_OK;
 }
 

@@ -232,3 +232,29 @@ def test_autotuner_picks_and_caches(torch_cuda, tmp_path, monkeypatch):
     jobs = _make_jobs(torch, SHAPES[:4], [pg.JOB_ROUNDTRIP] * 4, pg.F64, seed=9)
     w, times = autotune.tune_window(jobs, pg.F64, reps=2)
     assert w in times and all(t > 0 for t in times.values())
+
+
+def test_batch_dependency_wait_times_out_and_context_survives(torch_cuda):
+    # a dependency that can never complete: every wait on it runs out after
+    # its poll limit (~4 s), the launch ends, the status reports the time-out,
+    # and the next batch on the same context works
+    import time
+
+    import p3dfft_gb300 as pg
+    torch = torch_cuda
+    jobs = _make_jobs(torch, SHAPES[:2], [pg.JOB_ROUNDTRIP] * 2, pg.F64, seed=10)
+    b = pg.Batch(pg.F64).set_jobs(jobs)
+    b.block_pass(0)  # the X pass of job 0: its Y pass waits forever
+    t = time.perf_counter()
+    b.launch()
+    with pytest.raises(pg.P3DFFTError, match="timed out"):
+        b.check()
+    assert time.perf_counter() - t < 60
+    b.set_jobs(jobs)
+    b.launch()
+    b.check()
+    for j in jobs:
+        want = _alone(torch, j["plan"], j["kind"], j["in"])
+        torch.cuda.synchronize()
+        assert torch.equal(j["out"], want)
+    b.close()
