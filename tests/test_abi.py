@@ -75,3 +75,20 @@ def test_header_compiles_as_c(tmp_path):
     res = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-c", "-I", os.path.join(ROOT, "include"),
                           str(src), "-o", str(tmp_path / "t.o")], capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
+
+
+def test_fortran_module_binds_exported_symbols(lib):
+    # include/p3dfft.F90 (not compiled here: no Fortran compiler) binds every
+    # routine to a C symbol of the drop-in libraries
+    text = open(os.path.join(ROOT, "include", "p3dfft.F90")).read()
+    names = re.findall(r"bind\(C,\s*name='(\w+)'\)", text)
+    assert {"p3dfft_setup", "p3dfft_ftran_r2c", "p3dfft_btran_c2r", "p3dfft_get_dims", "p3dfft_clean",
+            "p3dfft_cheby", "get_timers", "set_timers"} <= set(names)
+    for name in names:
+        assert hasattr(lib.legacy, name), name
+        assert hasattr(lib.legacy_single, name), name
+    # the reference module's public names are all there
+    for name in ("p3dfft_type", "r8", "i8", "timers", "p3dfft_setup", "p3dfft_get_dims", "p3dfft_ftran_r2c",
+                 "p3dfft_btran_c2r", "p3dfft_ftran_r2c_many", "p3dfft_btran_c2r_many", "p3dfft_cheby",
+                 "p3dfft_cheby_many", "p3dfft_clean", "get_timers", "set_timers", "p3dfft_get_mpi_info"):
+        assert re.search(r"public\s*::[^\n]*\b%s\b" % name, text), name
