@@ -417,3 +417,27 @@ def test_host_row_block_transforms(torch_cuda, args, chunks, real_on_host):
     assert torch.equal(r.cpu(), want_r.cpu())
     plan.check()
     plan.close()
+
+
+@pytest.mark.parametrize("case", [((4096, 6, 4), "f64"), ((6, 4096, 4), "f64"), ((4, 6, 4096), "f64"),
+                                  ((8192, 4, 2), "f32"), ((4, 2, 8192), "f32")])
+def test_longest_lines(torch_cuda, case):
+    # the longest lines one tile holds: 4096 points on the F64 path, 8192 on F32
+    import p3dfft_gb300 as pg
+    shape, prec = case
+    a = _rand(shape[::-1], 43)
+    if prec == "f64":
+        gb, wb, gr, wr = _run_pair(torch_cuda, shape, a, "fft", "tff", pg.F64)
+        assert orc.normalised_linf(gb, wb) <= F64_TOL
+        assert orc.normalised_linf(gr, wr) <= F64_TOL
+    else:
+        gb, wb, gr, wr = _run_pair(torch_cuda, shape, a, "fft", "tff", pg.F32)
+        assert orc.relative_l2(gb, wb) <= F32_TOL
+        assert orc.relative_l2(gr, wr) <= F32_TOL
+
+
+@pytest.mark.parametrize("shape", [(8192, 4, 4), (4, 8192, 4), (4, 4, 16384)])
+def test_too_long_lines_are_rejected(torch_cuda, shape):
+    import p3dfft_gb300 as pg
+    with pytest.raises(pg.P3DFFTError, match="too long|unsupported"):
+        pg.Plan(*shape, precision=pg.F64)
