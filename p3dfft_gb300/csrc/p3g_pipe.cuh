@@ -131,6 +131,38 @@ P3G_D void strided_copy(const SParams& s, typename P::W* dst, int xt, int o1, in
     }
   };
   const int T = blockDim.x;
+  if constexpr (esz == 8) {
+    // 8-byte elements with adjacent columns: two columns per 16-byte copy when
+    // the tile's first column and the row stride keep the pair 16-byte aligned
+    // (a tile whose pair would cross the last valid column copies singly)
+    const bool pairs = s.in_xs == 1 && M >= 2 && ((ib | s.in_axis) & 1) == 0 &&
+                       (reinterpret_cast<uintptr_t>(in) & 15) == 0 && xt * M + M <= s.X;
+    if (pairs) {
+      const int MP = M >> 1, lmp = s.log2m - 1;
+      for (int e = threadIdx.x; e < MP * L; e += T) {
+        const int m = 2 * (e & (MP - 1));
+        const int j = e >> lmp;
+        const int src = j >= s.lmap_a1 ? j - s.lmap_d : (j < s.lmap_a0 ? j : -1);
+        const bool ok = src >= 0;
+        const char* g = ok ? in + (ib + m + (long long)src * s.in_axis) * esz : in;
+        const uint32_t nb = ok ? 16u : 0u;
+        int r0 = j, r1 = -1;
+        if (s.pre == 2) {
+          r0 = j + 1;
+          r1 = 2 * (L + 1) - (j + 1);
+        } else if (s.pre == 1 && j >= 1 && j <= L - 2) {
+          r1 = 2 * (L - 1) - j;
+        }
+        cp_async16(dst + r0 * M + m, g, nb);
+        if (r1 >= 0) cp_async16(dst + r1 * M + m, g, nb);
+        if (s.pre == 2 && j == 0) {
+          cp_async16(dst + m, in, 0);
+          cp_async16(dst + (L + 1) * M + m, in, 0);
+        }
+      }
+      return;
+    }
+  }
   if (s.in_xs != 1) {  // rows adjacent in memory (STRIDE1 user layout): rows fastest
     const FastDiv div_l(L);
     for (int e = threadIdx.x; e < M * L; e += T) {
