@@ -237,55 +237,67 @@ __device__ __noinline__ void batch_process_single(const BatchPass& bp, int tile,
 
 // ctl[0] = next queue item, ctl[1] = error, ctl[2 + d] = finished tiles of pass d.
 //
-// Each CTA holds a current item and, taken while the current one is worked
-// on, the ticket of the next.  When the next item is double-buffered and its
-// dependency is already complete, its tile is copied into the other buffer
-// (cp.async) while the current tile is transformed; otherwise the CTA waits
-// for the dependency after finishing the current item and loads then.
+// Each CTA holds a current item, the next item (its ticket, pass and whether
+// its dependency was already complete when looked up) and one more ticket
+// taken ahead.  When the next item is double-buffered and its dependency was
+// complete, its tile is copied into the other buffer (cp.async) while the
+// current tile is transformed; otherwise the CTA waits for the dependency
+// after finishing the current item and loads then.  Between the end of one
+// item and the start of the next, warp 1 publishes the finished item (fence +
+// counter) while thread 0 looks up the item after next, whose ticket was
+// fetched an item earlier: neither latency waits for the other.
 template <class P>
 __global__ void __launch_bounds__(kBatchThreads, 2)
     k_batch(const BatchPass* __restrict__ passes, int npass, int nitems, int* __restrict__ ctl, int buf_elems) {
   using W = typename P::W;
   __shared__ int s_first[kFirstCache];
-  __shared__ int s_item, s_pass, s_ready;
+  __shared__ int s_item, s_pass, s_ready, s_ok, s_cur, s_cpass;
   W* const buf0 = reinterpret_cast<W*>(p3g_smem);
+  int* const err = &ctl[1];
   for (int i = threadIdx.x; i < npass && i < kFirstCache; i += blockDim.x) s_first[i] = passes[i].first;
   __syncthreads();
-  // first item: wait for its dependency, then load
-  if (threadIdx.x == 0) {
-    const int it = atomicAdd(&ctl[0], 1);
-    int d = -1;
-    if (it < nitems && ld_relaxed(&ctl[1]) == 0) {
+  // looks up item `it` (thread 0): its pass (-1 past the end or after an
+  // error) and whether its dependency is already complete
+  auto lookup = [&](int it, int& d, int& ready) {
+    d = -1;
+    ready = 0;
+    if (it < nitems && ld_relaxed(err) == 0) {
       d = find_pass(passes, s_first, npass, it);
       const int dep = passes[d].dep;
-      if (dep >= 0 && !wait_count(&ctl[2 + dep], passes[dep].tiles, &ctl[1])) d = -1;
+      ready = dep < 0 || ld_acquire(&ctl[2 + dep]) >= passes[dep].tiles;
+      if (ready) __threadfence();
     }
-    s_item = it;
-    s_pass = d;
+  };
+  int ahead = 0;  // thread 0: the ticket after the next item
+  if (threadIdx.x == 0) {
+    // first item: wait for its dependency before loading it
+    const int it = atomicAdd(&ctl[0], 1);
+    int d, r;
+    lookup(it, d, r);
+    if (d >= 0 && !r && !wait_count(&ctl[2 + passes[d].dep], passes[passes[d].dep].tiles, err)) d = -1;
+    s_cur = it;
+    s_cpass = d;
+    s_item = 0;
+    s_pass = -1;
+    s_ready = 0;
+    if (d >= 0) {
+      const int it1 = atomicAdd(&ctl[0], 1);
+      ahead = atomicAdd(&ctl[0], 1);
+      int d1, r1;
+      lookup(it1, d1, r1);
+      s_item = it1;
+      s_pass = d1;
+      s_ready = r1;
+    }
   }
   __syncthreads();
-  int cur = s_item, dc = s_pass, b = 0;
+  int cur = s_cur, dc = s_cpass, nxt = s_item, dn = s_pass, b = 0;
+  bool ready = s_ready != 0;
   if (dc >= 0 && passes[dc].pipe) batch_issue<P>(passes[dc], cur - passes[dc].first, buf0);
   cp_async_commit();
+  __syncthreads();  // every thread has read the shared item slots
 #pragma unroll 1
   while (dc >= 0) {
-    __syncthreads();  // everyone has read s_item / s_pass of the current item
-    if (threadIdx.x == 0) {
-      const int it = atomicAdd(&ctl[0], 1);
-      int d = -1, ready = 0;
-      if (it < nitems && ld_relaxed(&ctl[1]) == 0) {
-        d = find_pass(passes, s_first, npass, it);
-        const int dep = passes[d].dep;
-        ready = dep < 0 || ld_acquire(&ctl[2 + dep]) >= passes[dep].tiles;
-        if (ready) __threadfence();
-      }
-      s_item = it;
-      s_pass = d;
-      s_ready = ready;
-    }
-    __syncthreads();
-    const int nxt = s_item, dn = s_pass;
-    const bool ready = s_ready != 0;
     const BatchPass& bc = passes[dc];
     const bool pipe = bc.pipe != 0;
     bool prefetched = false;
@@ -301,24 +313,40 @@ __global__ void __launch_bounds__(kBatchThreads, 2)
     } else {
       batch_process_single<P>(bc, cur - bc.first, buf0);
     }
-    // publish: the barrier orders every thread's stores before thread 0's
-    // gpu-scope fence and counter increment (the grid-barrier pattern)
+    // the barrier orders every thread's stores before warp 1's gpu-scope
+    // fence and counter increment (the grid-barrier pattern)
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 32) {
       __threadfence();
       atomicAdd(&ctl[2 + dc], 1);
     }
+    if (threadIdx.x == 0) {
+      int d2 = -1, r2 = 0;
+      const int it2 = ahead;
+      if (dn >= 0) {
+        ahead = atomicAdd(&ctl[0], 1);
+        lookup(it2, d2, r2);
+      }
+      s_item = it2;
+      s_pass = d2;
+      s_ready = r2;
+    }
+    __syncthreads();
+    const bool cur_ready = ready;
     cur = nxt;
     dc = dn;
     b ^= 1;
+    nxt = s_item;
+    dn = s_pass;
+    ready = s_ready != 0;
     if (dc >= 0 && !prefetched) {
-      if (!ready) {
+      if (!cur_ready) {
         if (threadIdx.x == 0) {
           const int dep = passes[dc].dep;
-          s_ready = wait_count(&ctl[2 + dep], passes[dep].tiles, &ctl[1]) ? 1 : 0;
+          s_ok = wait_count(&ctl[2 + dep], passes[dep].tiles, err) ? 1 : 0;
         }
         __syncthreads();
-        if (!s_ready) dc = -1;
+        if (!s_ok) dc = -1;
       }
       if (dc >= 0 && passes[dc].pipe) batch_issue<P>(passes[dc], cur - passes[dc].first, buf0 + b * buf_elems);
       cp_async_commit();
