@@ -72,7 +72,7 @@ __host__ __device__ constexpr int batch_pipe_elems() { return F64 ? 8 : 16; }
 // Double-buffered path: halve the tile width until the tile fits E points per
 // thread (c2r: the Hermitian merge holds E/2 + 2 items per thread); returns
 // the buffer size in elements (0 when it cannot fit).
-size_t pipe_fit_x(XParams& x, bool c2r, int E) {
+size_t pipe_fit_x(XParams& x, bool c2r, int E, int esize) {
   const int nh = x.nx / 2 + 1;
   auto fits = [&](int M) {
     return (long long)M * x.nx <= (long long)E * kBatchThreads &&
@@ -84,7 +84,8 @@ size_t pipe_fit_x(XParams& x, bool c2r, int E) {
   }
   if (!fits(x.M)) return 0;
   x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
-  return (size_t)x.M * (x.LS > 2 * nh ? x.LS : 2 * nh);
+  const int raw = 2 * xc2r_raw_stride(nh, esize);
+  return (size_t)x.M * (x.LS > raw ? x.LS : raw);
 }
 size_t pipe_fit_s(SParams& s, int E) {
   while (s.M > 1 && (long long)s.M * s.N > (long long)E * kBatchThreads) {
@@ -517,7 +518,7 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
       size_t pe = 0;
       if (!ap.sp.has_generic && ap.sp.nstages > 0 && x.nx >= 2) {
         XParams t = x;
-        pe = pipe_fit_x(t, kind == kBXc2r, pipe_e);
+        pe = pipe_fit_x(t, kind == kBXc2r, pipe_e, (int)es);
         if (pe) q.x = t;
       }
       if (pe) {

@@ -77,6 +77,11 @@ P3G_D void store_elem(void* base, int user, long long idx, typename P::C v) {
   else static_cast<typename P::W*>(base)[idx] = P::to_w(v);
 }
 
+// Stride of the raw line pairs of the pipelined X c2r tile: nh = N/2+1
+// complexes per line, rounded up to even for 8-byte elements so that two
+// complexes move with one 16-byte copy.
+P3G_HD int xc2r_raw_stride(int nh, int esize) { return esize == 8 ? (nh + 1) & ~1 : nh; }
+
 // Launchers (one per path).  Return the cudaError_t of the launch.
 template <class P>
 cudaError_t launch_x_r2c(const XParams& p, const StagePlan* sp, const float4* tw, int threads, size_t smem,

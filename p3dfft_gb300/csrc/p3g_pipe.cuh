@@ -492,6 +492,32 @@ P3G_D void xc2r_copy(const XParams& x, typename P::W* dst, int p0, int field) {
   using W = typename P::W;
   const int M = x.M, nh = x.nx / 2 + 1;
   const W* in = static_cast<const W*>(x.in) + field * x.in_field;
+  if constexpr (sizeof(W) == 8) {
+    // two complexes per 16-byte copy: raw stride rs even, line pitch even
+    const int rs = xc2r_raw_stride(nh, 8), hp = rs >> 1;
+    if ((x.in_line & 1) == 0 && (reinterpret_cast<uintptr_t>(in) & 15) == 0) {
+      const FastDiv fhp((uint32_t)hp);
+      for (int e = threadIdx.x; e < 2 * M * hp; e += blockDim.x) {
+        const int lt = (int)fhp.div((uint32_t)e);
+        const int k = 2 * (e - lt * hp);
+        const int line = 2 * p0 + lt;
+        const int nv = line < x.nlines ? min(max(x.nkeep - k, 0), 2) : 0;  // valid elements of the pair
+        const W* g = nv ? in + (long long)line * x.in_line + k : in;
+        cp_async16(dst + lt * rs + k, g, (uint32_t)(8 * nv));
+      }
+      return;
+    }
+    const FastDiv fnh((uint32_t)nh);
+    for (int e = threadIdx.x; e < 2 * M * nh; e += blockDim.x) {
+      const int lt = (int)fnh.div((uint32_t)e);
+      const int k = e - lt * nh;
+      const int line = 2 * p0 + lt;
+      const bool ok = line < x.nlines && k < x.nkeep;
+      const W* g = ok ? in + (long long)line * x.in_line + k : in;
+      cp_async8(dst + lt * rs + k, g, ok ? 8u : 0u);
+    }
+    return;
+  }
   const FastDiv fnh((uint32_t)nh);
   for (int e = threadIdx.x; e < 2 * M * nh; e += blockDim.x) {
     const int lt = (int)fnh.div((uint32_t)e);
@@ -518,7 +544,8 @@ P3G_D void xc2r_issue(const XPipeParams& q, int tile, int b) {
 template <class P, int MAXI>
 P3G_D void xc2r_merge(const XParams& x, typename P::W* sm) {
   using C = typename P::C;
-  const int N = x.nx, nh = N / 2 + 1, NP = 2 * nh, Mnh = x.M * nh;
+  const int N = x.nx, nh = N / 2 + 1, rs = xc2r_raw_stride(nh, (int)sizeof(typename P::W)), NP = 2 * rs,
+            Mnh = x.M * nh;
   const FastDiv fnh((uint32_t)nh);
   C z0[MAXI], z1[MAXI];
   int ip[MAXI], ik[MAXI];
@@ -536,7 +563,7 @@ P3G_D void xc2r_merge(const XParams& x, typename P::W* sm) {
       const int pr = (int)fnh.div((uint32_t)e);
       const int k = e - pr * nh;
       C x1 = P::from_w(sm[pr * NP + k]);
-      C x2 = P::from_w(sm[pr * NP + nh + k]);
+      C x2 = P::from_w(sm[pr * NP + rs + k]);
       if (k == 0 || 2 * k == N) {
         x1 = P::make(P::re(x1), P::re(P::zero()));
         x2 = P::make(P::re(x2), P::re(P::zero()));
@@ -548,7 +575,7 @@ P3G_D void xc2r_merge(const XParams& x, typename P::W* sm) {
     }
   }
   __syncthreads();
-  const int LS = x.LS, ps = x.ps;  // Z layout (padded), raw lines used NP = 2 nh
+  const int LS = x.LS, ps = x.ps;  // Z layout (padded), raw lines used NP = 2 rs
 #pragma unroll
   for (int i = 0; i < MAXI; ++i) {
     if (ip[i] >= 0) {

@@ -217,7 +217,8 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   };
   auto smem_for = [&](int M, size_t& buf_bytes) {
     // buffer stride rounded to 1 KB so both buffers (TMA destinations) stay aligned
-    const size_t need = (size_t)(kind == 0 ? M * n : M * (ap.ls > 2 * nh ? ap.ls : 2 * nh)) * esize;
+    const int raw = 2 * xc2r_raw_stride(nh, (int)esize);  // c2r raw line pair
+    const size_t need = (size_t)(kind == 0 ? M * n : M * (ap.ls > raw ? ap.ls : raw)) * esize;
     buf_bytes = (need + 1023) / 1024 * 1024;
     return 1024 + 2 * buf_bytes + (tw_shared ? (size_t)ap.tw_cnt * 16 : 0) + 16;
   };
