@@ -411,7 +411,7 @@ def run_batched(torch, pg, dev, steps, warmup, plain_f64_gpts):
     return out
 
 
-def run_serving(torch, pg, n_requests, plain_f64_gpts):
+def run_serving(torch, pg, n_requests, plain_f64_gpts, slots=3):
     """Serving form: requests (forward : backward : spectrum = 4:4:2, cubic or
     box grids with sides log-uniform over the 2^a 3^b 5^c values in [32,512],
     10 % asking for FP64 accuracy) through the continuous-batching server with
@@ -421,7 +421,7 @@ def run_serving(torch, pg, n_requests, plain_f64_gpts):
     from p3dfft_gb300 import serve
     cap_reqs = serve.make_requests(min(600, n_requests), seed=50)
     reqs = serve.poisson_arrivals(serve.make_requests(n_requests, seed=5), rate=1.0)  # rate set below
-    srv = serve.Server(budget_bytes=150e9, slots=3, max_jobs=64, window=4, keep_outputs=False)
+    srv = serve.Server(budget_bytes=150e9, slots=slots, max_jobs=64, window=4, keep_outputs=False)
     t = time.time()
     for r in cap_reqs + reqs:  # plans (tables) resident before the clock starts
         srv.plan(r.shape, pg.F64 if r.tol < serve.F32_TOL else pg.F32)
