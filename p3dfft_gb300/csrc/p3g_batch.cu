@@ -184,14 +184,14 @@ P3G_D void batch_process_pipe(const BatchPass& bp, int tile, typename P::W* buf)
     case kBXr2c: {
       xr2c_pack<P, E>(bp.x, buf);
       Tile<P> t{buf, nullptr, bp.x.M, bp.x.log2m, bp.x.LS, 1, bp.x.ps};
-      cta_fft<P, -1, E>(t, bp.sp, bp.tw);
+      cta_fft<P, -1, E, kLineMajor>(t, bp.sp, bp.tw);
       xr2c_store<P>(bp.x, buf, tile * bp.x.M, 0);
       break;
     }
     case kBXc2r: {
       xc2r_merge<P, E / 2 + 2>(bp.x, buf);
       Tile<P> t{buf, nullptr, bp.x.M, bp.x.log2m, bp.x.LS, 1, bp.x.ps};
-      cta_fft<P, 1, E>(t, bp.sp, bp.tw);
+      cta_fft<P, 1, E, kLineMajor>(t, bp.sp, bp.tw);
       xc2r_store<P>(bp.x, buf, tile * bp.x.M, 0);
       break;
     }
@@ -199,8 +199,8 @@ P3G_D void batch_process_pipe(const BatchPass& bp, int tile, typename P::W* buf)
       const int o1 = tile / bp.s.xtiles;
       strided_fix<P>(bp.s, false, buf);
       Tile<P> t{buf, nullptr, bp.s.M, bp.s.log2m, 1, bp.s.M};
-      if (bp.kind == kBFwd) cta_fft<P, -1, E>(t, bp.sp, bp.tw);
-      else cta_fft<P, 1, E>(t, bp.sp, bp.tw);
+      if (bp.kind == kBFwd) cta_fft<P, -1, E, kPointMajor>(t, bp.sp, bp.tw);
+      else cta_fft<P, 1, E, kPointMajor>(t, bp.sp, bp.tw);
       strided_store<P>(bp.s, buf, tile - o1 * bp.s.xtiles, o1, 0);
       break;
     }

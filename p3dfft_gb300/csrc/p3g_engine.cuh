@@ -93,7 +93,7 @@ template <class P>
 struct Tile {
   typename P::W* sm;       // M lines x N points
   typename P::W* scratch;  // same size, generic stages only
-  int M, log2m, LS, JS;
+  int M, log2m, LS, JS;    // point-major tiles (LS = 1) always have JS = M
   int ps = 0;              // line-major padding shift (0: none)
   P3G_D int addr(int line, int j) const { return line * LS + (LS == 1 ? j * JS : pad_index(j, ps)); }
   P3G_D uint32_t saddr(int line, int j) const {
@@ -130,51 +130,80 @@ P3G_D void cta_barrier() {
   asm volatile("bar.sync %0;" ::"n"(ID) : "memory");
 }
 
-template <class P, int DIR, int R, int E = kElemsPerThread>
+// Tile layouts a kernel can fix at compile time: the strided passes use
+// point-major tiles (LS = 1, JS = M), the X passes line-major ones (LS =
+// padded N, JS = 1); kAnyLayout reads the layout from the tile.
+enum { kAnyLayout = -1, kLineMajor = 0, kPointMajor = 1 };
+
+// One stage of radix R.  FULL: every thread owns exactly MAXB butterflies
+// (M N / R == MAXB x blockDim.x, the usual case), so no butterfly needs a
+// guard or a placeholder value.  With a known layout the butterfly -> point
+// mapping needs no runtime layout test: point-major, butterfly b reads
+// element b (line b mod M, position b / M); line-major, b / (N / R) is the
+// line.  In the power-of-two families ns is a power of two (they run first),
+// so the twiddle index is a mask.
+template <class P, int DIR, int R, int E, int LAY, bool FULL>
 __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const float4* __restrict__ tw) {
   using C = typename P::C;
   using W = typename P::W;
   constexpr int MAXB = (E + R - 1) / R;
+  constexpr bool kPow2 = (R & (R - 1)) == 0;
+  constexpr uint32_t kW = (uint32_t)sizeof(W);
   const int per_line = N / R;
-  const FastDiv fd_line((uint32_t)per_line), fd_ns((uint32_t)ns);
-  const int nb = t.M * per_line;
   const int T = blockDim.x;
+  const bool pm = LAY == kPointMajor || (LAY == kAnyLayout && t.LS == 1);
+  const FastDiv fd_line((uint32_t)(pm ? 1 : per_line)), fd_ns((uint32_t)(kPow2 ? 1 : ns));
+  const int nb = t.M * per_line;
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(t.sm);
-  const int ps = t.LS == 1 ? 0 : t.ps;
+  const int ps = pm ? 0 : t.ps;
   // bytes between inputs q, q+1 and between outputs q, q+1
-  const uint32_t jstride = (uint32_t)(t.JS * (int)sizeof(W)) * (uint32_t)pad_index(per_line, ps);
-  const uint32_t ostride = (uint32_t)(t.JS * (int)sizeof(W)) * (uint32_t)pad_index(ns, ps);
-  // Explicitly initialised: the arrays are written and read under correlated
-  // guards (b < nb) the compiler cannot prove, and inside a persistent tile
-  // loop an uninitialised element would otherwise be kept live around the
-  // loop, with every codelet's registers.
+  const uint32_t jstride = pm ? ((uint32_t)per_line << t.log2m) * kW
+                              : (uint32_t)(t.JS * (int)kW) * (uint32_t)pad_index(per_line, ps);
+  const uint32_t ostride = pm ? ((uint32_t)ns << t.log2m) * kW : (uint32_t)(t.JS * (int)kW) * (uint32_t)pad_index(ns, ps);
+  // Non-full stages: explicitly initialised, because the arrays are written
+  // and read under correlated guards (b < nb) the compiler cannot prove, and
+  // inside a persistent tile loop an uninitialised element would otherwise be
+  // kept live around the loop, with every codelet's registers.
   C v[MAXB][R];
   uint32_t oaddr[MAXB];
   bool live[MAXB];
+  if constexpr (!FULL) {
 #pragma unroll
-  for (int i = 0; i < MAXB; ++i) {
-    oaddr[i] = 0;
+    for (int i = 0; i < MAXB; ++i) {
+      oaddr[i] = 0;
 #pragma unroll
-    for (int q = 0; q < R; ++q) v[i][q] = P::zero();
+      for (int q = 0; q < R; ++q) v[i][q] = P::zero();
+    }
   }
 #pragma unroll
   for (int i = 0; i < MAXB; ++i) {
     const int b = threadIdx.x + i * T;
-    live[i] = b < nb;
+    live[i] = FULL || b < nb;
     if (live[i]) {
       int line, j;
-      t.decode(b, fd_line, line, j);
-      const uint32_t ia = sbase + (uint32_t)(t.addr(line, j) * (int)sizeof(W));
+      uint32_t ia;
+      if (pm) {
+        line = b & (t.M - 1);
+        j = b >> t.log2m;
+        ia = sbase + (uint32_t)b * kW;
+      } else {
+        uint32_t q, r;
+        fd_line.divmod((uint32_t)b, q, r);
+        line = (int)q;
+        j = (int)r;
+        ia = sbase + (uint32_t)(t.addr(line, j) * (int)kW);
+      }
 #pragma unroll
       for (int q = 0; q < R; ++q) v[i][q] = P::from_w(lds(ia + q * jstride, (W*)nullptr));
-      const int k = (int)(j - fd_ns.div((uint32_t)j) * (uint32_t)ns);
+      const int k = kPow2 ? (j & (ns - 1)) : (int)(j - fd_ns.div((uint32_t)j) * (uint32_t)ns);
       if (ns > 1) {
         const float4* twp = tw + k * (R - 1) - 1;
 #pragma unroll
         for (int q = 1; q < R; ++q) v[i][q] = cmul<(DIR > 0)>(v[i][q], load_tw(twp, q));
       }
       dft<R, DIR>(v[i]);
-      oaddr[i] = sbase + (uint32_t)(t.addr(line, (j - k) * R + k) * (int)sizeof(W));
+      const int jo = (j - k) * R + k;
+      oaddr[i] = sbase + (pm ? (uint32_t)(line + (jo << t.log2m)) * kW : (uint32_t)(t.addr(line, jo) * (int)kW));
     }
   }
   cta_barrier<(R == 16 ? 1 : R)>();
@@ -230,12 +259,15 @@ __device__ __noinline__ void stage_generic(const Tile<P>& t, int N, int p, int n
 // length ns(s) = product of the radices before it; both follow from the
 // family counts, so they are carried in registers instead of being loaded
 // per stage (stage 0 owns one placeholder twiddle, see build_stages).
-template <class P, int DIR, int R, int E>
+template <class P, int DIR, int R, int E, int LAY>
 __device__ __forceinline__ void run_family(const Tile<P>& t, const float4* __restrict__ tw, int N, int cnt, int& ns,
                                            int& off) {
+  constexpr int MAXB = (E + R - 1) / R;
+  const bool full = t.M * (N / R) == MAXB * (int)blockDim.x;
 #pragma unroll 1
   for (int c = 0; c < cnt; ++c) {
-    stage_reg<P, DIR, R, E>(t, N, ns, tw + off);
+    if (full) stage_reg<P, DIR, R, E, LAY, true>(t, N, ns, tw + off);
+    else stage_reg<P, DIR, R, E, LAY, false>(t, N, ns, tw + off);
     off += ns > 1 ? ns * (R - 1) : 1;
     ns *= R;
   }
@@ -250,8 +282,9 @@ __device__ __forceinline__ void run_family(const Tile<P>& t, const float4* __res
 // double-float operation count per point for the sizes used here).
 // tw points at the twiddle table entry tw_base (the full table with
 // tw_base = 0, or a pass's slice copied to shared memory).  E = elements each
-// thread holds per stage; the launch uses ceil(M N / E) threads.
-template <class P, int DIR, int E = kElemsPerThread>
+// thread holds per stage; the launch uses ceil(M N / E) threads.  LAY: the
+// tile layout when the caller knows it (kPointMajor, kLineMajor).
+template <class P, int DIR, int E = kElemsPerThread, int LAY = kAnyLayout>
 __device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __restrict__ sp,
                                         const float4* __restrict__ tw, int tw_base = 0) {
   const int N = __ldg(&sp->n);
@@ -261,12 +294,12 @@ __device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __res
   const int nst = __ldg(&sp->nstages);
   int ns = 1;
   int off = __ldg(&sp->tw_off[0]) - tw_base;
-  if constexpr (!P::kF64) run_family<P, DIR, 16, E>(t, tw, N, c[0], ns, off);
-  run_family<P, DIR, 8, E>(t, tw, N, c[1], ns, off);
-  run_family<P, DIR, 4, E>(t, tw, N, c[2], ns, off);
-  run_family<P, DIR, 2, E>(t, tw, N, c[3], ns, off);
-  run_family<P, DIR, 3, E>(t, tw, N, c[4], ns, off);
-  run_family<P, DIR, 5, E>(t, tw, N, c[5], ns, off);
+  if constexpr (!P::kF64) run_family<P, DIR, 16, E, LAY>(t, tw, N, c[0], ns, off);
+  run_family<P, DIR, 8, E, LAY>(t, tw, N, c[1], ns, off);
+  run_family<P, DIR, 4, E, LAY>(t, tw, N, c[2], ns, off);
+  run_family<P, DIR, 2, E, LAY>(t, tw, N, c[3], ns, off);
+  run_family<P, DIR, 3, E, LAY>(t, tw, N, c[4], ns, off);
+  run_family<P, DIR, 5, E, LAY>(t, tw, N, c[5], ns, off);
   const int sg = c[0] + c[1] + c[2] + c[3] + c[4] + c[5];
 #pragma unroll 1
   for (int s = sg; s < nst; ++s)

@@ -54,7 +54,7 @@ P3G_D void x_r2c_tile(const XParams& prm, const StagePlan* __restrict__ sp, cons
   }
   __syncthreads();
   Tile<P> t{sm, sm + M * LS, M, prm.log2m, LS, 1, ps};
-  cta_fft<P, -1>(t, sp, tw);
+  cta_fft<P, -1, kElemsPerThread, kLineMajor>(t, sp, tw);
   const int nk = prm.nkeep;
   for (int e = threadIdx.x; e < M * nk; e += blockDim.x) {
     const int pr = e / nk;
@@ -108,7 +108,7 @@ P3G_D void x_c2r_tile(const XParams& prm, const StagePlan* __restrict__ sp, cons
   }
   __syncthreads();
   Tile<P> t{sm, sm + M * LS, M, prm.log2m, LS, 1, ps};
-  cta_fft<P, 1>(t, sp, tw);
+  cta_fft<P, 1, kElemsPerThread, kLineMajor>(t, sp, tw);
   const float* smf = reinterpret_cast<const float*>(sm);
   constexpr int kW = sizeof(W) / sizeof(float);
   for (int e = threadIdx.x; e < 2 * M * N; e += blockDim.x) {
@@ -184,7 +184,7 @@ P3G_D void strided_tile(const SParams& prm, const StagePlan* __restrict__ sp, co
   }
   __syncthreads();
   Tile<P> t{sm, sm + M * N, M, prm.log2m, 1, M};
-  cta_fft<P, DIR>(t, sp, tw);
+  cta_fft<P, DIR, kElemsPerThread, kPointMajor>(t, sp, tw);
   const bool out_rows_fast = prm.out_xs != 1;
   const FastDiv div_lo(prm.Lout);
   for (int e = threadIdx.x; e < M * prm.Lout; e += blockDim.x) {

@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       const SPipeParams& q = pp;
       const StridedSmem<P> sm = strided_smem<P>(q.c);
       Tile<P> t{sm.buf0 + b * q.c.buf_elems, nullptr, q.s.M, q.s.log2m, 1, q.s.M};
-      cta_fft<P, DIR, PipeLimits<P>::kE>(t, sp, sm.tw, q.c.tw_base);
+      cta_fft<P, DIR, PipeLimits<P>::kE, kPointMajor>(t, sp, sm.tw, q.c.tw_base);
     }
     {
       int xt, o1, o2;
@@ -473,7 +473,7 @@ __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::k
     xr2c_pack<P, XPipeLimits<P>::kE>(pp.x, xpipe_buf<P>(pp.c, b));
     {
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
-      cta_fft<P, -1, XPipeLimits<P>::kE>(t, sp, tw_g, 0);
+      cta_fft<P, -1, XPipeLimits<P>::kE, kLineMajor>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;
@@ -652,7 +652,7 @@ __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::k
     xc2r_merge<P, XPipeLimits<P>::kE / 2 + 2>(pp.x, xpipe_buf<P>(pp.c, b));  // host: T * MAXI >= M nh
     {
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
-      cta_fft<P, 1, XPipeLimits<P>::kE>(t, sp, tw_g, 0);
+      cta_fft<P, 1, XPipeLimits<P>::kE, kLineMajor>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;
