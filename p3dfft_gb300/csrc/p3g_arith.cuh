@@ -133,7 +133,13 @@ P3G_HD void two_sum(float a, float b, float& s, float& e) {
 // dropped (relative error <= 2^-23), below 2^-126 the value flushes to a signed
 // zero, at or above 2^128 hi is +-inf: the F64 path has binary32's exponent
 // range, and its error bound is relative to the largest magnitude of a field.
-P3G_HD df d2df(double x) {
+//
+// d2df_edge handles every exponent; d2df takes a shorter route for binary64
+// exponents 949..1150 (2^-74 <= |x| < 2^128, the values FFT data has) and
+// gives the same bits: hi is the high word rebiased and funnel-shifted by 3,
+// lo = rem * 2^(e-1075) with the sign in the scale and +0 added, so that
+// rem == 0 gives +0 as the edge route does.
+P3G_HD df d2df_edge(double x) {
   const uint64_t b = d2u(x);
   const uint32_t hw = (uint32_t)(b >> 32), lw = (uint32_t)b;
   const uint32_t sign = hw & 0x80000000u;
@@ -163,6 +169,30 @@ P3G_HD df d2df(double x) {
   return r;
 }
 
+// (hi:lo) << 3, upper word
+P3G_HD uint32_t shl3_funnel(uint32_t lo, uint32_t hi) {
+#if defined(__CUDA_ARCH__)
+  return __funnelshift_l(lo, hi, 3);
+#else
+  return (hi << 3) | (lo >> 29);
+#endif
+}
+
+P3G_HD df d2df(double x) {
+  const uint64_t b = d2u(x);
+  const uint32_t hw = (uint32_t)(b >> 32), lw = (uint32_t)b;
+  const uint32_t a = hw & 0x7FFFFFFFu;
+  if (a - (949u << 20) >= (202u << 20)) return d2df_edge(x);  // e < 949 or e > 1150
+  const uint32_t hb = shl3_funnel(lw, a - (896u << 20)) | (hw & 0x80000000u);
+  // 2^(e-1075) = 2^(e_hi - 179) with the sign of x; e_hi >= 53, so the
+  // subtraction stays inside the exponent field
+  const uint32_t scale = (hb & 0xFF800000u) - (52u << 23);
+  df r;
+  r.hi = u2f(hb);
+  r.lo = ffma(u32_to_f32_rn(lw & 0x1FFFFFFFu), u2f(scale), 0.0f);
+  return r;
+}
+
 // Nearest integer of a binary32 value below 2^30.
 P3G_HD int32_t f32_to_i32_rn(float v) {
 #if defined(__CUDA_ARCH__)
@@ -181,9 +211,12 @@ P3G_HD int32_t f32_to_i32_rn(float v) {
 // No step crosses a binade otherwise: the widened s has at least 2^29 ulps of
 // mantissa above its binade and at least 2^29 below the next.  Subnormal
 // binary32 parts are flushed.
-P3G_HD double df2d(float hi, float lo) {
-  float s, t;
-  two_sum(hi, lo, s, t);
+//
+// df2d_st converts any canonical pair (s, t); df2d takes a shorter route when
+// s's binary32 exponent is 52..254 and s is not a power of two (so no binade
+// change can happen): t, its sign taken relative to s, becomes a signed k that
+// is added to the 64-bit pattern, with the same result as df2d_st.
+P3G_HD double df2d_st(float s, float t) {
   const uint32_t sb = f2u(s);
   const uint32_t sign = sb & 0x80000000u;
   const int es = (int)((sb >> 23) & 0xFFu);
@@ -199,6 +232,21 @@ P3G_HD double df2d(float hi, float lo) {
   if ((tb & 0x7FFFFFFFu) == 0u || scale_e > 254) return u2d(d);
   const int64_t k = f32_to_i32_rn(u2f(tb & 0x7FFFFFFFu) * u2f((uint32_t)scale_e << 23));
   return u2d(down ? d - (uint64_t)k : d + (uint64_t)k);
+}
+
+P3G_HD double df2d(float hi, float lo) {
+  float s, t;
+  two_sum(hi, lo, s, t);
+  const uint32_t sb = f2u(s);
+  const uint32_t ex = sb & 0x7F800000u;
+  if (ex - (52u << 23) >= (203u << 23) || (sb & 0x7FFFFFu) == 0u) return df2d_st(s, t);
+  // widened s: sign | (es + 896) << 20 | ms >> 3 : (ms & 7) << 29
+  const uint32_t dh = (((sb >> 3) & 0x0FFFFFFFu) | (sb & 0x80000000u)) + (896u << 20);
+  const uint32_t dl = sb << 29;
+  // k = t / ulp64(s) rounded, positive when t raises |s|
+  const int32_t k = f32_to_i32_rn(u2f(f2u(t) ^ (sb & 0x80000000u)) * u2f((306u << 23) - ex));
+  const uint64_t d = ((uint64_t)dh << 32) | dl;
+  return u2d(d + (uint64_t)(int64_t)k);
 }
 
 // ------------------------------------------------------- double-float ops
