@@ -149,8 +149,9 @@ int p3g_batch_capture(p3g_batch batch);
 int p3g_batch_replay(p3g_batch batch, void* stream);
 /* Synchronises the stream and reports a timed-out dependency wait. */
 int p3g_batch_status(p3g_batch batch, void* stream);
-/* info = {passes, work items, persistent CTAs, launches so far} */
-int p3g_batch_info(p3g_batch batch, long long info[4]);
+/* info = {passes, work items, persistent CTAs, launches so far, threads per
+ * CTA (128, or 256 when a line is longer than 2048 points)} */
+int p3g_batch_info(p3g_batch batch, long long info[5]);
 /* Test hook for the bounded dependency waits: makes the passes that depend
  * on pass `pass` (queue order, as numbered by set_jobs) wait for a tile that
  * never completes, so their waits run out (about 4 s) and the next

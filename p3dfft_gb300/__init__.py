@@ -280,9 +280,9 @@ class Batch:
         _check(_core().p3g_batch_block_pass(self._h, int(index)))
 
     def info(self):
-        a = (ctypes.c_longlong * 4)()
+        a = (ctypes.c_longlong * 5)()
         _check(_core().p3g_batch_info(self._h, a))
-        return {"passes": a[0], "items": a[1], "ctas": a[2], "launches": a[3]}
+        return {"passes": a[0], "items": a[1], "ctas": a[2], "launches": a[3], "threads": a[4]}
 
     def close(self):
         if self._h:

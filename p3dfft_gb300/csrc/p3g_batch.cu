@@ -58,11 +58,15 @@ struct BatchPass {
 
 constexpr int kBatchSpinLimit = 1 << 22;  // polls of ~1 us: about 4 s
 
-// 256 threads and two CTAs per SM on both paths (128 registers per thread):
-// while one CTA waits on its loads the other computes.  Tiles hold at most
-// kElemsPerThread x 256 = 4096 points.
-constexpr int kBatchThreads = 256;
-constexpr int kBatchTile = kElemsPerThread * kBatchThreads;
+// 128 threads and four CTAs per SM on both paths (128 registers per thread):
+// while one CTA waits on its loads or at a barrier the others compute (12 %
+// faster than two 256-thread CTAs on uneven grids of sides 48..256).  Tiles
+// then hold at most kElemsPerThread x 128 = 2048 points; a batch with a
+// longer line runs 256-thread CTAs (two per SM, 4096-point tiles).
+constexpr int kBatchThreadsSmall = 128;
+constexpr int kBatchThreadsLarge = 256;
+template <int T>
+__host__ __device__ constexpr int batch_min_blocks() { return 65536 / 128 / T; }
 
 // Points per thread of the double-buffered path (as the pipelined pass
 // kernels): 8 on F64, 16 on F32.
@@ -72,11 +76,11 @@ __host__ __device__ constexpr int batch_pipe_elems() { return F64 ? 8 : 16; }
 // Double-buffered path: halve the tile width until the tile fits E points per
 // thread (c2r: the Hermitian merge holds E/2 + 2 items per thread); returns
 // the buffer size in elements (0 when it cannot fit).
-size_t pipe_fit_x(XParams& x, bool c2r, int E, int esize) {
+size_t pipe_fit_x(XParams& x, bool c2r, int E, int esize, int threads) {
   const int nh = x.nx / 2 + 1;
   auto fits = [&](int M) {
-    return (long long)M * x.nx <= (long long)E * kBatchThreads &&
-           (!c2r || (long long)M * nh <= (long long)(E / 2 + 2) * kBatchThreads);
+    return (long long)M * x.nx <= (long long)E * threads &&
+           (!c2r || (long long)M * nh <= (long long)(E / 2 + 2) * threads);
   };
   while (x.M > 1 && !fits(x.M)) {
     x.M >>= 1;
@@ -87,33 +91,35 @@ size_t pipe_fit_x(XParams& x, bool c2r, int E, int esize) {
   const int raw = 2 * xc2r_raw_stride(nh, esize);
   return (size_t)x.M * (x.LS > raw ? x.LS : raw);
 }
-size_t pipe_fit_s(SParams& s, int E) {
-  while (s.M > 1 && (long long)s.M * s.N > (long long)E * kBatchThreads) {
+size_t pipe_fit_s(SParams& s, int E, int threads) {
+  while (s.M > 1 && (long long)s.M * s.N > (long long)E * threads) {
     s.M >>= 1;
     s.log2m--;
   }
-  if ((long long)s.M * s.N > (long long)E * kBatchThreads) return 0;
+  if ((long long)s.M * s.N > (long long)E * threads) return 0;
   s.xtiles = (s.X + s.M - 1) / s.M;
   return (size_t)s.M * s.N;
 }
 
 // Halve the plan's tile width until one tile fits the batch CTA; returns the
 // tile's shared-memory bytes (0 when even one line is too long).
-size_t fit_x(XParams& x, const AxisPlan& ap, size_t esize) {
-  while (x.M > 1 && (long long)x.M * x.nx > kBatchTile) {
+size_t fit_x(XParams& x, const AxisPlan& ap, size_t esize, int threads) {
+  const long long tile = (long long)kElemsPerThread * threads;
+  while (x.M > 1 && (long long)x.M * x.nx > tile) {
     x.M >>= 1;
     x.log2m--;
   }
-  if ((long long)x.M * x.nx > kBatchTile) return 0;
+  if ((long long)x.M * x.nx > tile) return 0;
   x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
   return (size_t)x.M * x.LS * esize * (ap.sp.has_generic ? 2 : 1);
 }
-size_t fit_s(SParams& s, const AxisPlan& ap, size_t esize) {
-  while (s.M > 1 && (long long)s.M * s.N > kBatchTile) {
+size_t fit_s(SParams& s, const AxisPlan& ap, size_t esize, int threads) {
+  const long long tile = (long long)kElemsPerThread * threads;
+  while (s.M > 1 && (long long)s.M * s.N > tile) {
     s.M >>= 1;
     s.log2m--;
   }
-  if ((long long)s.M * s.N > kBatchTile) return 0;
+  if ((long long)s.M * s.N > tile) return 0;
   s.xtiles = (s.X + s.M - 1) / s.M;
   return (size_t)s.M * s.N * esize * (ap.sp.has_generic ? 2 : 1);
 }
@@ -247,8 +253,8 @@ __device__ __noinline__ void batch_process_single(const BatchPass& bp, int tile,
 // item and the start of the next, warp 1 publishes the finished item (fence +
 // counter) while thread 0 looks up the item after next, whose ticket was
 // fetched an item earlier: neither latency waits for the other.
-template <class P>
-__global__ void __launch_bounds__(kBatchThreads, 2)
+template <class P, int T>
+__global__ void __launch_bounds__(T, batch_min_blocks<T>())
     k_batch(const BatchPass* __restrict__ passes, int npass, int nitems, int* __restrict__ ctl, int buf_elems) {
   using W = typename P::W;
   __shared__ int s_first[kFirstCache];
@@ -357,37 +363,44 @@ __global__ void __launch_bounds__(kBatchThreads, 2)
 }
 
 // Opts the kernel in to the largest dynamic shared memory the device allows
-// next to its static shared variables (once per path), then reads the
-// occupancy for this batch's tile size.
-template <class P>
-cudaError_t batch_config(size_t smem, int& threads, int& per_sm, size_t& max_dyn) {
-  threads = kBatchThreads;
+// next to its static shared variables (once per path and CTA size), then
+// reads the occupancy for this batch's tile size.
+template <class P, int T>
+cudaError_t batch_config_t(size_t smem, int& per_sm, size_t& max_dyn) {
   static size_t s_max_dyn = 0;
   cudaError_t e = cudaSuccess;
   if (!s_max_dyn) {
     cudaFuncAttributes fa{};
     int dev = 0, optin = 0;
-    e = cudaFuncGetAttributes(&fa, k_batch<P>);
+    e = cudaFuncGetAttributes(&fa, k_batch<P, T>);
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) return e;
     const size_t dyn = (size_t)optin - fa.sharedSizeBytes;
-    e = cudaFuncSetAttribute(k_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    e = cudaFuncSetAttribute(k_batch<P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
     s_max_dyn = dyn;
   }
   max_dyn = s_max_dyn;
   if (smem > max_dyn) return cudaErrorInvalidValue;
   per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<P>, threads, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<P, T>, T, smem);
   if (e == cudaSuccess && per_sm < 1) per_sm = 1;
   return e;
+}
+template <class P>
+cudaError_t batch_config(size_t smem, int threads, int& per_sm, size_t& max_dyn) {
+  return threads == kBatchThreadsSmall ? batch_config_t<P, kBatchThreadsSmall>(smem, per_sm, max_dyn)
+                                       : batch_config_t<P, kBatchThreadsLarge>(smem, per_sm, max_dyn);
 }
 
 template <class P>
 cudaError_t batch_launch(const BatchPass* d_pass, int npass, int nitems, int* ctl, int buf_elems, int grid,
                          int threads, size_t smem, cudaStream_t st) {
-  k_batch<P><<<grid, threads, smem, st>>>(d_pass, npass, nitems, ctl, buf_elems);
+  if (threads == kBatchThreadsSmall)
+    k_batch<P, kBatchThreadsSmall><<<grid, threads, smem, st>>>(d_pass, npass, nitems, ctl, buf_elems);
+  else
+    k_batch<P, kBatchThreadsLarge><<<grid, threads, smem, st>>>(d_pass, npass, nitems, ctl, buf_elems);
   return cudaGetLastError();
 }
 
@@ -440,6 +453,136 @@ struct p3g_batch_s {
   }
 };
 
+// Every job's chain of passes for CTAs of `threads` threads: tile widths,
+// double-buffered or single-tile items, and the shared memory the items need
+// (smem bytes for single-tile and spectrum items, buf_elems per buffer of the
+// double-buffered ones).  fit = false when a line is longer than the tile.
+static int build_chains(p3g_batch b, int njobs, const p3g_job* jobs, int threads,
+                        std::vector<std::vector<BatchPass>>& chains, size_t& smem, size_t& buf_elems, bool& fit) {
+  const bool f64 = b->prec == P3G_F64;
+  const int pipe_e = f64 ? batch_pipe_elems<true>() : batch_pipe_elems<false>();
+  const int nwarps = threads / 32;
+  chains.assign(njobs, {});
+  smem = 0;
+  buf_elems = 0;
+  fit = true;
+  for (int j = 0; j < njobs; ++j) {
+    const p3g_job& jb = jobs[j];
+    p3g_plan p = jb.plan;
+    const std::string who = "job " + std::to_string(j) + ": ";
+    if (!p) return fail(P3G_E_ARG, who + "plan is NULL");
+    if (p->prec != b->prec) return fail(P3G_E_ARG, who + "plan precision differs from the batch's");
+    if (jb.kind < P3G_JOB_ROUNDTRIP || jb.kind > P3G_JOB_SPECTRUM) return fail(P3G_E_ARG, who + "unknown kind");
+    if (!jb.in || !jb.out || !jb.work) return fail(P3G_E_ARG, who + "NULL array");
+    if (!p->z_ok[0]) return fail(P3G_E_UNSUPPORTED, who + "Z FFT unsupported for nz");
+    const JobLayout L = job_layout(p, jb.kind);
+    unsigned char* w = static_cast<unsigned char*>(jb.work);
+    void* wa = w;
+    void* wb = L.wb ? w + L.wa : nullptr;
+    void* cplx = L.cplx ? w + L.wa + L.wb : nullptr;
+    const StagePlan* dsp = p->d_sp;
+    bool fits = true;
+    const size_t es = p->esize();
+    // double-buffered when the axis has no generic prime stage and its tile
+    // fits the pipelined CTA; else single-tile (scratch tile, no prefetch)
+    auto x_pass = [&](int kind, const XParams& x) {
+      BatchPass q{};
+      q.kind = kind;
+      q.x = x;
+      const AxisPlan& ap = p->ax_x;
+      size_t pe = 0;
+      if (!ap.sp.has_generic && ap.sp.nstages > 0 && x.nx >= 2) {
+        XParams t = x;
+        pe = pipe_fit_x(t, kind == kBXc2r, pipe_e, (int)es, threads);
+        if (pe) q.x = t;
+      }
+      if (pe) {
+        q.pipe = 1;
+        buf_elems = std::max(buf_elems, pe);
+        const size_t ur = f64 ? 8 : 4;
+        q.chunk = (int)ur;
+        const uintptr_t a = reinterpret_cast<uintptr_t>(x.in);
+        if ((x.nx * ur) % 16 == 0 && a % 16 == 0) q.chunk = 16;
+        else if ((x.nx * ur) % 8 == 0 && a % 8 == 0) q.chunk = 8;
+      } else {
+        const size_t need = fit_x(q.x, ap, es, threads);
+        fits = fits && need > 0;
+        smem = std::max(smem, need);
+      }
+      q.tiles = q.x.tiles;
+      q.sp = dsp + ap.sp_index;
+      q.tw = p->d_tw;
+      chains[j].push_back(q);
+    };
+    auto s_pass = [&](int kind, const SParams& s, const AxisPlan& ap) {
+      BatchPass q{};
+      q.kind = kind;
+      q.s = s;
+      size_t pe = 0;
+      if (!ap.sp.has_generic && ap.sp.nstages > 0 && s.N >= 2) {
+        SParams t = s;
+        pe = pipe_fit_s(t, pipe_e, threads);
+        if (pe) q.s = t;
+      }
+      if (pe) {
+        q.pipe = 1;
+        buf_elems = std::max(buf_elems, pe);
+      } else {
+        const size_t need = fit_s(q.s, ap, es, threads);
+        fits = fits && need > 0;
+        smem = std::max(smem, need);
+      }
+      q.tiles = q.s.xtiles * q.s.O1;
+      q.sp = dsp + ap.sp_index;
+      q.tw = p->d_tw;
+      chains[j].push_back(q);
+    };
+    const long long rsize = (long long)p->nx * p->ny * p->nz;
+    const long long csize = (long long)p->nxhpc * p->nyc * p->nzc;
+    if (jb.kind == P3G_JOB_SPECTRUM) {
+      SpecParams sp;
+      int rc = make_spectrum_params(p, cplx, static_cast<double*>(jb.out), jb.kmax, jb.scale, jb.flags, csize, sp);
+      if (rc) return rc;
+      BatchPass q{};
+      q.kind = kBZero;
+      q.spec = sp;
+      q.tiles = 1;
+      chains[j].push_back(q);
+    }
+    if (jb.kind != P3G_JOB_BACKWARD) {
+      XParams x;
+      SParams y, z;
+      void* fout = jb.kind == P3G_JOB_FORWARD ? jb.out : cplx;
+      make_forward_params(p, jb.in, fout, wa, wb, 0, rsize, csize, x, y, z);
+      x_pass(kBXr2c, x);
+      s_pass(kBFwd, y, p->ax_y);
+      s_pass(kBFwd, z, p->ax_z[0]);
+    }
+    if (jb.kind == P3G_JOB_ROUNDTRIP || jb.kind == P3G_JOB_BACKWARD) {
+      SParams z, y;
+      XParams x;
+      const void* bin = jb.kind == P3G_JOB_BACKWARD ? jb.in : cplx;
+      make_backward_params(p, bin, jb.out, wa, wb, 0, csize, rsize, z, y, x);
+      s_pass(kBBwd, z, p->ax_z[0]);
+      s_pass(kBBwd, y, p->ax_y);
+      x_pass(kBXc2r, x);
+    }
+    if (!fits) {
+      fit = false;
+      return P3G_OK;
+    }
+    if (jb.kind == P3G_JOB_SPECTRUM) {
+      BatchPass q = chains[j][0];
+      q.kind = kBSpec;
+      q.rows_per_item = nwarps * 4;
+      q.tiles = (q.spec.rows + q.rows_per_item - 1) / q.rows_per_item;
+      smem = std::max(smem, (size_t)nwarps * (q.spec.kmax + 1) * sizeof(double));
+      chains[j].push_back(q);
+    }
+  }
+  return P3G_OK;
+}
+
 extern "C" {
 
 long long p3g_job_work_bytes(p3g_plan plan, int kind) {
@@ -484,123 +627,20 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
   if (window <= 0) window = njobs;
   std::lock_guard<std::mutex> lk(b->mu);
   const bool f64 = b->prec == P3G_F64;
-  const int threads = kBatchThreads;
-  const int nwarps = threads / 32;
-  // per job: its chain of passes
-  std::vector<std::vector<BatchPass>> chains(njobs);
+  // per job: its chain of passes; 128-thread CTAs unless a line needs the
+  // 256-thread tile
+  std::vector<std::vector<BatchPass>> chains;
   size_t smem = 0;        // single-tile and spectrum items (bytes)
   size_t buf_elems = 0;   // one buffer of the double-buffered items (elements)
-  const int pipe_e = f64 ? batch_pipe_elems<true>() : batch_pipe_elems<false>();
-  for (int j = 0; j < njobs; ++j) {
-    const p3g_job& jb = jobs[j];
-    p3g_plan p = jb.plan;
-    const std::string who = "job " + std::to_string(j) + ": ";
-    if (!p) return fail(P3G_E_ARG, who + "plan is NULL");
-    if (p->prec != b->prec) return fail(P3G_E_ARG, who + "plan precision differs from the batch's");
-    if (jb.kind < P3G_JOB_ROUNDTRIP || jb.kind > P3G_JOB_SPECTRUM) return fail(P3G_E_ARG, who + "unknown kind");
-    if (!jb.in || !jb.out || !jb.work) return fail(P3G_E_ARG, who + "NULL array");
-    if (!p->z_ok[0]) return fail(P3G_E_UNSUPPORTED, who + "Z FFT unsupported for nz");
-    const JobLayout L = job_layout(p, jb.kind);
-    unsigned char* w = static_cast<unsigned char*>(jb.work);
-    void* wa = w;
-    void* wb = L.wb ? w + L.wa : nullptr;
-    void* cplx = L.cplx ? w + L.wa + L.wb : nullptr;
-    const StagePlan* dsp = p->d_sp;
-    bool fits = true;
-    const size_t es = p->esize();
-    // double-buffered when the axis has no generic prime stage and its tile
-    // fits the pipelined CTA; else single-tile (scratch tile, no prefetch)
-    auto x_pass = [&](int kind, const XParams& x) {
-      BatchPass q{};
-      q.kind = kind;
-      q.x = x;
-      const AxisPlan& ap = p->ax_x;
-      size_t pe = 0;
-      if (!ap.sp.has_generic && ap.sp.nstages > 0 && x.nx >= 2) {
-        XParams t = x;
-        pe = pipe_fit_x(t, kind == kBXc2r, pipe_e, (int)es);
-        if (pe) q.x = t;
-      }
-      if (pe) {
-        q.pipe = 1;
-        buf_elems = std::max(buf_elems, pe);
-        const size_t ur = f64 ? 8 : 4;
-        q.chunk = (int)ur;
-        const uintptr_t a = reinterpret_cast<uintptr_t>(x.in);
-        if ((x.nx * ur) % 16 == 0 && a % 16 == 0) q.chunk = 16;
-        else if ((x.nx * ur) % 8 == 0 && a % 8 == 0) q.chunk = 8;
-      } else {
-        const size_t need = fit_x(q.x, ap, es);
-        fits = fits && need > 0;
-        smem = std::max(smem, need);
-      }
-      q.tiles = q.x.tiles;
-      q.sp = dsp + ap.sp_index;
-      q.tw = p->d_tw;
-      chains[j].push_back(q);
-    };
-    auto s_pass = [&](int kind, const SParams& s, const AxisPlan& ap) {
-      BatchPass q{};
-      q.kind = kind;
-      q.s = s;
-      size_t pe = 0;
-      if (!ap.sp.has_generic && ap.sp.nstages > 0 && s.N >= 2) {
-        SParams t = s;
-        pe = pipe_fit_s(t, pipe_e);
-        if (pe) q.s = t;
-      }
-      if (pe) {
-        q.pipe = 1;
-        buf_elems = std::max(buf_elems, pe);
-      } else {
-        const size_t need = fit_s(q.s, ap, es);
-        fits = fits && need > 0;
-        smem = std::max(smem, need);
-      }
-      q.tiles = q.s.xtiles * q.s.O1;
-      q.sp = dsp + ap.sp_index;
-      q.tw = p->d_tw;
-      chains[j].push_back(q);
-    };
-    const long long rsize = (long long)p->nx * p->ny * p->nz;
-    const long long csize = (long long)p->nxhpc * p->nyc * p->nzc;
-    if (jb.kind == P3G_JOB_SPECTRUM) {
-      SpecParams sp;
-      int rc = make_spectrum_params(p, cplx, static_cast<double*>(jb.out), jb.kmax, jb.scale, jb.flags, csize, sp);
-      if (rc) return rc;
-      BatchPass q{};
-      q.kind = kBZero;
-      q.spec = sp;
-      q.tiles = 1;
-      chains[j].push_back(q);
-    }
-    if (jb.kind != P3G_JOB_BACKWARD) {
-      XParams x;
-      SParams y, z;
-      void* fout = jb.kind == P3G_JOB_FORWARD ? jb.out : cplx;
-      make_forward_params(p, jb.in, fout, wa, wb, 0, rsize, csize, x, y, z);
-      x_pass(kBXr2c, x);
-      s_pass(kBFwd, y, p->ax_y);
-      s_pass(kBFwd, z, p->ax_z[0]);
-    }
-    if (jb.kind == P3G_JOB_ROUNDTRIP || jb.kind == P3G_JOB_BACKWARD) {
-      SParams z, y;
-      XParams x;
-      const void* bin = jb.kind == P3G_JOB_BACKWARD ? jb.in : cplx;
-      make_backward_params(p, bin, jb.out, wa, wb, 0, csize, rsize, z, y, x);
-      s_pass(kBBwd, z, p->ax_z[0]);
-      s_pass(kBBwd, y, p->ax_y);
-      x_pass(kBXc2r, x);
-    }
-    if (!fits) return fail(P3G_E_UNSUPPORTED, who + "a line is longer than a batch tile (4096 points)");
-    if (jb.kind == P3G_JOB_SPECTRUM) {
-      BatchPass q = chains[j][0];
-      q.kind = kBSpec;
-      q.rows_per_item = nwarps * 4;
-      q.tiles = (q.spec.rows + q.rows_per_item - 1) / q.rows_per_item;
-      smem = std::max(smem, (size_t)nwarps * (q.spec.kmax + 1) * sizeof(double));
-      chains[j].push_back(q);
-    }
+  int threads = kBatchThreadsSmall;
+  for (;;) {
+    bool fit = false;
+    const int rc = build_chains(b, njobs, jobs, threads, chains, smem, buf_elems, fit);
+    if (rc != P3G_OK) return rc;
+    if (fit) break;
+    if (threads == kBatchThreadsLarge)
+      return fail(P3G_E_UNSUPPORTED, "a line is longer than a batch tile (4096 points)");
+    threads = kBatchThreadsLarge;
   }
   {
     const size_t es = f64 ? 16 : 8;
@@ -628,10 +668,10 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
       }
   }
   if (items > 0x7FFFFFF0LL) return fail(P3G_E_UNSUPPORTED, "too many work items");
-  int per_sm = 1, thr = threads;
+  int per_sm = 1;
   size_t max_dyn = 0;
-  cudaError_t e = f64 ? batch_config<PathF64>(smem, thr, per_sm, max_dyn)
-                      : batch_config<PathF32>(smem, thr, per_sm, max_dyn);
+  cudaError_t e = f64 ? batch_config<PathF64>(smem, threads, per_sm, max_dyn)
+                      : batch_config<PathF32>(smem, threads, per_sm, max_dyn);
   if (e != cudaSuccess && smem > max_dyn && max_dyn > 0)
     return fail(P3G_E_UNSUPPORTED, "a job's tile needs " + std::to_string(smem) + " bytes of shared memory, above " +
                                        std::to_string(max_dyn));
@@ -668,7 +708,7 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
   b->nitems = (int)items;
   b->smem = smem;
   b->buf_elems = (int)buf_elems;
-  b->threads = thr;
+  b->threads = threads;
   const long long slots = (long long)b->sm_count * per_sm;
   b->grid = (int)std::max(1LL, std::min(slots, items));
   return P3G_OK;
@@ -758,12 +798,13 @@ int p3g_batch_block_pass(p3g_batch b, int pass) {
   return P3G_OK;
 }
 
-int p3g_batch_info(p3g_batch b, long long info[4]) {
+int p3g_batch_info(p3g_batch b, long long info[5]) {
   if (!b) return fail(P3G_E_STATE, "batch is NULL");
   info[0] = b->npass;
   info[1] = b->nitems;
   info[2] = b->grid;
   info[3] = b->launches;
+  info[4] = b->threads;
   return P3G_OK;
 }
 

@@ -204,6 +204,29 @@ def test_batch_many_small_grids(torch_cuda):
     b.close()
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_batch_long_lines_use_large_ctas(torch_cuda, prec):
+    # batches of lines up to 2048 points run 128-thread CTAs; a 4096-point
+    # line needs the 256-thread tile, and the results stay the plain API's
+    import p3dfft_gb300 as pg
+    torch = torch_cuda
+    precision = pg.F64 if prec == "f64" else pg.F32
+    small = _make_jobs(torch, [(64, 48, 40), (2048, 4, 6)], [pg.JOB_ROUNDTRIP] * 2, precision, seed=9)
+    b = pg.Batch(precision).set_jobs(small)
+    assert b.info()["threads"] == 128
+    b.close()
+    jobs = _make_jobs(torch, [(4096, 6, 4), (64, 48, 40), (8, 4096, 2)], [pg.JOB_ROUNDTRIP] * 3, precision, seed=10)
+    b = pg.Batch(precision).set_jobs(jobs)
+    assert b.info()["threads"] == 256
+    b.launch()
+    b.check()
+    for j in jobs:
+        want = _alone(torch, j["plan"], j["kind"], j["in"])
+        torch.cuda.synchronize()
+        assert torch.equal(j["out"], want)
+    b.close()
+
+
 def test_batch_rejects_mixed_precision(torch_cuda):
     import p3dfft_gb300 as pg
     torch = torch_cuda
