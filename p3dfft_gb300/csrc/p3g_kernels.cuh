@@ -45,7 +45,22 @@ struct SParams {
   int post;         // 0: result row k = buffer[k], 1: DST-I, result k = i*buffer[k+1]
   int lmap_a0, lmap_a1, lmap_d;  // load: row j <- input row j - d if j >= a1, j if j < a0, else 0
   int smap_s0, smap_d;           // store: output row jo <- result row jo (jo < s0) or jo + d
+  // 1: 8-byte elements whose rows may start at an odd element (an odd row
+  // stride, e.g. the nx/2+1 modes of a binary32 complex row).  Such a row's
+  // tiles start one column later and wrap around (the last tile also takes
+  // column 0), so that full tiles start on a 16-byte boundary and load two
+  // columns per copy.
+  int xphase;
 };
+
+// First column of tile xt of row (o1, o2) and the row's phase: 0, or 1 when
+// xphase is set and the row starts at an odd 8-byte element.  Column x0 + m
+// of the tile is valid below X + phase and is column x0 + m - X past X.
+P3G_HD int strided_phase(const SParams& s, int o1, int o2) {
+  if (!s.xphase) return 0;
+  return (int)(((unsigned long long)reinterpret_cast<uintptr_t>(s.in) / 8u + (unsigned long long)o1 * s.in_o1 +
+                (unsigned long long)o2 * s.in_o2) & 1u);
+}
 
 struct ChebyParams {
   void* data;          // user complex output of the 'ffc' transform

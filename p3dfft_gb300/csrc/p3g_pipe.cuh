@@ -99,13 +99,18 @@ template <class P>
 P3G_D void strided_copy(const SParams& s, typename P::W* dst, int xt, int o1, int o2) {
   using W = typename P::W;
   const int M = s.M, L = s.L;
-  const long long ib = (long long)o1 * s.in_o1 + (long long)o2 * s.in_o2 + (long long)xt * M * s.in_xs;
+  const int ph = strided_phase(s, o1, o2);
+  const int x0 = xt * M + ph;
+  const long long ib0 = (long long)o1 * s.in_o1 + (long long)o2 * s.in_o2;
+  const long long ib = ib0 + (long long)x0 * s.in_xs;
   const char* in = static_cast<const char*>(s.in);
   constexpr int esz = (int)sizeof(W);
   auto one = [&](int m, int j) {
     const int src = j >= s.lmap_a1 ? j - s.lmap_d : (j < s.lmap_a0 ? j : -1);
-    const bool ok = src >= 0 && xt * M + m < s.X;
-    const char* g = ok ? in + (ib + (long long)m * s.in_xs + (long long)src * s.in_axis) * esz : in;
+    const int c = x0 + m;
+    const bool ok = src >= 0 && c < s.X + ph;
+    const int cw = c < s.X ? c : c - s.X;  // the phase-shifted row's last tile wraps to column 0
+    const char* g = ok ? in + (ib0 + (long long)cw * s.in_xs + (long long)src * s.in_axis) * esz : in;
     const uint32_t nb = ok ? (uint32_t)esz : 0u;
     int r0 = j, r1 = -1;
     if (s.pre == 2) {
@@ -136,7 +141,7 @@ P3G_D void strided_copy(const SParams& s, typename P::W* dst, int xt, int o1, in
     // the tile's first column and the row stride keep the pair 16-byte aligned
     // (a tile whose pair would cross the last valid column copies singly)
     const bool pairs = s.in_xs == 1 && M >= 2 && ((ib | s.in_axis) & 1) == 0 &&
-                       (reinterpret_cast<uintptr_t>(in) & 15) == 0 && xt * M + M <= s.X;
+                       (reinterpret_cast<uintptr_t>(in) & 15) == 0 && x0 + M <= s.X;
     if (pairs) {
       const int MP = M >> 1, lmp = s.log2m - 1;
       for (int e = threadIdx.x; e < MP * L; e += T) {
@@ -207,7 +212,7 @@ template <class P>
 P3G_D void strided_fix(const SParams& s, bool tma, typename P::W* sm) {
   using W = typename P::W;
   using C = typename P::C;
-  const bool raw_user = s.in_user != 0;
+  const bool raw_user = s.in_user != 0 && P::kF64;  // binary32 user data is the working format
   if (raw_user || s.pre == 2 || (tma && s.pre == 1)) {
     const int M = s.M, L = s.L;
     const int rows = tma ? L : s.N;
@@ -230,30 +235,33 @@ template <class P>
 P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int o1, int o2) {
   using C = typename P::C;
   const int M = s.M;
-  const int x0 = xt * M;
-  const long long obase = (long long)o1 * s.out_o1 + (long long)o2 * s.out_o2 + (long long)x0 * s.out_xs;
+  const int ph = strided_phase(s, o1, o2);  // the tile's columns as loaded by strided_copy
+  const int x0 = xt * M + ph;
+  const int xend = s.X + ph;
+  const long long obase = (long long)o1 * s.out_o1 + (long long)o2 * s.out_o2;
   auto one = [&](int m, int jo) {
     const int k = jo < s.smap_s0 ? jo : jo + s.smap_d;
+    const int c = x0 + m < s.X ? x0 + m : x0 + m - s.X;
     C v;
     if (s.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
     else v = P::from_w(sm[k * M + m]);
-    store_elem<P>(s.out, s.out_user, obase + (long long)m * s.out_xs + (long long)jo * s.out_axis, v);
+    store_elem<P>(s.out, s.out_user, obase + (long long)c * s.out_xs + (long long)jo * s.out_axis, v);
   };
   const int T = blockDim.x;
   if (s.out_xs != 1) {  // rows adjacent in memory (STRIDE1 user layout): rows fastest
     const FastDiv div_lo(s.Lout);
     for (int e = threadIdx.x; e < M * s.Lout; e += T) {
       const int m = (int)div_lo.div(e);
-      if (x0 + m < s.X) one(m, e - m * s.Lout);
+      if (x0 + m < xend) one(m, e - m * s.Lout);
     }
   } else if ((T & (M - 1)) == 0) {
     const int m = threadIdx.x & (M - 1);
-    if (x0 + m < s.X)
+    if (x0 + m < xend)
       for (int jo = threadIdx.x >> s.log2m; jo < s.Lout; jo += T >> s.log2m) one(m, jo);
   } else {
     for (int e = threadIdx.x; e < M * s.Lout; e += T) {
       const int m = e & (M - 1);
-      if (x0 + m < s.X) one(m, e >> s.log2m);
+      if (x0 + m < xend) one(m, e >> s.log2m);
     }
   }
 }

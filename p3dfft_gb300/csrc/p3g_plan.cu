@@ -432,7 +432,8 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
     // (no zero band and no shift; the backward passes of an unpruned grid
     // have a0 == a1 and d == 0)
     const bool identity_rows = (s.lmap_a0 >= s.L && s.lmap_a1 >= s.L) || (s.lmap_d == 0 && s.lmap_a0 >= s.lmap_a1);
-    if (p->use_tma && s.in_xs == 1 && s.pre <= 1 && identity_rows && (!s.in_user || device_memory(s.in))) {
+    if (p->use_tma && s.in_xs == 1 && s.pre <= 1 && identity_rows && !s.xphase &&
+        (!s.in_user || device_memory(s.in))) {
       const int brows = pick_box_rows(s.L, ap.n, s.M, esize);
       if (brows > 0 && encode_strided_map(&map, s.in, esize, s.X, s.L, s.O1, nv, s.in_axis, s.in_o1, s.in_o2, s.M,
                                           brows)) {
@@ -636,6 +637,8 @@ void make_backward_params(p3g_plan p, const void* in, void* out, void* wa, void*
     z.in_o1 = p->nxhpc;
   }
   z.in_o2 = dim_in;
+  // binary32 complex rows of nxhpc modes start at odd elements for odd nxhpc
+  z.xphase = p->prec == P3G_F32 && z.in_xs == 1;
   z.out_axis = (long long)p->nyc * P_;
   z.out_o1 = P_;
   z.out_o2 = z_field;
