@@ -408,6 +408,11 @@ def run_batched(torch, pg, dev, steps, warmup, plain_f64_gpts):
     out["tuning_s"] = round(time.time() - t_tune, 1)
     if plain_f64_gpts:
         out["f32_vs_plain_f64_1024cubed"] = round(results["f32"]["value"] / plain_f64_gpts, 3)
+    # the same 64 grids: FP32 batched form against FP64 batched and against
+    # FP64 through the plain per-plan API
+    out["f32_vs_f64_batched_same_grids"] = round(results["f32"]["value"] / results["f64"]["value"], 3)
+    out["f32_vs_f64_plain_api_same_grids"] = round(results["f64"]["plain_api_ms_per_step"] /
+                                                   results["f32"]["ms_per_step"], 3)
     return out
 
 
