@@ -331,6 +331,31 @@ P3G_D typename P::W* xpipe_buf(const PipeCommon& pc, int b) {
   return reinterpret_cast<typename P::W*>(align1k(p3g_pipe_smem)) + b * pc.buf_elems;
 }
 
+// cp.async of CH bytes (16, 8 or 4)
+template <int CH>
+P3G_D void cp_async_n(void* d, const void* g, uint32_t nb) {
+  if constexpr (CH == 16) cp_async16(d, g, nb);
+  else if constexpr (CH == 8) cp_async8(d, g, nb);
+  else cp_async4(d, g, nb);
+}
+
+// Line by line: each thread copies every blockDim.x-th chunk of each line, with
+// the line's addresses formed once (lines at least blockDim.x chunks long).
+template <class P, int CH>
+P3G_D void xr2c_copy_lines(const XParams& x, const char* in, char* dst, int p0) {
+  using UR = typename P::UR;
+  const int lbytes = x.nx * (int)sizeof(UR);
+  const int step = (int)blockDim.x * CH;
+  for (int lt = 0; lt < 2 * x.M; ++lt) {
+    const int line = 2 * p0 + lt;
+    const bool ok = line < x.nlines;
+    const char* g = in + (ok ? (long long)line * x.in_line * (long long)sizeof(UR) : 0LL);
+    char* d = dst + lt * lbytes;
+    const uint32_t nb = ok ? (uint32_t)CH : 0u;
+    for (int c = (int)threadIdx.x * CH; c < lbytes; c += step) cp_async_n<CH>(d + c, g + c, nb);
+  }
+}
+
 // r2c: real lines 2p, 2p+1 of the tile (first pair p0 of field `field`)
 // copied raw ([line][x]) into dst, `chunk` bytes per copy, without a commit.
 template <class P>
@@ -340,6 +365,12 @@ P3G_D void xr2c_copy(const XParams& x, int chunk, typename P::W* dst_w, int p0, 
   const char* in = reinterpret_cast<const char*>(static_cast<const UR*>(x.in) + field * x.in_field);
   char* dst = reinterpret_cast<char*>(dst_w);
   const int cpl = N * (int)sizeof(UR) / chunk;  // copies per line
+  if (cpl >= (int)blockDim.x) {
+    if (chunk == 16) xr2c_copy_lines<P, 16>(x, in, dst, p0);
+    else if (chunk == 8) xr2c_copy_lines<P, 8>(x, in, dst, p0);
+    else xr2c_copy_lines<P, 4>(x, in, dst, p0);
+    return;
+  }
   const FastDiv fcpl((uint32_t)cpl);
   for (int e = threadIdx.x; e < 2 * M * cpl; e += blockDim.x) {
     const int lt = (int)fcpl.div((uint32_t)e);
@@ -504,6 +535,19 @@ P3G_D void xc2r_copy(const XParams& x, typename P::W* dst, int p0, int field) {
     // two complexes per 16-byte copy: raw stride rs even, line pitch even
     const int rs = xc2r_raw_stride(nh, 8), hp = rs >> 1;
     if ((x.in_line & 1) == 0 && (reinterpret_cast<uintptr_t>(in) & 15) == 0) {
+      if (hp >= (int)blockDim.x) {  // line by line, addresses formed once per line
+        for (int lt = 0; lt < 2 * M; ++lt) {
+          const int line = 2 * p0 + lt;
+          const int keep = line < x.nlines ? x.nkeep : 0;
+          const W* g = in + (line < x.nlines ? (long long)line * x.in_line : 0LL);
+          W* d = dst + lt * rs;
+          for (int k = 2 * (int)threadIdx.x; k < rs; k += 2 * (int)blockDim.x) {
+            const int nv = min(max(keep - k, 0), 2);
+            cp_async16(d + k, nv ? g + k : in, (uint32_t)(8 * nv));
+          }
+        }
+        return;
+      }
       const FastDiv fhp((uint32_t)hp);
       for (int e = threadIdx.x; e < 2 * M * hp; e += blockDim.x) {
         const int lt = (int)fhp.div((uint32_t)e);
@@ -523,6 +567,20 @@ P3G_D void xc2r_copy(const XParams& x, typename P::W* dst, int p0, int field) {
       const bool ok = line < x.nlines && k < x.nkeep;
       const W* g = ok ? in + (long long)line * x.in_line + k : in;
       cp_async8(dst + lt * rs + k, g, ok ? 8u : 0u);
+    }
+    return;
+  }
+  if (nh >= (int)blockDim.x) {  // line by line, addresses formed once per line
+    for (int lt = 0; lt < 2 * M; ++lt) {
+      const int line = 2 * p0 + lt;
+      const int keep = line < x.nlines ? x.nkeep : 0;
+      const W* g = in + (line < x.nlines ? (long long)line * x.in_line : 0LL);
+      W* d = dst + lt * nh;
+      for (int k = threadIdx.x; k < nh; k += blockDim.x) {
+        const bool ok = k < keep;
+        if constexpr (sizeof(W) == 16) cp_async16(d + k, ok ? g + k : in, ok ? 16u : 0u);
+        else cp_async8(d + k, ok ? g + k : in, ok ? 8u : 0u);
+      }
     }
     return;
   }
