@@ -14,7 +14,7 @@ struct XParams {
   const void* in;
   void* out;
   long long in_field, out_field;  // element stride between fields (nv)
-  long long in_line, out_line;    // element stride between lines
+  int in_line, out_line;          // element stride between lines (below 2^31, checked at plan creation)
   int nlines;                     // lines per field (ny * nz)
   int nx;                         // real line length = complex FFT length
   int nkeep;                      // complex modes per line stored (r2c) / read (c2r)
@@ -32,9 +32,13 @@ struct SParams {
   const void* in;
   void* out;
   int in_user, out_user;  // 1: user complex format, 0: workspace format
-  long long in_axis, in_o1, in_o2;
-  long long out_axis, out_o1, out_o2;
-  long long in_xs, out_xs;  // stride between x columns: 1, or nyc*nzc for the STRIDE1 user layout
+  // per-element strides (along the axis, between x columns: 1, or nyc*nzc
+  // for the STRIDE1 user layout) are below 2^31, checked at plan creation;
+  // row (o1) and field (o2) strides are 64-bit
+  int in_axis, out_axis;
+  int in_xs, out_xs;
+  long long in_o1, in_o2;
+  long long out_o1, out_o2;
   int X;            // valid x columns
   int M, log2m;     // tile width (power of two)
   int xtiles, O1;   // tiles per row, number of o1 rows (o2 = fields from the grid)

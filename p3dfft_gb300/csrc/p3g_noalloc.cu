@@ -69,7 +69,7 @@ int forward_passes(p3g_plan p, const void* in, void* out, int zi, bool fsign, vo
     x.in_field = (long long)p->nx * p->ny * p->nz;
     x.out_field = (long long)p->nz * p->ny * P_;
     x.in_line = p->nx;
-    x.out_line = P_;
+    x.out_line = (int)P_;
     x.nlines = p->ny * p->nz;
     x.nx = p->nx;
     x.nkeep = p->nxhpc;
@@ -87,10 +87,10 @@ int forward_passes(p3g_plan p, const void* in, void* out, int zi, bool fsign, vo
     s.in_xs = s.out_xs = 1;
     s.in = wa;
     s.out = ybuf;
-    s.in_axis = P_;
+    s.in_axis = (int)P_;
     s.in_o1 = (long long)p->ny * P_;
     s.in_o2 = (long long)p->nz * p->ny * P_;
-    s.out_axis = P_;
+    s.out_axis = (int)P_;
     s.out_o1 = (long long)p->nyc * P_;
     s.out_o2 = (long long)p->nz * p->nyc * P_;
     s.X = p->nxhpc;
@@ -116,10 +116,10 @@ int forward_passes(p3g_plan p, const void* in, void* out, int zi, bool fsign, vo
     s.in = ybuf;
     s.out = out;
     s.out_user = 1;
-    s.in_axis = (long long)p->nyc * P_;
+    s.in_axis = (int)(p->nyc * P_);
     s.in_o1 = P_;
     s.in_o2 = (long long)p->nz * p->nyc * P_;
-    s.out_axis = (long long)p->nxhpc * p->nyc;
+    s.out_axis = p->nxhpc * p->nyc;
     s.out_o1 = p->nxhpc;
     s.out_o2 = (long long)p->nxhpc * p->nyc * p->nzc;
     s.X = p->nxhpc;

@@ -543,7 +543,7 @@ void make_forward_params(p3g_plan p, const void* in, void* out, void* wa, void* 
   x.in_field = dim_in;
   x.out_field = wa_field;
   x.in_line = p->nx;
-  x.out_line = P_;
+  x.out_line = (int)P_;
   x.nlines = p->ny * p->nz;
   x.nx = p->nx;
   x.nkeep = p->nxhpc;
@@ -557,10 +557,10 @@ void make_forward_params(p3g_plan p, const void* in, void* out, void* wa, void* 
   y.in_xs = y.out_xs = 1;
   y.in = wa;
   y.out = ybuf;
-  y.in_axis = P_;
+  y.in_axis = (int)P_;
   y.in_o1 = (long long)p->ny * P_;
   y.in_o2 = wa_field;
-  y.out_axis = P_;
+  y.out_axis = (int)P_;
   y.out_o1 = (long long)p->nyc * P_;
   y.out_o2 = y_field;
   y.X = p->nxhpc;
@@ -582,15 +582,15 @@ void make_forward_params(p3g_plan p, const void* in, void* out, void* wa, void* 
   z.in = ybuf;
   z.out = out;
   z.out_user = 1;
-  z.in_axis = (long long)p->nyc * P_;
+  z.in_axis = (int)(p->nyc * P_);
   z.in_o1 = P_;
   z.in_o2 = y_field;
   if (p->layout == P3G_LAYOUT_STRIDE1) {  // (nzc, nyc, nxhpc), z fastest (module.F90:245-254)
     z.out_axis = 1;
     z.out_o1 = p->nzc;
-    z.out_xs = (long long)p->nyc * p->nzc;
+    z.out_xs = p->nyc * p->nzc;
   } else {
-    z.out_axis = (long long)p->nxhpc * p->nyc;
+    z.out_axis = p->nxhpc * p->nyc;
     z.out_o1 = p->nxhpc;
   }
   z.out_o2 = dim_out;
@@ -631,15 +631,15 @@ void make_backward_params(p3g_plan p, const void* in, void* out, void* wa, void*
   if (p->layout == P3G_LAYOUT_STRIDE1) {
     z.in_axis = 1;
     z.in_o1 = p->nzc;
-    z.in_xs = (long long)p->nyc * p->nzc;
+    z.in_xs = p->nyc * p->nzc;
   } else {
-    z.in_axis = (long long)p->nxhpc * p->nyc;
+    z.in_axis = p->nxhpc * p->nyc;
     z.in_o1 = p->nxhpc;
   }
   z.in_o2 = dim_in;
   // binary32 complex rows of nxhpc modes start at odd elements for odd nxhpc
   z.xphase = p->prec == P3G_F32 && z.in_xs == 1;
-  z.out_axis = (long long)p->nyc * P_;
+  z.out_axis = (int)(p->nyc * P_);
   z.out_o1 = P_;
   z.out_o2 = z_field;
   z.X = p->nxhpc;
@@ -661,10 +661,10 @@ void make_backward_params(p3g_plan p, const void* in, void* out, void* wa, void*
   y.in_xs = y.out_xs = 1;
   y.in = zbuf;
   y.out = wa;
-  y.in_axis = P_;
+  y.in_axis = (int)P_;
   y.in_o1 = (long long)p->nyc * P_;
   y.in_o2 = z_field;
-  y.out_axis = P_;
+  y.out_axis = (int)P_;
   y.out_o1 = (long long)p->ny * P_;
   y.out_o2 = wa_field;
   y.X = p->nxhpc;
@@ -685,7 +685,7 @@ void make_backward_params(p3g_plan p, const void* in, void* out, void* wa, void*
   x.out = out;
   x.in_field = wa_field;
   x.out_field = dim_out;
-  x.in_line = P_;
+  x.in_line = (int)P_;
   x.out_line = p->nx;
   x.nlines = p->ny * p->nz;
   x.nx = p->nx;
@@ -1064,6 +1064,10 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     delete p;
     return fail(P3G_E_UNSUPPORTED, m);
   };
+  // the kernels form per-element offsets within a plane in 32 bits
+  if ((long long)p->pitch * ny >= (1LL << 31) || (long long)p->nxhpc * p->nyc >= (1LL << 31) ||
+      (long long)p->nyc * p->nzc >= (1LL << 31))
+    return bad("a plane of more than 2^31 elements is not supported");
   if (!add_axis(p->ax_x, nx, (ny * nz + 1) / 2)) return bad("x length " + std::to_string(nx) + " is too long");
   {
     // line padding for the X tiles (pad_index in p3g_engine.cuh): only for
