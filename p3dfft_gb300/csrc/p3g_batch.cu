@@ -176,7 +176,7 @@ P3G_D void batch_issue(const BatchPass& bp, int tile, typename P::W* buf) {
     case kBXc2r: xc2r_copy<P>(bp.x, buf, tile * bp.x.M, 0); break;
     default: {
       const int o1 = tile / bp.s.xtiles;
-      strided_copy<P>(bp.s, buf, tile - o1 * bp.s.xtiles, o1, 0);
+      strided_copy<P, true>(bp.s, buf, tile - o1 * bp.s.xtiles, o1, 0);
       break;
     }
   }

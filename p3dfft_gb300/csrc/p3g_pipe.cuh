@@ -95,7 +95,7 @@ P3G_D void strided_decode(const SPipeParams& q, int tile, int& xt, int& o1, int&
 // o2) into dst, without a commit; the DCT-I/DST-I extension rows are extra
 // copies of the same elements (the DST-I negation happens in the fix-up
 // step).
-template <class P>
+template <class P, bool WALK = false>
 P3G_D void strided_copy(const SParams& s, typename P::W* dst, int xt, int o1, int o2) {
   using W = typename P::W;
   const int M = s.M, L = s.L;
@@ -144,6 +144,21 @@ P3G_D void strided_copy(const SParams& s, typename P::W* dst, int xt, int o1, in
                        (reinterpret_cast<uintptr_t>(in) & 15) == 0 && x0 + M <= s.X;
     if (pairs) {
       const int MP = M >> 1, lmp = s.log2m - 1;
+      const bool identity = s.pre == 0 && ((s.lmap_a0 >= L && s.lmap_a1 >= L) || (s.lmap_d == 0 && s.lmap_a0 >= s.lmap_a1));
+      if (WALK && identity && (T & (MP - 1)) == 0) {
+        // rows one to one: each thread keeps one column pair and walks its
+        // rows with addresses advanced by constant steps (faster inside the
+        // batch kernel; slower for the long lines of the pass kernels, whose
+        // loads are measured ~10 % slower with it)
+        const int m = 2 * (threadIdx.x & (MP - 1));
+        const int j0 = threadIdx.x >> lmp, js = T >> lmp;
+        const char* g = in + (ib + m + (long long)j0 * s.in_axis) * esz;
+        const long long gstep = (long long)js * s.in_axis * esz;
+        W* d = dst + j0 * M + m;
+#pragma unroll 4
+        for (int j = j0; j < L; j += js, g += gstep, d += js * M) cp_async16(d, g, 16u);
+        return;
+      }
       for (int e = threadIdx.x; e < MP * L; e += T) {
         const int m = 2 * (e & (MP - 1));
         const int j = e >> lmp;
@@ -248,6 +263,30 @@ P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int 
     store_elem<P>(s.out, s.out_user, obase + (long long)c * s.out_xs + (long long)jo * s.out_axis, v);
   };
   const int T = blockDim.x;
+  if (s.out_xs == 1 && s.post == 0 && (s.smap_s0 >= s.Lout || s.smap_d == 0) && (T & (M - 1)) == 0) {
+    // rows stored one to one (no pruning gap, no DST shift): each thread keeps
+    // one column and walks its rows with a shared-memory address and an
+    // output pointer advanced by constant steps
+    const int m = threadIdx.x & (M - 1);
+    if (x0 + m >= xend) return;
+    const int c = x0 + m < s.X ? x0 + m : x0 + m - s.X;
+    const int j0 = threadIdx.x >> s.log2m, js = T >> s.log2m;
+    using W = typename P::W;
+    uint32_t a = (uint32_t)__cvta_generic_to_shared(sm) + (uint32_t)((j0 * M + m) * (int)sizeof(W));
+    const uint32_t astep = (uint32_t)(T * (int)sizeof(W));
+    const long long o = obase + c + (long long)j0 * s.out_axis;
+    const long long ostep = (long long)js * s.out_axis;
+    if (s.out_user) {
+      typename P::UC* d = static_cast<typename P::UC*>(s.out) + o;
+#pragma unroll 4
+      for (int jo = j0; jo < s.Lout; jo += js, a += astep, d += ostep) *d = P::to_uc(P::from_w(lds(a, (W*)nullptr)));
+    } else {
+      W* d = static_cast<W*>(s.out) + o;
+#pragma unroll 4
+      for (int jo = j0; jo < s.Lout; jo += js, a += astep, d += ostep) *d = lds(a, (W*)nullptr);
+    }
+    return;
+  }
   if (s.out_xs != 1) {  // rows adjacent in memory (STRIDE1 user layout): rows fastest
     const FastDiv div_lo(s.Lout);
     for (int e = threadIdx.x; e < M * s.Lout; e += T) {
