@@ -306,7 +306,8 @@ def run_ours(args):
                      "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                      "peak_kind": peak_kind, "traffic": traffic,
-                     "traffic_source": "ncu DRAM read+write of the 1024x1024x32 Y-pass launch, 0.909 per algorithmic byte, scaled to this launch",
+                     "traffic_source": "ncu DRAM read+write of the 1024x1024x32 Y-pass launch, 0.909 per "
+                                       "algorithmic byte, scaled to this launch",
                      "step_bytes_model": bm["rt"],
                      "step_frac": round(bm["rt"] / (ms64 * 1e-3) / 1e9 / peak, 4)},
         "gpu_launches": launches,

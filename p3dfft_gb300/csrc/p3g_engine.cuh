@@ -159,7 +159,8 @@ __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const
   // bytes between inputs q, q+1 and between outputs q, q+1
   const uint32_t jstride = pm ? ((uint32_t)per_line << t.log2m) * kW
                               : (uint32_t)(t.JS * (int)kW) * (uint32_t)pad_index(per_line, ps);
-  const uint32_t ostride = pm ? ((uint32_t)ns << t.log2m) * kW : (uint32_t)(t.JS * (int)kW) * (uint32_t)pad_index(ns, ps);
+  const uint32_t ostride =
+      pm ? ((uint32_t)ns << t.log2m) * kW : (uint32_t)(t.JS * (int)kW) * (uint32_t)pad_index(ns, ps);
   // Non-full stages: explicitly initialised, because the arrays are written
   // and read under correlated guards (b < nb) the compiler cannot prove, and
   // inside a persistent tile loop an uninitialised element would otherwise be

@@ -144,7 +144,8 @@ P3G_D void strided_copy(const SParams& s, typename P::W* dst, int xt, int o1, in
                        (reinterpret_cast<uintptr_t>(in) & 15) == 0 && x0 + M <= s.X;
     if (pairs) {
       const int MP = M >> 1, lmp = s.log2m - 1;
-      const bool identity = s.pre == 0 && ((s.lmap_a0 >= L && s.lmap_a1 >= L) || (s.lmap_d == 0 && s.lmap_a0 >= s.lmap_a1));
+      const bool identity =
+          s.pre == 0 && ((s.lmap_a0 >= L && s.lmap_a1 >= L) || (s.lmap_d == 0 && s.lmap_a0 >= s.lmap_a1));
       if (WALK && identity && (T & (MP - 1)) == 0) {
         // rows one to one: each thread keeps one column pair and walks its
         // rows with addresses advanced by constant steps (faster inside the

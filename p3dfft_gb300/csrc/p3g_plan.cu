@@ -769,7 +769,8 @@ std::vector<RowBlock> row_blocks(int nyc, int chunks) {
   std::vector<RowBlock> r;
   if (chunks < 1) chunks = 1;
   if (chunks > nyc) chunks = nyc;
-  for (int c = 0; c < chunks; ++c) r.push_back({(int)((long long)c * nyc / chunks), (int)((long long)(c + 1) * nyc / chunks)});
+  for (int c = 0; c < chunks; ++c)
+    r.push_back({(int)((long long)c * nyc / chunks), (int)((long long)(c + 1) * nyc / chunks)});
   return r;
 }
 

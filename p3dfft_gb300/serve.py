@@ -5,22 +5,23 @@ spectra (forward transform, then |u_hat|^2 binned into integer spherical
 shells in binary64 with the conjugate half counted), of any grid size.
 Plans (twiddles, stage tables) and each shape's input grid stay resident on
 the device.  The loop keeps ``slots`` launch slots, each a CUDA stream with
-one batch object per precision; whenever a slot is free it admits the oldest
-pending requests (FIFO) that fit the device-memory budget and the per-launch
-job limit, and launches them as one persistent batch (p3g_batch_*) per
-precision.  Requests that arrive while other slots are busy are admitted as
-slots and memory free up, and the slots' launches overlap on the GPU.
+one batch object per precision; whenever a slot is free it admits pending
+requests that fit the device-memory budget and the per-launch job limit,
+and launches them as one persistent batch (p3g_batch_*) per precision.
+Requests that arrive while other slots are busy are admitted as slots and
+memory free up, and the slots' launches overlap on the GPU.
 
-Scheduling (``launch_work``; None = FIFO): a free slot takes the pending requests with the least estimated work first (points
-x 2.5 for FP64, x 1.3 for spectra) until the launch holds ``launch_work``
-point-equivalents (at least one request), except that a request that has
-waited ``age_limit`` seconds goes first.  Every result of a launch is known
-only when the whole launch ends, so bounded launches keep a small request
-from waiting for a large batch; the size order keeps bursts of small
-requests from queueing behind large ones, and the age limit keeps large
-requests from starving.  Measured at 70 % load (10,000 requests of sides
-32..512): p99 22 ms FIFO against 16 ms with a 40M-point bound, mean 3.4 ms
-against 2.6 ms, for ~5 % less closed-loop capacity.
+Scheduling (``launch_work``; None = FIFO): a free slot takes the pending
+requests with the least estimated work first (points x 2.5 for FP64, x 1.3
+for spectra) until the launch holds ``launch_work`` point-equivalents (at
+least one request), except that a request that has waited ``age_limit``
+seconds goes first.  Every result of a launch is known only when the whole
+launch ends, so bounded launches keep a small request from waiting for a
+large batch; the size order keeps bursts of small requests from queueing
+behind large ones, and the age limit keeps large requests from starving.
+Measured at 70 % load (10,000 requests of sides 32..512): p99 22 ms FIFO
+against 16 ms with a 40M-point bound, mean 3.4 ms against 2.6 ms, for ~5 %
+less closed-loop capacity.
 
 Admission: a request holds its input, output and work buffer while in
 flight, and the sum over in-flight requests stays within the device-memory
