@@ -187,10 +187,9 @@ template <class P>
 P3G_D void batch_process_pipe(const BatchPass& bp, int tile, typename P::W* buf) {
   constexpr int E = batch_pipe_elems<P::kF64>();
   switch (bp.kind) {
-    case kBXr2c: {
-      xr2c_pack<P, E>(bp.x, buf);
+    case kBXr2c: {  // the first FFT stage reads the raw line pairs
       Tile<P> t{buf, nullptr, bp.x.M, bp.x.log2m, bp.x.LS, 1, bp.x.ps};
-      cta_fft<P, -1, E, kLineMajor>(t, bp.sp, bp.tw);
+      cta_fft<P, -1, E, kLineMajor, true>(t, bp.sp, bp.tw);
       xr2c_store<P>(bp.x, buf, tile * bp.x.M, 0);
       break;
     }

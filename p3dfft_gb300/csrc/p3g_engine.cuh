@@ -73,6 +73,16 @@ P3G_D float2 lds(uint32_t a, float2*) {
   asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];\n" : "=f"(v.x), "=f"(v.y) : "r"(a));
   return v;
 }
+P3G_D double lds1(uint32_t a, double*) {
+  double v;
+  asm volatile("ld.shared.f64 %0, [%1];\n" : "=d"(v) : "r"(a));
+  return v;
+}
+P3G_D float lds1(uint32_t a, float*) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];\n" : "=f"(v) : "r"(a));
+  return v;
+}
 P3G_D void sts(uint32_t a, float4 v) {
   asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};\n" ::"r"(a), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
                : "memory");
@@ -141,8 +151,11 @@ enum { kAnyLayout = -1, kLineMajor = 0, kPointMajor = 1 };
 // mapping needs no runtime layout test: point-major, butterfly b reads
 // element b (line b mod M, position b / M); line-major, b / (N / R) is the
 // line.  In the power-of-two families ns is a power of two (they run first),
-// so the twiddle index is a mask.
-template <class P, int DIR, int R, int E, int LAY, bool FULL>
+// so the twiddle index is a mask.  RAWX (first stage of a line-major X r2c
+// tile): the inputs come straight from the raw real lines 2*line and
+// 2*line+1 ([line][x], one user real each) as z = x1 + i x2, so no separate
+// packing pass precedes the FFT.
+template <class P, int DIR, int R, int E, int LAY, bool FULL, bool RAWX = false>
 __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const float4* __restrict__ tw) {
   using C = typename P::C;
   using W = typename P::W;
@@ -194,8 +207,19 @@ __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const
         j = (int)r;
         ia = sbase + (uint32_t)(t.addr(line, j) * (int)kW);
       }
+      if constexpr (RAWX) {
+        using UR = typename P::UR;
+        constexpr uint32_t kU = (uint32_t)sizeof(UR);
+        const uint32_t ra = sbase + (uint32_t)((2 * line * N + j) * (int)kU);
+        const uint32_t rstep = (uint32_t)per_line * kU, lstep = (uint32_t)N * kU;
 #pragma unroll
-      for (int q = 0; q < R; ++q) v[i][q] = P::from_w(lds(ia + q * jstride, (W*)nullptr));
+        for (int q = 0; q < R; ++q)
+          v[i][q] = P::make(P::from_ur(lds1(ra + q * rstep, (UR*)nullptr)),
+                            P::from_ur(lds1(ra + lstep + q * rstep, (UR*)nullptr)));
+      } else {
+#pragma unroll
+        for (int q = 0; q < R; ++q) v[i][q] = P::from_w(lds(ia + q * jstride, (W*)nullptr));
+      }
       const int k = kPow2 ? (j & (ns - 1)) : (int)(j - fd_ns.div((uint32_t)j) * (uint32_t)ns);
       if (ns > 1) {
         const float4* twp = tw + k * (R - 1) - 1;
@@ -260,15 +284,22 @@ __device__ __noinline__ void stage_generic(const Tile<P>& t, int N, int p, int n
 // length ns(s) = product of the radices before it; both follow from the
 // family counts, so they are carried in registers instead of being loaded
 // per stage (stage 0 owns one placeholder twiddle, see build_stages).
-template <class P, int DIR, int R, int E, int LAY>
+template <class P, int DIR, int R, int E, int LAY, bool RAWX>
 __device__ __forceinline__ void run_family(const Tile<P>& t, const float4* __restrict__ tw, int N, int cnt, int& ns,
-                                           int& off) {
+                                           int& off, bool& raw) {
   constexpr int MAXB = (E + R - 1) / R;
   const bool full = t.M * (N / R) == MAXB * (int)blockDim.x;
 #pragma unroll 1
   for (int c = 0; c < cnt; ++c) {
-    if (full) stage_reg<P, DIR, R, E, LAY, true>(t, N, ns, tw + off);
-    else stage_reg<P, DIR, R, E, LAY, false>(t, N, ns, tw + off);
+    if (RAWX && raw) {  // the plan's first stage reads the raw line pairs
+      if (full) stage_reg<P, DIR, R, E, LAY, true, RAWX>(t, N, ns, tw + off);
+      else stage_reg<P, DIR, R, E, LAY, false, RAWX>(t, N, ns, tw + off);
+      raw = false;
+    } else if (full) {
+      stage_reg<P, DIR, R, E, LAY, true>(t, N, ns, tw + off);
+    } else {
+      stage_reg<P, DIR, R, E, LAY, false>(t, N, ns, tw + off);
+    }
     off += ns > 1 ? ns * (R - 1) : 1;
     ns *= R;
   }
@@ -284,8 +315,10 @@ __device__ __forceinline__ void run_family(const Tile<P>& t, const float4* __res
 // tw points at the twiddle table entry tw_base (the full table with
 // tw_base = 0, or a pass's slice copied to shared memory).  E = elements each
 // thread holds per stage; the launch uses ceil(M N / E) threads.  LAY: the
-// tile layout when the caller knows it (kPointMajor, kLineMajor).
-template <class P, int DIR, int E = kElemsPerThread, int LAY = kAnyLayout>
+// tile layout when the caller knows it (kPointMajor, kLineMajor).  RAWX: the
+// tile still holds the raw real line pairs of an X r2c tile (plans without
+// generic stages only), read by the first stage.
+template <class P, int DIR, int E = kElemsPerThread, int LAY = kAnyLayout, bool RAWX = false>
 __device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __restrict__ sp,
                                         const float4* __restrict__ tw, int tw_base = 0) {
   const int N = __ldg(&sp->n);
@@ -295,12 +328,13 @@ __device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __res
   const int nst = __ldg(&sp->nstages);
   int ns = 1;
   int off = __ldg(&sp->tw_off[0]) - tw_base;
-  if constexpr (!P::kF64) run_family<P, DIR, 16, E, LAY>(t, tw, N, c[0], ns, off);
-  run_family<P, DIR, 8, E, LAY>(t, tw, N, c[1], ns, off);
-  run_family<P, DIR, 4, E, LAY>(t, tw, N, c[2], ns, off);
-  run_family<P, DIR, 2, E, LAY>(t, tw, N, c[3], ns, off);
-  run_family<P, DIR, 3, E, LAY>(t, tw, N, c[4], ns, off);
-  run_family<P, DIR, 5, E, LAY>(t, tw, N, c[5], ns, off);
+  bool raw = RAWX;
+  if constexpr (!P::kF64) run_family<P, DIR, 16, E, LAY, RAWX>(t, tw, N, c[0], ns, off, raw);
+  run_family<P, DIR, 8, E, LAY, RAWX>(t, tw, N, c[1], ns, off, raw);
+  run_family<P, DIR, 4, E, LAY, RAWX>(t, tw, N, c[2], ns, off, raw);
+  run_family<P, DIR, 2, E, LAY, RAWX>(t, tw, N, c[3], ns, off, raw);
+  run_family<P, DIR, 3, E, LAY, RAWX>(t, tw, N, c[4], ns, off, raw);
+  run_family<P, DIR, 5, E, LAY, RAWX>(t, tw, N, c[5], ns, off, raw);
   const int sg = c[0] + c[1] + c[2] + c[3] + c[4] + c[5];
 #pragma unroll 1
   for (int s = sg; s < nst; ++s)

@@ -434,84 +434,6 @@ P3G_D void xr2c_issue(const XPipeParams& q, int tile, int b) {
   cp_async_commit();
 }
 
-// Real lines 2p, 2p+1 -> complex line p (z = x1 + i x2) in the padded
-// working layout, in place: every thread reads its items, a barrier, then
-// writes them.  MAXI >= M N / blockDim.x.  Even N: items go two adjacent
-// positions at a time (vector reads of both lines, two adjacent stores).
-// Ends with a barrier.
-template <class P, int MAXI>
-P3G_D void xr2c_pack(const XParams& x, typename P::W* sm) {
-  using C = typename P::C;
-  using UR = typename P::UR;
-  const UR* raw = reinterpret_cast<const UR*>(sm);
-  const int N = x.nx;
-  if ((N & 1) == 0) {
-    constexpr int H = (MAXI + 1) / 2;
-    const int NH = N >> 1, MNH = x.M * NH;
-    const FastDiv fNH((uint32_t)NH);
-    C v0[H], v1[H];
-#pragma unroll
-    for (int i = 0; i < H; ++i) v0[i] = v1[i] = P::zero();  // see stage_reg
-#pragma unroll
-    for (int i = 0; i < H; ++i) {
-      const int e = threadIdx.x + i * blockDim.x;
-      if (e < MNH) {
-        const int pr = (int)fNH.div((uint32_t)e);
-        const int xi = 2 * (e - pr * NH);
-        const UR* r0 = raw + (2 * pr) * N + xi;  // xi and N even: 2-element aligned
-        if constexpr (P::kF64) {
-          const double2 a = *reinterpret_cast<const double2*>(r0);
-          const double2 c = *reinterpret_cast<const double2*>(r0 + N);
-          v0[i] = P::make(P::from_ur(a.x), P::from_ur(c.x));
-          v1[i] = P::make(P::from_ur(a.y), P::from_ur(c.y));
-        } else {
-          const float2 a = *reinterpret_cast<const float2*>(r0);
-          const float2 c = *reinterpret_cast<const float2*>(r0 + N);
-          v0[i] = P::make(a.x, c.x);
-          v1[i] = P::make(a.y, c.y);
-        }
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < H; ++i) {
-      const int e = threadIdx.x + i * blockDim.x;
-      if (e < MNH) {
-        const int pr = (int)fNH.div((uint32_t)e);
-        const int j = pr * x.LS + pad_index(2 * (e - pr * NH), x.ps);  // even: j and j+1 share a pad group
-        sm[j] = P::to_w(v0[i]);
-        sm[j + 1] = P::to_w(v1[i]);
-      }
-    }
-    __syncthreads();
-    return;
-  }
-  const int MN = x.M * N;
-  const FastDiv fN((uint32_t)N);
-  C v[MAXI];
-#pragma unroll
-  for (int i = 0; i < MAXI; ++i) v[i] = P::zero();  // see stage_reg
-#pragma unroll
-  for (int i = 0; i < MAXI; ++i) {
-    const int e = threadIdx.x + i * blockDim.x;
-    if (e < MN) {
-      const int pr = (int)fN.div((uint32_t)e);
-      const int xi = e - pr * N;
-      v[i] = P::make(P::from_ur(raw[(2 * pr) * N + xi]), P::from_ur(raw[(2 * pr + 1) * N + xi]));
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int i = 0; i < MAXI; ++i) {
-    const int e = threadIdx.x + i * blockDim.x;
-    if (e < MN) {
-      const int pr = (int)fN.div((uint32_t)e);
-      sm[pr * x.LS + pad_index(e - pr * N, x.ps)] = P::to_w(v[i]);
-    }
-  }
-  __syncthreads();
-}
-
 // X1[k] = (Z[k] + conj Z[N-k]) / 2, X2[k] = -i (Z[k] - conj Z[N-k]) / 2,
 // modes k < nkeep stored to the working layout.
 template <class P>
@@ -549,10 +471,10 @@ __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::k
     else cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
-    xr2c_pack<P, XPipeLimits<P>::kE>(pp.x, xpipe_buf<P>(pp.c, b));
     {
+      // the first FFT stage reads the raw line pairs (packing fused into it)
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
-      cta_fft<P, -1, XPipeLimits<P>::kE, kLineMajor>(t, sp, tw_g, 0);
+      cta_fft<P, -1, XPipeLimits<P>::kE, kLineMajor, true>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;
