@@ -189,14 +189,13 @@ P3G_D void batch_process_pipe(const BatchPass& bp, int tile, typename P::W* buf)
   switch (bp.kind) {
     case kBXr2c: {  // the first FFT stage reads the raw line pairs
       Tile<P> t{buf, nullptr, bp.x.M, bp.x.log2m, bp.x.LS, 1, bp.x.ps};
-      cta_fft<P, -1, E, kLineMajor, true>(t, bp.sp, bp.tw);
+      cta_fft<P, -1, E, kLineMajor, kRawR2C>(t, bp.sp, bp.tw);
       xr2c_store<P>(bp.x, buf, tile * bp.x.M, 0);
       break;
     }
-    case kBXc2r: {
-      xc2r_merge<P, E / 2 + 2>(bp.x, buf);
+    case kBXc2r: {  // the first FFT stage reads the raw half spectra
       Tile<P> t{buf, nullptr, bp.x.M, bp.x.log2m, bp.x.LS, 1, bp.x.ps};
-      cta_fft<P, 1, E, kLineMajor>(t, bp.sp, bp.tw);
+      cta_fft<P, 1, E, kLineMajor, kRawC2R>(t, bp.sp, bp.tw);
       xc2r_store<P>(bp.x, buf, tile * bp.x.M, 0);
       break;
     }

@@ -151,11 +151,21 @@ enum { kAnyLayout = -1, kLineMajor = 0, kPointMajor = 1 };
 // mapping needs no runtime layout test: point-major, butterfly b reads
 // element b (line b mod M, position b / M); line-major, b / (N / R) is the
 // line.  In the power-of-two families ns is a power of two (they run first),
-// so the twiddle index is a mask.  RAWX (first stage of a line-major X r2c
-// tile): the inputs come straight from the raw real lines 2*line and
-// 2*line+1 ([line][x], one user real each) as z = x1 + i x2, so no separate
-// packing pass precedes the FFT.
-template <class P, int DIR, int R, int E, int LAY, bool FULL, bool RAWX = false>
+// so the twiddle index is a mask.
+//
+// RAW (first stage of a line-major X tile only) reads the tile's raw line
+// pairs instead of the packed complex line, so no separate pass precedes the
+// FFT:
+//   kRawR2C: real lines 2*line, 2*line+1 ([line][x], one user real each);
+//            z[p] = x1[p] + i x2[p].
+//   kRawC2R: the pair's half spectra (lines 2*line, 2*line+1 at a stride of
+//            rs working-format complexes, nh = N/2+1 modes each); the
+//            Hermitian extension z[p] = X1[p] + i X2[p] with
+//            X[p] = conj X[N-p] above N/2 and the imaginary parts of the
+//            p = 0 and p = N/2 modes ignored (as c2r does).
+enum { kRawNone = 0, kRawR2C = 1, kRawC2R = 2 };
+
+template <class P, int DIR, int R, int E, int LAY, bool FULL, int RAW = kRawNone>
 __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const float4* __restrict__ tw) {
   using C = typename P::C;
   using W = typename P::W;
@@ -207,7 +217,7 @@ __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const
         j = (int)r;
         ia = sbase + (uint32_t)(t.addr(line, j) * (int)kW);
       }
-      if constexpr (RAWX) {
+      if constexpr (RAW == kRawR2C) {
         using UR = typename P::UR;
         constexpr uint32_t kU = (uint32_t)sizeof(UR);
         const uint32_t ra = sbase + (uint32_t)((2 * line * N + j) * (int)kU);
@@ -216,6 +226,27 @@ __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const
         for (int q = 0; q < R; ++q)
           v[i][q] = P::make(P::from_ur(lds1(ra + q * rstep, (UR*)nullptr)),
                             P::from_ur(lds1(ra + lstep + q * rstep, (UR*)nullptr)));
+      } else if constexpr (RAW == kRawC2R) {
+        const int nh = N / 2 + 1;
+        const int rs = sizeof(W) == 8 ? (nh + 1) & ~1 : nh;  // raw line stride (xc2r_raw_stride)
+        const uint32_t ra = sbase + (uint32_t)(line * 2 * rs * (int)kW);
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+          const int pt = j + q * per_line;
+          const bool mir = 2 * pt > N;
+          const int pm = mir ? N - pt : pt;
+          C x1 = P::from_w(lds(ra + (uint32_t)(pm * (int)kW), (W*)nullptr));
+          C x2 = P::from_w(lds(ra + (uint32_t)((rs + pm) * (int)kW), (W*)nullptr));
+          if (pm == 0 || 2 * pm == N) {
+            x1 = P::make(P::re(x1), P::re(P::zero()));
+            x2 = P::make(P::re(x2), P::re(P::zero()));
+          }
+          if (mir) {
+            x1 = cconj(x1);
+            x2 = cconj(x2);
+          }
+          v[i][q] = x1 + rot<1>(x2);
+        }
       } else {
 #pragma unroll
         for (int q = 0; q < R; ++q) v[i][q] = P::from_w(lds(ia + q * jstride, (W*)nullptr));
@@ -284,16 +315,16 @@ __device__ __noinline__ void stage_generic(const Tile<P>& t, int N, int p, int n
 // length ns(s) = product of the radices before it; both follow from the
 // family counts, so they are carried in registers instead of being loaded
 // per stage (stage 0 owns one placeholder twiddle, see build_stages).
-template <class P, int DIR, int R, int E, int LAY, bool RAWX>
+template <class P, int DIR, int R, int E, int LAY, int RAW>
 __device__ __forceinline__ void run_family(const Tile<P>& t, const float4* __restrict__ tw, int N, int cnt, int& ns,
                                            int& off, bool& raw) {
   constexpr int MAXB = (E + R - 1) / R;
   const bool full = t.M * (N / R) == MAXB * (int)blockDim.x;
 #pragma unroll 1
   for (int c = 0; c < cnt; ++c) {
-    if (RAWX && raw) {  // the plan's first stage reads the raw line pairs
-      if (full) stage_reg<P, DIR, R, E, LAY, true, RAWX>(t, N, ns, tw + off);
-      else stage_reg<P, DIR, R, E, LAY, false, RAWX>(t, N, ns, tw + off);
+    if (RAW != kRawNone && raw) {  // the plan's first stage reads the raw line pairs
+      if (full) stage_reg<P, DIR, R, E, LAY, true, RAW>(t, N, ns, tw + off);
+      else stage_reg<P, DIR, R, E, LAY, false, RAW>(t, N, ns, tw + off);
       raw = false;
     } else if (full) {
       stage_reg<P, DIR, R, E, LAY, true>(t, N, ns, tw + off);
@@ -315,10 +346,10 @@ __device__ __forceinline__ void run_family(const Tile<P>& t, const float4* __res
 // tw points at the twiddle table entry tw_base (the full table with
 // tw_base = 0, or a pass's slice copied to shared memory).  E = elements each
 // thread holds per stage; the launch uses ceil(M N / E) threads.  LAY: the
-// tile layout when the caller knows it (kPointMajor, kLineMajor).  RAWX: the
-// tile still holds the raw real line pairs of an X r2c tile (plans without
-// generic stages only), read by the first stage.
-template <class P, int DIR, int E = kElemsPerThread, int LAY = kAnyLayout, bool RAWX = false>
+// tile layout when the caller knows it (kPointMajor, kLineMajor).  RAW: the
+// tile still holds the raw line pairs of an X r2c or c2r tile (kRawR2C,
+// kRawC2R; plans without generic stages only), read by the first stage.
+template <class P, int DIR, int E = kElemsPerThread, int LAY = kAnyLayout, int RAW = kRawNone>
 __device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __restrict__ sp,
                                         const float4* __restrict__ tw, int tw_base = 0) {
   const int N = __ldg(&sp->n);
@@ -328,13 +359,13 @@ __device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __res
   const int nst = __ldg(&sp->nstages);
   int ns = 1;
   int off = __ldg(&sp->tw_off[0]) - tw_base;
-  bool raw = RAWX;
-  if constexpr (!P::kF64) run_family<P, DIR, 16, E, LAY, RAWX>(t, tw, N, c[0], ns, off, raw);
-  run_family<P, DIR, 8, E, LAY, RAWX>(t, tw, N, c[1], ns, off, raw);
-  run_family<P, DIR, 4, E, LAY, RAWX>(t, tw, N, c[2], ns, off, raw);
-  run_family<P, DIR, 2, E, LAY, RAWX>(t, tw, N, c[3], ns, off, raw);
-  run_family<P, DIR, 3, E, LAY, RAWX>(t, tw, N, c[4], ns, off, raw);
-  run_family<P, DIR, 5, E, LAY, RAWX>(t, tw, N, c[5], ns, off, raw);
+  bool raw = RAW != kRawNone;
+  if constexpr (!P::kF64) run_family<P, DIR, 16, E, LAY, RAW>(t, tw, N, c[0], ns, off, raw);
+  run_family<P, DIR, 8, E, LAY, RAW>(t, tw, N, c[1], ns, off, raw);
+  run_family<P, DIR, 4, E, LAY, RAW>(t, tw, N, c[2], ns, off, raw);
+  run_family<P, DIR, 2, E, LAY, RAW>(t, tw, N, c[3], ns, off, raw);
+  run_family<P, DIR, 3, E, LAY, RAW>(t, tw, N, c[4], ns, off, raw);
+  run_family<P, DIR, 5, E, LAY, RAW>(t, tw, N, c[5], ns, off, raw);
   const int sg = c[0] + c[1] + c[2] + c[3] + c[4] + c[5];
 #pragma unroll 1
   for (int s = sg; s < nst; ++s)

@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::k
     {
       // the first FFT stage reads the raw line pairs (packing fused into it)
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
-      cta_fft<P, -1, XPipeLimits<P>::kE, kLineMajor, true>(t, sp, tw_g, 0);
+      cta_fft<P, -1, XPipeLimits<P>::kE, kLineMajor, kRawR2C>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;
@@ -566,54 +566,6 @@ P3G_D void xc2r_issue(const XPipeParams& q, int tile, int b) {
   cp_async_commit();
 }
 
-// Hermitian extension of the raw pair lines into Z = X1 + i X2 (padded
-// working layout), in place: read all, barrier, write.  MAXI >= M nh /
-// blockDim.x.  Ends with a barrier.
-template <class P, int MAXI>
-P3G_D void xc2r_merge(const XParams& x, typename P::W* sm) {
-  using C = typename P::C;
-  const int N = x.nx, nh = N / 2 + 1, rs = xc2r_raw_stride(nh, (int)sizeof(typename P::W)), NP = 2 * rs,
-            Mnh = x.M * nh;
-  const FastDiv fnh((uint32_t)nh);
-  C z0[MAXI], z1[MAXI];
-  int ip[MAXI], ik[MAXI];
-#pragma unroll
-  for (int i = 0; i < MAXI; ++i) {  // see stage_reg
-    z0[i] = P::zero();
-    z1[i] = P::zero();
-    ik[i] = 0;
-  }
-#pragma unroll
-  for (int i = 0; i < MAXI; ++i) {
-    const int e = threadIdx.x + i * blockDim.x;
-    ip[i] = -1;
-    if (e < Mnh) {
-      const int pr = (int)fnh.div((uint32_t)e);
-      const int k = e - pr * nh;
-      C x1 = P::from_w(sm[pr * NP + k]);
-      C x2 = P::from_w(sm[pr * NP + rs + k]);
-      if (k == 0 || 2 * k == N) {
-        x1 = P::make(P::re(x1), P::re(P::zero()));
-        x2 = P::make(P::re(x2), P::re(P::zero()));
-      }
-      z0[i] = x1 + rot<1>(x2);
-      z1[i] = cconj(x1) + rot<1>(cconj(x2));
-      ip[i] = pr;
-      ik[i] = k;
-    }
-  }
-  __syncthreads();
-  const int LS = x.LS, ps = x.ps;  // Z layout (padded), raw lines used NP = 2 rs
-#pragma unroll
-  for (int i = 0; i < MAXI; ++i) {
-    if (ip[i] >= 0) {
-      sm[ip[i] * LS + pad_index(ik[i], ps)] = P::to_w(z0[i]);
-      if (ik[i] > 0 && 2 * ik[i] < N) sm[ip[i] * LS + pad_index(N - ik[i], ps)] = P::to_w(z1[i]);
-    }
-  }
-  __syncthreads();
-}
-
 // x1 = Re z, x2 = Im z to the user's real lines (format conversion fused).
 // Even N: each thread takes positions n, n+1 of a line pair, reads the two
 // complex values once and writes two-element vectors to both lines.
@@ -677,10 +629,10 @@ __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::k
     else cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
-    xc2r_merge<P, XPipeLimits<P>::kE / 2 + 2>(pp.x, xpipe_buf<P>(pp.c, b));  // host: T * MAXI >= M nh
     {
+      // the first FFT stage reads the raw half spectra (Hermitian merge fused into it)
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
-      cta_fft<P, 1, XPipeLimits<P>::kE, kLineMajor>(t, sp, tw_g, 0);
+      cta_fft<P, 1, XPipeLimits<P>::kE, kLineMajor, kRawC2R>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;
