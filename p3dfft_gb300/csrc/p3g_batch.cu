@@ -74,14 +74,11 @@ template <bool F64>
 __host__ __device__ constexpr int batch_pipe_elems() { return F64 ? 8 : 16; }
 
 // Double-buffered path: halve the tile width until the tile fits E points per
-// thread (c2r: the Hermitian merge holds E/2 + 2 items per thread); returns
-// the buffer size in elements (0 when it cannot fit).
-size_t pipe_fit_x(XParams& x, bool c2r, int E, int esize, int threads) {
+// thread; returns the buffer size in elements (0 when it cannot fit), room
+// for the packed tile or the raw line pairs, whichever is larger.
+size_t pipe_fit_x(XParams& x, int E, int esize, int threads) {
   const int nh = x.nx / 2 + 1;
-  auto fits = [&](int M) {
-    return (long long)M * x.nx <= (long long)E * threads &&
-           (!c2r || (long long)M * nh <= (long long)(E / 2 + 2) * threads);
-  };
+  auto fits = [&](int M) { return (long long)M * x.nx <= (long long)E * threads; };
   while (x.M > 1 && !fits(x.M)) {
     x.M >>= 1;
     x.log2m--;
@@ -491,7 +488,7 @@ static int build_chains(p3g_batch b, int njobs, const p3g_job* jobs, int threads
       size_t pe = 0;
       if (!ap.sp.has_generic && ap.sp.nstages > 0 && x.nx >= 2) {
         XParams t = x;
-        pe = pipe_fit_x(t, kind == kBXc2r, pipe_e, (int)es, threads);
+        pe = pipe_fit_x(t, pipe_e, (int)es, threads);
         if (pe) q.x = t;
       }
       if (pe) {

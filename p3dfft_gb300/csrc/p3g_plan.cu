@@ -207,11 +207,6 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   const int nh = n / 2 + 1;
   auto threads_for = [&](int M) {
     int t = (M * n + E - 1) / E;
-    if (kind == 2) {
-      const int maxi = E / 2 + 2;
-      const int t2 = (M * nh + maxi - 1) / maxi;
-      t = t > t2 ? t : t2;
-    }
     t = (t + 31) / 32 * 32;
     return t < 32 ? 32 : t;
   };
