@@ -49,6 +49,10 @@ def test_plan_rejects_bad_sizes_without_gpu(lib):
     assert b"Invalid dimensions" in lib.core.p3g_last_error()
     assert lib.core.p3g_plan_create(ctypes.byref(h), 8, 8, 8, 10, 8, 8, 0, 0, 0) == -1
     assert lib.core.p3g_plan_create(ctypes.byref(h), 8, 8, 8, 8, 8, 8, 7, 0, 0) == -1
+    # a plane of 2^31 or more elements (131072/2+1 modes x 32768 rows) is refused before any
+    # device work: the kernels form offsets within a plane in 32 bits
+    assert lib.core.p3g_plan_create(ctypes.byref(h), 131072, 32768, 2, 0, 0, 0, 0, 0, 0) == -4
+    assert b"2^31" in lib.core.p3g_last_error()
 
 
 def test_legacy_use_before_setup_prints_and_returns(lib):
