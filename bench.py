@@ -32,13 +32,15 @@ METRIC = "3D r2c+c2r Gpts/s & %HBM roofline, FP32 vs FP64 at stated error; serve
 UNIT = "Gpts/s"
 
 CONFIGS = {
-    "large": dict(grid=(1024, 1024, 1024), ops=("fft", "tff"),
+    "large": dict(grid=(1024, 1024, 1024), ops=("fft", "tff"), input="modes",
                   workload="1024^3 FP64 r2c+c2r round trip (32 seeded Fourier modes + N(0,1e-3) noise)"),
-    "noncubic": dict(grid=(768, 1024, 540), ops=("fft", "tff"),
+    "noncubic": dict(grid=(768, 1024, 540), ops=("fft", "tff"), input="modes",
                      workload="768x1024x540 FP64 r2c+c2r round trip (32 seeded Fourier modes + N(0,1e-3) noise)"),
-    "small": dict(grid=(128, 128, 128), ops=("fft", "tff"), workload="128^3 FP64 r2c+c2r round trip, U[-1,1)"),
-    "cheby": dict(grid=(512, 512, 257), ops=("ffc", "cff"),
-                  workload="512x512x257 FP64 FFT(x,y) + DCT-I(z) round trip"),
+    "small": dict(grid=(128, 128, 128), ops=("fft", "tff"), input="uniform",
+                  workload="128^3 FP64 r2c+c2r round trip, U[-1,1)"),
+    "cheby": dict(grid=(512, 512, 257), ops=("ffc", "cff"), input="cheby",
+                  workload="512x512x257 FP64 FFT(x,y) + DCT-I(z) round trip, 16 seeded sin cos T_m(z) terms "
+                           "on Gauss-Lobatto z + 1e-6 noise; p3dfft_cheby beside it"),
 }
 
 
@@ -62,26 +64,39 @@ def load_peaks():
 
 
 # ----------------------------------------------------------------- inputs
-def make_input(torch, grid, seed, device, kind):
-    """Seeded synthetic field on the device, (nz, ny, nx) float64."""
-    nx, ny, nz = grid
-    g = torch.Generator(device=device)
-    g.manual_seed(seed)
-    if kind == "uniform":
-        return torch.rand((nz, ny, nx), generator=g, device=device, dtype=torch.float64) * 2 - 1
+def modes_list(grid, seed, count=32):
+    """The seeded Fourier modes of the large/noncubic workloads: wavevector k
+    (integer, 0 < |k| <= nx/4), amplitude in [0.5, 1.5), phase in [0, 2 pi)."""
+    nx = grid[0]
     rng = np.random.default_rng(seed)
-    x = torch.arange(nx, device=device, dtype=torch.float64) / nx
-    y = torch.arange(ny, device=device, dtype=torch.float64) / ny
-    z = torch.arange(nz, device=device, dtype=torch.float64) / nz
-    f = torch.randn((nz, ny, nx), generator=g, device=device, dtype=torch.float64) * 1e-3
     kmax = nx / 4
-    for _ in range(32):
+    out = []
+    for _ in range(count):
         while True:
             k = rng.integers(-int(kmax), int(kmax) + 1, size=3)
             if 0 < np.sqrt((k ** 2).sum()) <= kmax:
                 break
         amp = rng.uniform(0.5, 1.5)
         ph = rng.uniform(0, 2 * np.pi)
+        out.append((tuple(int(v) for v in k), float(amp), float(ph)))
+    return out
+
+
+def make_input(torch, grid, seed, device, kind):
+    """Seeded synthetic field on the device, (nz, ny, nx) float64: U[-1,1)
+    ("uniform"), or the sum of modes_list's cosines plus N(0, 1e-3) noise."""
+    nx, ny, nz = grid
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    if kind == "uniform":
+        return torch.rand((nz, ny, nx), generator=g, device=device, dtype=torch.float64) * 2 - 1
+    if kind == "cheby":
+        return make_cheby_input(torch, grid, seed, device)
+    x = torch.arange(nx, device=device, dtype=torch.float64) / nx
+    y = torch.arange(ny, device=device, dtype=torch.float64) / ny
+    z = torch.arange(nz, device=device, dtype=torch.float64) / nz
+    f = torch.randn((nz, ny, nx), generator=g, device=device, dtype=torch.float64) * 1e-3
+    for k, amp, ph in modes_list(grid, seed):
         # cos(2 pi (kx x + ky y + kz z) + ph), built separably
         ax = torch.exp(1j * (2 * np.pi * k[0] * x + ph))
         ay = torch.exp(1j * 2 * np.pi * k[1] * y)
@@ -89,6 +104,45 @@ def make_input(torch, grid, seed, device, kind):
         for zi in range(0, nz, 64):  # chunk to bound temporaries
             blk = az[zi:zi + 64, None, None] * ay[None, :, None] * ax[None, None, :]
             f[zi:zi + 64] += amp * blk.real
+    return f
+
+
+def expected_modes(grid, modes):
+    """Analytic forward (unnormalised, e^{-i}) spectrum of the modes field at
+    the kept half (kx >= 0): amp N/2 e^{i ph} at k and amp N/2 e^{-i ph} at -k,
+    each stored at its kx >= 0 representative.  {(iz, iy, ix): complex}."""
+    nx, ny, nz = grid
+    half = nx * ny * nz / 2.0
+    want = {}
+    for k, amp, ph in modes:
+        for sgn in (1, -1):
+            kx, ky, kz = (sgn * v for v in k)
+            if kx < 0:
+                continue
+            idx = (kz % nz, ky % ny, kx)
+            want[idx] = want.get(idx, 0) + amp * half * np.exp(1j * sgn * ph)
+    return want
+
+
+def make_cheby_input(torch, grid, seed, device):
+    """The Chebyshev workload's field: z on the Gauss-Lobatto points
+    cos(pi (k-1)/(nz-1)), f = sum of 16 seeded sin(2 pi a x) cos(2 pi b y)
+    T_m(z) with a, b <= 64, m <= 128, plus U[-1e-6, 1e-6) noise."""
+    import math
+    nx, ny, nz = grid
+    rng = np.random.default_rng(seed)
+    xs = torch.arange(nx, device=device, dtype=torch.float64) / nx
+    ys = torch.arange(ny, device=device, dtype=torch.float64) / ny
+    zs = torch.cos(math.pi * torch.arange(nz, device=device, dtype=torch.float64) / (nz - 1))
+    f = torch.zeros((nz, ny, nx), dtype=torch.float64, device=device)
+    for _ in range(16):
+        a, b, m = int(rng.integers(0, 65)), int(rng.integers(0, 65)), int(rng.integers(0, 129))
+        tz = torch.cos(m * torch.arccos(zs.clamp(-1, 1)))  # T_m on the Lobatto points
+        f += (torch.sin(2 * math.pi * a * xs)[None, None, :] * torch.cos(2 * math.pi * b * ys)[None, :, None]
+              * tz[:, None, None])
+    g = torch.Generator(device=device)
+    g.manual_seed(seed + 1)
+    f += 1e-6 * (torch.rand(f.shape, generator=g, device=device, dtype=torch.float64) * 2 - 1)
     return f
 
 
@@ -191,6 +245,137 @@ def aggregate_gpts(world: int, points_per_replica: int, ms: float) -> float:
     return world * points_per_replica / (ms * 1e-3) / 1e9
 
 
+def rt_norm(grid, ops):
+    """Round-trip normalisation: N for FFTs, nx ny 2 (nz - 1) with DCT-I on z
+    (unnormalised REDFT00 twice) and nx ny 2 (nz + 1) with DST-I."""
+    nx, ny, nz = grid
+    z = ops[0][2]
+    if z == "c":
+        return nx * ny * 2 * (nz - 1)
+    if z == "s":
+        return nx * ny * 2 * (nz + 1)
+    if z in "n0":
+        return nx * ny
+    return nx * ny * nz
+
+
+def gpu_linf(a, w) -> float:
+    return float((a - w).abs().max() / w.abs().max())
+
+
+def gpu_rel_l2(torch, a, w) -> float:
+    return float(torch.linalg.vector_norm(a - w) / torch.linalg.vector_norm(w))
+
+
+def accuracy(torch, grid, ops, kind, x, plan64, plan32, stream, lz=None, seed=None):
+    """Outputs on the full grid against the CPU oracle (numpy/scipy FP64
+    restatement of the reference path, all host cores), outside any timed
+    region: forward and backward of the F64 path (normalised L-inf, bound
+    1e-12), of the F32 path (relative L2, bound 1e-6), the round trip under
+    the samples' rule, the analytic spectrum of the modes field, and
+    p3dfft_cheby for the Chebyshev workload."""
+    from oracle import p3dfft_oracle as orc
+    orc.WORKERS = os.cpu_count() or 1
+    t0 = time.time()
+    nx, ny, nz = grid
+    n = nx * ny * nz
+    dev = x.device
+    ref = orc.OraclePlan(nx, ny, nz)
+    a = x.cpu().numpy()
+    wb_np = ref.ftran_r2c(a, ops[0])
+    want_b = torch.from_numpy(wb_np).to(dev)
+    b64 = plan64.ftran_r2c(x, op=ops[0], stream=stream)
+    torch.cuda.synchronize()
+    out = {"f64_forward_normalised_linf_vs_oracle": gpu_linf(b64, want_b)}
+    if kind == "modes":
+        want = expected_modes(grid, modes_list(grid, seed))
+        idx = torch.tensor(list(want.keys()), device=dev)
+        got = b64[idx[:, 0], idx[:, 1], idx[:, 2]]
+        w = torch.tensor(list(want.values()), dtype=torch.complex128, device=dev)
+        # the N(0, 1e-3) noise adds ~1e-3 sqrt(N) per mode against amplitudes of ~N/2
+        out["f64_modes_max_rel_err"] = float(((got - w).abs() / w.abs()).max())
+        out["modes_checked"] = len(want)
+    r64 = plan64.btran_c2r(b64, op=ops[1], stream=stream)
+    want_r = torch.from_numpy(ref.btran_c2r(wb_np, ops[1])).to(dev)
+    torch.cuda.synchronize()
+    out["f64_backward_normalised_linf_vs_oracle"] = gpu_linf(r64, want_r)
+    rt = float((r64.div_(rt_norm(grid, ops)) - x).abs().max())
+    out["f64_roundtrip_max_abs"] = rt
+    out["f64_roundtrip_normalised_linf"] = rt / float(x.abs().max())
+    out["roundtrip_rule_f64"] = 1e-14 * n * 0.25
+    del r64
+    if lz is not None:
+        c = plan64.cheby(x, lz, stream=stream)
+        want_c = torch.from_numpy(ref.cheby(a, lz)).to(dev)
+        torch.cuda.synchronize()
+        out["f64_cheby_normalised_linf_vs_oracle"] = gpu_linf(c, want_c)
+        del c, want_c
+    del b64
+    if plan32 is not None:
+        b32 = plan32.ftran_r2c(x.float(), op=ops[0], stream=stream)
+        torch.cuda.synchronize()
+        out["f32_forward_rel_l2_vs_oracle"] = gpu_rel_l2(torch, b32.to(torch.complex128), want_b)
+        r32 = plan32.btran_c2r(want_b.to(torch.complex64), op=ops[1], stream=stream)
+        torch.cuda.synchronize()
+        out["f32_backward_rel_l2_vs_oracle"] = gpu_rel_l2(torch, r32.double(), want_r)
+        r32 = plan32.btran_c2r(b32, op=ops[1], stream=stream)
+        torch.cuda.synchronize()
+        rt32 = float((r32.double().div_(rt_norm(grid, ops)) - x).abs().max())
+        out["f32_roundtrip_max_abs"] = rt32
+        out["roundtrip_rule_f32"] = 1e-5 * n * 0.25
+        del b32, r32
+    out["oracle_threads"] = orc.WORKERS
+    out["oracle_s"] = round(time.time() - t0, 1)
+    del want_b, want_r, wb_np, a
+    return out
+
+
+def measure_config(torch, pg, name, args, dev, stream, seed, with_accuracy=True, clock=None):
+    """One workload: FP64 and FP32 round trips timed with CUDA events on the
+    plan's stream (the plan timers give the per-pass times; `clock`, a
+    ClockSampler, runs around the timed loops), then the outputs against the
+    oracle."""
+    import contextlib
+    clock = clock if clock is not None else contextlib.nullcontext()
+    cfg = CONFIGS[name]
+    grid, ops = cfg["grid"], cfg["ops"]
+    nx, ny, nz = grid
+    npts = nx * ny * nz
+    x = make_input(torch, grid, seed, dev, cfg["input"])
+    res = {"workload": cfg["workload"], "grid": list(grid), "ops": list(ops)}
+    plan = pg.Plan(nx, ny, nz, precision=pg.F64, timers=True)
+    plan.set_options(*MODES[args.mode])
+    b = torch.empty(plan.complex_shape, dtype=torch.complex128, device=dev)
+    r = torch.empty_like(x)
+    plan32 = pg.Plan(nx, ny, nz, precision=pg.F32)
+    plan32.set_options(*MODES[args.mode])
+    x32 = x.float()
+    b32 = torch.empty(plan32.complex_shape, dtype=torch.complex64, device=dev)
+    r32 = torch.empty_like(x32)
+    with clock:
+        ms64, launches = time_device(torch, plan, x, b, r, ops, args.steps, args.warmup, stream)
+        ms32, _ = time_device(torch, plan32, x32, b32, r32, ops, args.steps, args.warmup, stream)
+    timers = plan.timers()
+    del b, r, x32, b32, r32
+    peak, _ = load_peaks()
+    bm64, bm32 = bytes_model(grid, 8), bytes_model(grid, 4)
+    res.update({
+        "f64": {"value": round(npts / (ms64 * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_step": round(ms64, 4),
+                "step_frac_of_measured_hbm": round(bm64["rt"] / (ms64 * 1e-3) / 1e9 / peak, 4)},
+        "f32": {"value": round(npts / (ms32 * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_step": round(ms32, 4),
+                "step_frac_of_measured_hbm": round(bm32["rt"] / (ms32 * 1e-3) / 1e9 / peak, 4),
+                "speedup_vs_f64": round(ms64 / ms32, 3)},
+    })
+    if with_accuracy:
+        res["error"] = accuracy(torch, grid, ops, cfg["input"], x, plan, plan32, stream,
+                                lz=2.0 if name == "cheby" else None, seed=seed)
+    plan.close()
+    plan32.close()
+    del x
+    torch.cuda.empty_cache()
+    return res, ms64, ms32, timers, launches
+
+
 def run_ours(args):
     import torch
     import p3dfft_gb300 as pg
@@ -214,30 +399,17 @@ def run_ours(args):
     # every torch op and every plan call below runs on one stream
     ctx = torch.cuda.stream(stream)
     ctx.__enter__()
+    seed = 1234 + rank
 
-    # ---- FP64 (headline)
-    plan = pg.Plan(nx, ny, nz, precision=pg.F64, timers=True)
-    plan.set_options(*MODES[args.mode])
-    kind = "uniform" if args.config == "small" else "modes"
-    x = make_input(torch, grid, 1234 + rank, dev, kind)
-    b = torch.empty(plan.complex_shape, dtype=torch.complex128, device=dev)
-    r = torch.empty_like(x)
+    # ---- FP64 (headline) and FP32 on the same grid, timed with clocks sampled
     if dist:
         dist.barrier()
-    with ClockSampler(local) as clk:
-        ms64, launches = time_device(torch, plan, x, b, r, ops, args.steps, args.warmup, stream)
+    clk = ClockSampler(local)
+    head, ms64, ms32, timers, launches = measure_config(torch, pg, args.config, args, dev, stream, seed,
+                                                        with_accuracy=False, clock=clk)
     ms64 = max_over_ranks(torch, dist, ms64, dev)
-    timers = plan.timers()
-    # per-pass kernel times over the timed steps (plan timers: slots 5,7,8,9,10,12)
+    ms32 = max_over_ranks(torch, dist, ms32, dev)
     bm = bytes_model(grid, 8)
-    scale = 1.0 / nx / ny / nz
-    # accuracy on the full grid: round trip, and F32 vs F64 forward below
-    plan.ftran_r2c(x, b, op=ops[0], stream=stream)
-    fwd64 = b.clone()
-    b.mul_(scale)
-    plan.btran_c2r(b, r, op=ops[1], stream=stream)
-    torch.cuda.synchronize()
-    rt_err = float((r - x).abs().max() / x.abs().max())
     pass_ms = {
         "x_r2c": timers[4] * 1e3 / args.steps, "y_fwd": timers[6] * 1e3 / args.steps,
         "z_fwd": timers[7] * 1e3 / args.steps, "z_bwd": timers[8] * 1e3 / args.steps,
@@ -257,30 +429,35 @@ def run_ours(args):
     traffic = None
     if dom in TRAFFIC_PER_ALGO_BYTE:
         traffic = int(TRAFFIC_PER_ALGO_BYTE[dom] * dom_bytes)
-    del r
-    plan.close()
 
-    # ---- FP32 form on the same grid
-    plan32 = pg.Plan(nx, ny, nz, precision=pg.F32)
-    plan32.set_options(*MODES[args.mode])
-    x32 = x.float()
-    b32 = torch.empty(plan32.complex_shape, dtype=torch.complex64, device=dev)
-    r32 = torch.empty_like(x32)
-    ms32, _ = time_device(torch, plan32, x32, b32, r32, ops, args.steps, args.warmup, stream)
-    plan32.ftran_r2c(x32, b32, op=ops[0], stream=stream)
-    torch.cuda.synchronize()
-    diff = (b32.to(torch.complex128) - fwd64)
-    err32 = float(torch.linalg.vector_norm(diff) / torch.linalg.vector_norm(fwd64))
-    del b32, r32, x32, diff, fwd64
-    plan32.close()
-    ms32 = max_over_ranks(torch, dist, ms32, dev)
+    # ---- accuracy of the headline workload against the oracle (not timed)
+    error = None
+    x = None
+    if not args.skip_accuracy:
+        plan = pg.Plan(nx, ny, nz, precision=pg.F64)
+        plan32 = pg.Plan(nx, ny, nz, precision=pg.F32)
+        x = make_input(torch, grid, seed, dev, cfg["input"])
+        error = accuracy(torch, grid, ops, cfg["input"], x, plan, plan32, stream,
+                         lz=2.0 if args.config == "cheby" else None, seed=seed)
+        plan.close()
+        plan32.close()
 
     # ---- end to end through the drop-in C-ABI with pinned host buffers
     e2e = None
     if not args.skip_e2e:
+        if x is None:
+            x = make_input(torch, grid, seed, dev, cfg["input"])
         e2e = run_e2e(torch, pg, grid, ops, x, max(1, args.steps // 2), dev)
-    del x, b
+    del x
     torch.cuda.empty_cache()
+
+    # ---- the other configured workloads, each timed and checked against the oracle
+    configs = {}
+    if not args.skip_configs:
+        for name in ("noncubic", "cheby", "small"):
+            if name == args.config:
+                continue
+            configs[name] = measure_config(torch, pg, name, args, dev, stream, seed)[0]
     batched = serving = None
     if not args.skip_forms:
         batched = run_batched(torch, pg, dev, args.steps, args.warmup, npts / (ms64 * 1e-3) / 1e9)
@@ -295,10 +472,10 @@ def run_ours(args):
                    "arithmetic": "binary64 I/O, double-float (2 x binary32) butterflies",
                    "l2": "inputs larger than L2 (8 GB per field), no flush needed",
                    "parallelism": f"replicas x{world}"},
-        "error": {"f64_roundtrip_normalised_linf": rt_err,
-                  "f32_forward_rel_l2_vs_f64": err32},
+        "error": error,
         "f32": {"value": round(aggregate_gpts(world, npts, ms32), 3), "unit": UNIT, "ms_per_step": round(ms32, 4),
-                "rel_l2_vs_f64": err32, "speedup_vs_f64": round(ms64 / ms32, 3)},
+                "speedup_vs_f64": round(ms64 / ms32, 3),
+                "step_frac": round(bytes_model(grid, 4)["rt"] / (ms32 * 1e-3) / 1e9 / peak, 4)},
         "passes_ms": {k: round(v, 4) for k, v in pass_ms.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "launches_per_step": nl,
                      "algorithmic_bytes_per_launch": int(dom_bytes),
@@ -316,6 +493,8 @@ def run_ours(args):
     }
     if e2e:
         line["e2e"] = e2e
+    if configs:
+        line["configs"] = configs
     if batched:
         line["batched"] = batched
     if serving:
@@ -505,39 +684,38 @@ def run_e2e(torch, pg, grid, ops, x_dev, steps, dev):
 
 
 # ------------------------------------------------------------ CPU arms
-def cpu_sample_grid(args):
-    return (256, 256, 256) if args.config in ("large", "noncubic") else CONFIGS[args.config]["grid"]
-
-
-def cpu_round_trips(grid, ops, seconds, max_steps=None):
+def cpu_round_trips(grid, ops, seconds, max_steps=None, warmup=1):
+    """Round trips of the whole grid through the oracle port on every host
+    core (U[-1,1) input: the FFT's time does not depend on the values)."""
     from oracle import p3dfft_oracle as orc
     orc.WORKERS = os.cpu_count() or 1
     nx, ny, nz = grid
     a = np.random.default_rng(7).uniform(-1, 1, size=(nz, ny, nx))
     p = orc.OraclePlan(nx, ny, nz)
-    b = p.ftran_r2c(a, ops[0])  # warm-up (plans, page faults)
-    p.btran_c2r(b, ops[1])
+    for _ in range(warmup):  # plans, page faults
+        p.btran_c2r(p.ftran_r2c(a, ops[0]), ops[1])
     n = 0
     t0 = time.perf_counter()
     while True:
         b = p.ftran_r2c(a, ops[0])
         p.btran_c2r(b, ops[1])
+        del b
         n += 1
         el = time.perf_counter() - t0
-        if el >= seconds or (max_steps and n >= max_steps):
+        if (max_steps and n >= max_steps) or (not max_steps and el >= seconds):
             break
     return n, el, orc.WORKERS
 
 
 def cpu_baseline(args):
-    grid = cpu_sample_grid(args)
+    grid = CONFIGS[args.config]["grid"]
     ops = CONFIGS[args.config]["ops"]
     n, el, cores = cpu_round_trips(grid, ops, seconds=args.cpu_seconds)
     pts = grid[0] * grid[1] * grid[2]
     return {"value": round(pts * n / el / 1e9, 4), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{n} FP64 r2c+c2r round trips of {grid[0]}x{grid[1]}x{grid[2]} (oracle: numpy/scipy "
-                      f"pocketfft restatement of the reference path, scipy.fft workers={cores}); the FFTW+MPI "
-                      f"reference does not build here (no Fortran/MPI/FFTW)"}
+            "sample": f"{n} FP64 r2c+c2r round trips of the whole {grid[0]}x{grid[1]}x{grid[2]} grid after one "
+                      f"untimed (oracle: numpy/scipy pocketfft restatement of the reference path, scipy.fft "
+                      f"workers={cores}); the FFTW+MPI reference does not build here (no Fortran/MPI/FFTW)"}
 
 
 def run_reference(args):
@@ -545,23 +723,22 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    grid = cpu_sample_grid(args)
+    grid = CONFIGS[args.config]["grid"]
     ops = CONFIGS[args.config]["ops"]
-    for _ in range(args.warmup):
-        cpu_round_trips(grid, ops, seconds=0, max_steps=1)
-    n, el, cores = cpu_round_trips(grid, ops, seconds=0, max_steps=args.steps)
+    n, el, cores = cpu_round_trips(grid, ops, seconds=0, max_steps=args.steps, warmup=args.warmup)
     pts = grid[0] * grid[1] * grid[2]
     value = pts * n / el / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / n * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": CONFIGS[args.config]["workload"], "sample_grid": list(grid),
+        "config": {"workload": CONFIGS[args.config]["workload"], "grid": list(grid), "sample_grid": list(grid),
                    "ops": list(ops)},
         "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"each step one FP64 round trip of {grid[0]}x{grid[1]}x{grid[2]} through the "
-                                   f"oracle port (scipy.fft, {cores} threads); the FFTW+MPI reference does not "
-                                   f"build here"},
+                         "sample": f"each step one FP64 round trip of the whole {grid[0]}x{grid[1]}x{grid[2]} "
+                                   f"grid through the oracle port (scipy.fft, {cores} threads; U[-1,1) input, "
+                                   f"the FFT's time does not depend on the values); the FFTW+MPI reference does "
+                                   f"not build here"},
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -580,6 +757,8 @@ def main():
     ap.add_argument("--skip-forms", action="store_true", help="skip the batched and serving forms")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-accuracy", action="store_true", help="skip the oracle comparisons of the headline grid")
+    ap.add_argument("--skip-configs", action="store_true", help="skip the other configured workloads")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
     if args.impl == "reference":

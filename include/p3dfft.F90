@@ -29,7 +29,7 @@ module p3dfft
   real(r8), save, public :: timers(12) = 0.0_r8
 
   public :: p3dfft_setup, p3dfft_get_dims, p3dfft_get_mpi_info
-  public :: p3dfft_ftran_r2c, p3dfft_btran_c2r, p3dfft_cheby
+  public :: p3dfft_ftran_r2c, p3dfft_btran_c2r, p3dfft_cheby, p3dfft_ftran_r2c_1d
   public :: p3dfft_ftran_r2c_many, p3dfft_btran_c2r_many, p3dfft_cheby_many
   public :: p3dfft_clean, get_timers, set_timers
 
@@ -72,6 +72,11 @@ module p3dfft
       real(p3dfft_type) :: b(*)
       character(kind=c_char) :: op(*)
     end subroutine c_btran_many
+    subroutine c_ftran_1d(a, b) bind(C, name='p3dfft_ftran_r2c_1d')
+      import :: p3dfft_type
+      real(p3dfft_type) :: a(*)
+      real(p3dfft_type) :: b(*)
+    end subroutine c_ftran_1d
     subroutine c_cheby(a, b, lz) bind(C, name='p3dfft_cheby')
       import :: p3dfft_type
       real(p3dfft_type) :: a(*)
@@ -184,6 +189,13 @@ contains
   end subroutine p3dfft_btran_c2r_many
 
   ! ftran.F90:383-464: 'ffc' transform, scaling and the derivative recurrence
+  ! ftran.F90:787-814: the X r2c alone; cXgYZ holds nx/2+1 complexes per line
+  subroutine p3dfft_ftran_r2c_1d(rXgYZ, cXgYZ)
+    real(p3dfft_type), intent(in) :: rXgYZ(*)
+    real(p3dfft_type), intent(inout) :: cXgYZ(*)
+    call c_ftran_1d(rXgYZ, cXgYZ)
+  end subroutine p3dfft_ftran_r2c_1d
+
   subroutine p3dfft_cheby(XgYZ, XYZg, Lz)
     real(p3dfft_type), intent(in) :: XgYZ(*)
     complex(p3dfft_type), intent(inout) :: XYZg(*)

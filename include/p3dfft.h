@@ -47,6 +47,9 @@ extern void FORT_MOD_NAME(p3dfft_ftran_r2c_many)(p3dfft_real_t* A, int* dim_in, 
 extern void FORT_MOD_NAME(p3dfft_btran_c2r)(p3dfft_real_t* A, p3dfft_real_t* B, unsigned char* op);
 extern void FORT_MOD_NAME(p3dfft_btran_c2r_many)(p3dfft_real_t* A, int* dim_in, p3dfft_real_t* B, int* dim_out,
                                                  int* nv, unsigned char* op);
+/* ftran.F90:787 (a module routine of the reference without a C prototype in
+ * its header): the X r2c alone, real (nx, ny, nz) -> complex (nx/2+1, ny, nz) */
+extern void FORT_MOD_NAME(p3dfft_ftran_r2c_1d)(p3dfft_real_t* rXgYZ, p3dfft_real_t* cXgYZ);
 /* ftran.F90:359, :321 */
 extern void FORT_MOD_NAME(p3dfft_cheby)(p3dfft_real_t* A, p3dfft_real_t* B, p3dfft_real_t* Lz);
 extern void FORT_MOD_NAME(p3dfft_cheby_many)(p3dfft_real_t* A, int* dim_in, p3dfft_real_t* B, int* dim_out,

@@ -88,6 +88,12 @@ int p3g_ftran_r2c_to_host(p3g_plan plan, const void* in, void* out_host, void* s
 int p3g_btran_c2r_from_host(p3g_plan plan, const void* in_host, void* stage, void* out, const char* op, int chunks,
                             void* stream, void* copy_stream);
 
+/* p3dfft_ftran_r2c_1d (reference build/ftran.F90:787-814): the real-to-
+ * complex X transform alone, every (y, z) line of the real field in to
+ * nx/2+1 complexes per line out, lines packed (complex (nx/2+1, ny, nz),
+ * user format), unnormalised and not pruned. */
+int p3g_ftran_r2c_1d(p3g_plan plan, const void* in, void* out, void* stream);
+
 /* p3dfft_cheby (reference build/ftran.F90:321-464): 'ffc' transform, scaling
  * by 1/(nx*ny*(nzc-1)) and the Chebyshev-derivative recurrence along z with
  * factor 4/lz. */
@@ -172,8 +178,8 @@ long long p3g_plan_device_bytes(p3g_plan plan);
 /* Kernel launches issued by this plan since creation. */
 long long p3g_plan_launches(p3g_plan plan);
 
-/* Allocation-free forward transform (one field, XYZ layout, single-tile
- * kernels).  No counterpart in the reference.  For callers that must not
+/* Allocation-free forward transform (one field, XYZ or STRIDE1 layout,
+ * single-tile kernels).  No counterpart in the reference.  For callers that must not
  * allocate device memory after start-up (fixed-budget serving workers,
  * frameworks that route every allocation through their own pool, loops that
  * cannot afford cudaMalloc's device synchronisation): the workspace is a

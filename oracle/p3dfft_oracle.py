@@ -169,8 +169,8 @@ class OraclePlan:
         """Z transform selected by one op letter, along axis 0 (ftran.F90:620-643)."""
         if ch in ("t", "f"):
             if forward:
-                return sfft.fft(a, axis=0, workers=WORKERS)
-            return sfft.ifft(a, axis=0, norm="forward", workers=WORKERS)
+                return sfft.fft(a, axis=0, workers=WORKERS, overwrite_x=True)
+            return sfft.ifft(a, axis=0, norm="forward", workers=WORKERS, overwrite_x=True)
         if ch == "c":  # REDFT00 on re and im parts (fft_exec.F90:646-701)
             if a.shape[0] < 2:
                 raise OracleError("DCT-I needs nz >= 2")
@@ -190,22 +190,30 @@ class OraclePlan:
             raise OracleError(f"input shape {x.shape} != {(self.nz, self.ny, self.nx)}")
         # X r2c into buf2 (ftran.F90:525-534)
         buf2 = sfft.rfft(x, axis=2, workers=WORKERS)
-        # seg_copy_x keeps x modes 1..nxhpc (ftran.F90:554)
+        # seg_copy_x keeps x modes 1..nxhpc (ftran.F90:554); a copy only when pruned
         buf = np.ascontiguousarray(buf2[:, :, : self.nxhpc])
+        del buf2
         # Y c2c per z-plane (ftran.F90:576-584)
-        buf = sfft.fft(buf, axis=1, workers=WORKERS)
+        buf = sfft.fft(buf, axis=1, workers=WORKERS, overwrite_x=True)
         # seg_copy_y: y = 1..nycph from y, y = nycph+1..nyc from y+dny (ftran.F90:736-738)
         dny = self.ny - self.nyc
-        b1 = np.empty((self.nz, self.nyc, self.nxhpc), dtype=np.complex128)
-        b1[:, : self.nycph] = buf[:, : self.nycph]
-        b1[:, self.nycph:] = buf[:, self.nycph + dny: self.nyc + dny]
+        if dny == 0:
+            b1 = buf  # the identity copy
+        else:
+            b1 = np.empty((self.nz, self.nyc, self.nxhpc), dtype=np.complex128)
+            b1[:, : self.nycph] = buf[:, : self.nycph]
+            b1[:, self.nycph:] = buf[:, self.nycph + dny: self.nyc + dny]
+        del buf
         # Z op over the full nz (ftran.F90:740-763)
         b1 = self._zop(b1, op[2], forward=True)
         # seg_copy_z: z = 1..nzcph from z, z = nzcph+1..nzc from z+dnz (ftran.F90:705-706)
         dnz = self.nz - self.nzc
-        out = np.empty((self.nzc, self.nyc, self.nxhpc), dtype=np.complex128)
-        out[: self.nzcph] = b1[: self.nzcph]
-        out[self.nzcph:] = b1[self.nzcph + dnz: self.nzc + dnz]
+        if dnz == 0:
+            out = b1
+        else:
+            out = np.empty((self.nzc, self.nyc, self.nxhpc), dtype=np.complex128)
+            out[: self.nzcph] = b1[: self.nzcph]
+            out[self.nzcph:] = b1[self.nzcph + dnz: self.nzc + dnz]
         if self.stride1:
             out = np.ascontiguousarray(out.transpose(2, 1, 0))
         return out
@@ -229,10 +237,10 @@ class OraclePlan:
             c = c.transpose(2, 1, 0)
         if c.shape != (self.nzc, self.nyc, self.nxhpc):
             raise OracleError(f"input shape {c.shape} != {(self.nzc, self.nyc, self.nxhpc)}")
-        c = c.astype(np.complex128)
         nz, ny, nzc, nyc = self.nz, self.ny, self.nzc, self.nyc
         dnz = nz - nzc
-        # seg_copy_z low, seg_copy_z high, seg_zero_z (btran.F90:553-555)
+        # seg_copy_z low, seg_copy_z high, seg_zero_z (btran.F90:553-555); the
+        # input is never modified (every path below works on a copy)
         buf1 = np.empty((nz, nyc, self.nxhpc), dtype=np.complex128)
         buf1[: self.nzcph] = c[: self.nzcph]
         buf1[nz - self.nzcph:] = c[nz - self.nzcph - dnz: nz - dnz]
@@ -240,17 +248,25 @@ class OraclePlan:
         buf1 = self._zop(buf1, op[0], forward=False)
         # seg_copy_y low/high + seg_zero_y (btran.F90:585-588)
         dny = ny - nyc
-        buf = np.empty((nz, ny, self.nxhpc), dtype=np.complex128)
-        buf[:, : self.nycph] = buf1[:, : self.nycph]
-        buf[:, ny - self.nycph:] = buf1[:, ny - self.nycph - dny: ny - dny]
-        buf[:, self.nycph: ny - self.nycph] = 0
+        if dny == 0:
+            buf = buf1
+        else:
+            buf = np.empty((nz, ny, self.nxhpc), dtype=np.complex128)
+            buf[:, : self.nycph] = buf1[:, : self.nycph]
+            buf[:, ny - self.nycph:] = buf1[:, ny - self.nycph - dny: ny - dny]
+            buf[:, self.nycph: ny - self.nycph] = 0
+        del buf1
         # Y c2c backward (btran.F90:615-624)
-        buf = sfft.ifft(buf, axis=1, norm="forward", workers=WORKERS)
+        buf = sfft.ifft(buf, axis=1, norm="forward", workers=WORKERS, overwrite_x=True)
         # seg_copy_x + seg_zero_x (btran.F90:662-663)
-        b1 = np.zeros((nz, ny, self.nxhp), dtype=np.complex128)
-        b1[:, :, : self.nxhpc] = buf
+        if self.nxhpc == self.nxhp:
+            b1 = buf
+        else:
+            b1 = np.zeros((nz, ny, self.nxhp), dtype=np.complex128)
+            b1[:, :, : self.nxhpc] = buf
+        del buf
         # X c2r (btran.F90:665-670), unnormalised
-        return sfft.irfft(b1, n=self.nx, axis=2, norm="forward", workers=WORKERS)
+        return sfft.irfft(b1, n=self.nx, axis=2, norm="forward", workers=WORKERS, overwrite_x=True)
 
     def cheby(self, x: np.ndarray, lz: float) -> np.ndarray:
         """p3dfft_cheby, ftran.F90:383-464: 'ffc' transform, 1/(nx*ny*(nzc-1))

@@ -25,6 +25,7 @@ from . import _lib
 __all__ = [
     "P3DFFTError", "Plan", "F64", "F32", "p3dfft_setup", "p3dfft_get_dims", "p3dfft_get_mpi_info",
     "p3dfft_ftran_r2c", "p3dfft_btran_c2r", "p3dfft_ftran_r2c_many", "p3dfft_btran_c2r_many",
+    "p3dfft_ftran_r2c_1d",
     "p3dfft_cheby", "p3dfft_cheby_many", "p3dfft_clean", "get_timers", "set_timers",
 ]
 
@@ -137,6 +138,14 @@ class Plan:
             out = torch.empty(shape, dtype=self._dtypes()[0], device=c.device)
         _check(_core().p3g_btran_c2r(self._h, _ptr(c), _ptr(out), op.encode(), nv, dim_in, dim_out,
                                      _stream_ptr(stream)))
+        return out
+
+    def ftran_r2c_1d(self, x, out=None, stream=None):
+        """The X r2c alone (p3g_ftran_r2c_1d): complex (nz, ny, nx//2+1), every mode."""
+        if out is None:
+            import torch
+            out = torch.empty((self.nz, self.ny, self.nx // 2 + 1), dtype=self._dtypes()[1], device=x.device)
+        _check(_core().p3g_ftran_r2c_1d(self._h, _ptr(x), _ptr(out), _stream_ptr(stream)))
         return out
 
     def cheby(self, x, lz, out=None, nv=1, dim_in=0, dim_out=0, stream=None):
@@ -392,6 +401,15 @@ def p3dfft_btran_c2r_many(XYZg, dim_in, XgYZ, dim_out, nv, op="tff"):
                                     ctypes.byref(_ci(nv)), op.encode())
     _legacy_check()
     return XgYZ
+
+
+def p3dfft_ftran_r2c_1d(rXgYZ, cXgYZ):
+    """ftran.F90:787-814: the X r2c alone, real (nz, ny, nx) -> complex (nz, ny, nx//2+1)."""
+    _check_host(rXgYZ)
+    _check_host(cXgYZ, True)
+    _legacy().p3dfft_ftran_r2c_1d(_ptr(rXgYZ), _ptr(cXgYZ))
+    _legacy_check()
+    return cXgYZ
 
 
 def _lz_arg(lz):

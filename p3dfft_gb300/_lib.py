@@ -29,6 +29,7 @@ CORE_SIGNATURES = {
                                      ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_void_p]),
     "p3g_cheby": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                  ctypes.c_longlong, ctypes.c_longlong, ctypes.c_void_p]),
+    "p3g_ftran_r2c_1d": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "p3g_get_timers": (ctypes.c_int, [ctypes.c_void_p, _c_double_p]),
     "p3g_set_timers": (ctypes.c_int, [ctypes.c_void_p]),
     "p3g_plan_device_bytes": (ctypes.c_longlong, [ctypes.c_void_p]),
@@ -72,6 +73,7 @@ LEGACY_SIGNATURES = {
                                      ctypes.c_char_p]),
     "p3dfft_btran_c2r_many": (None, [ctypes.c_void_p, _c_int_p, ctypes.c_void_p, _c_int_p, _c_int_p,
                                      ctypes.c_char_p]),
+    "p3dfft_ftran_r2c_1d": (None, [ctypes.c_void_p, ctypes.c_void_p]),
     "p3dfft_cheby": (None, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "p3dfft_cheby_many": (None, [ctypes.c_void_p, _c_int_p, ctypes.c_void_p, _c_int_p, _c_int_p,
                                  ctypes.c_void_p]),

@@ -26,7 +26,8 @@ OBJ = os.path.join(OUT, "obj")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 CORE_SOURCES = ["p3g_kernels_f64.cu", "p3g_kernels_f32.cu", "p3g_plan.cu", "p3g_noalloc.cu", "p3g_spectrum.cu",
-                "p3g_batch.cu"]
+                "p3g_batch.cu", "p3g_batch_f64_128.cu", "p3g_batch_f64_256.cu", "p3g_batch_f32_128.cu",
+                "p3g_batch_f32_256.cu"]
 LEGACY_SOURCE = "p3g_legacy.cpp"
 LIBS = {
     "core": "libp3dfft_gb300.so",

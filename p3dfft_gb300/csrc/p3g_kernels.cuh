@@ -22,6 +22,7 @@ struct XParams {
   int tiles;                      // tiles per field
   int LS;                         // shared-memory stride between line pairs (>= padded N)
   int ps;                         // line padding shift (see pad_index), 0 = none
+  int out_user;                   // r2c: 1 stores the user complex format (X-only transform)
 };
 
 // Strided Y/Z passes: a tile is M consecutive x columns of one (o1, o2) row
@@ -32,9 +33,11 @@ struct SParams {
   const void* in;
   void* out;
   int in_user, out_user;  // 1: user complex format, 0: workspace format
-  // per-element strides (along the axis, between x columns: 1, or nyc*nzc
-  // for the STRIDE1 user layout) are below 2^31, checked at plan creation;
-  // row (o1) and field (o2) strides are 64-bit
+  // single per-element strides (along the axis, between x columns: 1, or
+  // nyc*nzc for the STRIDE1 user layout) are 32-bit and below 2^31 (plan
+  // creation checks the strides themselves); the kernels form their products
+  // with row and column indices, which span the whole field, in 64 bits.
+  // Row (o1) and field (o2) strides are 64-bit
   int in_axis, out_axis;
   int in_xs, out_xs;
   long long in_o1, in_o2;
@@ -100,6 +103,11 @@ P3G_D void store_elem(void* base, int user, long long idx, typename P::C v) {
 // complexes per line, rounded up to even for 8-byte elements so that two
 // complexes move with one 16-byte copy.
 P3G_HD int xc2r_raw_stride(int nh, int esize) { return esize == 8 ? (nh + 1) & ~1 : nh; }
+
+// Raises a kernel's dynamic shared-memory limit to `bytes` once per device:
+// the attribute belongs to the device that is current when it is set, so a
+// process that launches on several GPUs sets it on each (thread-safe).
+cudaError_t opt_in_smem(const void* func, int bytes);
 
 // Launchers (one per path).  Return the cudaError_t of the launch.
 template <class P>

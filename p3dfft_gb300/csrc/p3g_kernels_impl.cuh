@@ -33,7 +33,6 @@ P3G_D void x_r2c_tile(const XParams& prm, const StagePlan* __restrict__ sp, cons
   const int M = prm.M;
   const int p0 = tile * M;  // first pair of the tile
   const auto* in = static_cast<const typename P::UR*>(prm.in) + field * prm.in_field;
-  W* out = static_cast<W*>(prm.out) + field * prm.out_field;
 
   float* smf = reinterpret_cast<float*>(sm);
   constexpr int kW = sizeof(W) / sizeof(float);  // floats per element: 4 (F64) or 2 (F32)
@@ -55,17 +54,7 @@ P3G_D void x_r2c_tile(const XParams& prm, const StagePlan* __restrict__ sp, cons
   __syncthreads();
   Tile<P> t{sm, sm + M * LS, M, prm.log2m, LS, 1, ps};
   cta_fft<P, -1, kElemsPerThread, kLineMajor>(t, sp, tw);
-  const int nk = prm.nkeep;
-  for (int e = threadIdx.x; e < M * nk; e += blockDim.x) {
-    const int pr = e / nk;
-    const int k = e - pr * nk;
-    const int line = 2 * (p0 + pr);
-    if (line >= prm.nlines) continue;
-    const C a = P::from_w(sm[pr * LS + pad_index(k, ps)]);
-    const C b = cconj(P::from_w(sm[pr * LS + pad_index(k == 0 ? 0 : N - k, ps)]));
-    out[(long long)line * prm.out_line + k] = P::to_w(cscale2(a + b, 0.5f));
-    if (line + 1 < prm.nlines) out[(long long)(line + 1) * prm.out_line + k] = P::to_w(cscale2(rot<-1>(a - b), 0.5f));
-  }
+  xr2c_store<P>(prm, sm, p0, field);
 }
 
 template <class P>
@@ -148,8 +137,10 @@ P3G_D void strided_tile(const SParams& prm, const StagePlan* __restrict__ sp, co
   const int o1 = (int)(bid % prm.O1);
   const int o2 = (int)(bid / prm.O1);
   const int x0 = xt * M;
-  const long long ibase = (long long)o1 * prm.in_o1 + (long long)o2 * prm.in_o2 + x0 * prm.in_xs;
-  const long long obase = (long long)o1 * prm.out_o1 + (long long)o2 * prm.out_o2 + x0 * prm.out_xs;
+  // per-element strides are 32-bit; their products with row and column
+  // indices span the whole field and are formed in 64 bits
+  const long long ibase = (long long)o1 * prm.in_o1 + (long long)o2 * prm.in_o2 + (long long)x0 * prm.in_xs;
+  const long long obase = (long long)o1 * prm.out_o1 + (long long)o2 * prm.out_o2 + (long long)x0 * prm.out_xs;
 
   if (prm.pre == 2 && threadIdx.x < M) {  // DST-I odd extension: zero rows 0 and L+1
     sm[threadIdx.x] = P::to_w(P::zero());
@@ -171,7 +162,7 @@ P3G_D void strided_tile(const SParams& prm, const StagePlan* __restrict__ sp, co
     const int src = j >= prm.lmap_a1 ? j - prm.lmap_d : (j < prm.lmap_a0 ? j : -1);
     C v = P::zero();
     if (x0 + m < prm.X && src >= 0)
-      v = load_elem<P, CG>(prm.in, prm.in_user, ibase + m * prm.in_xs + src * prm.in_axis);
+      v = load_elem<P, CG>(prm.in, prm.in_user, ibase + (long long)m * prm.in_xs + (long long)src * prm.in_axis);
     if (prm.pre == 0) {
       sm[j * M + m] = P::to_w(v);
     } else if (prm.pre == 1) {
@@ -201,7 +192,7 @@ P3G_D void strided_tile(const SParams& prm, const StagePlan* __restrict__ sp, co
     C v;
     if (prm.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
     else v = P::from_w(sm[k * M + m]);
-    store_elem<P>(prm.out, prm.out_user, obase + m * prm.out_xs + jo * prm.out_axis, v);
+    store_elem<P>(prm.out, prm.out_user, obase + (long long)m * prm.out_xs + (long long)jo * prm.out_axis, v);
   }
 }
 
@@ -247,34 +238,25 @@ __global__ void k_cheby(const ChebyParams prm) {
 template <class P>
 cudaError_t launch_x_r2c(const XParams& p, const StagePlan* sp, const float4* tw, int threads, size_t smem,
                          int nfields, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_x_r2c<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr = true;
-  }
+  cudaError_t ea = opt_in_smem((const void*)k_x_r2c<P>, 227 * 1024);
+  if (ea != cudaSuccess) return ea;
   k_x_r2c<P><<<dim3(p.tiles, nfields), threads, smem, st>>>(p, sp, tw);
   return cudaGetLastError();
 }
 template <class P>
 cudaError_t launch_x_c2r(const XParams& p, const StagePlan* sp, const float4* tw, int threads, size_t smem,
                          int nfields, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_x_c2r<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr = true;
-  }
+  cudaError_t ea = opt_in_smem((const void*)k_x_c2r<P>, 227 * 1024);
+  if (ea != cudaSuccess) return ea;
   k_x_c2r<P><<<dim3(p.tiles, nfields), threads, smem, st>>>(p, sp, tw);
   return cudaGetLastError();
 }
 template <class P>
 cudaError_t launch_strided(const SParams& p, const StagePlan* sp, const float4* tw, bool forward_sign, int threads,
                            size_t smem, int nfields, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_strided<P, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_strided<P, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr = true;
-  }
+  cudaError_t ea = opt_in_smem((const void*)k_strided<P, -1>, 227 * 1024);
+  if (ea == cudaSuccess) ea = opt_in_smem((const void*)k_strided<P, 1>, 227 * 1024);
+  if (ea != cudaSuccess) return ea;
   const long long blocks = (long long)p.xtiles * p.O1 * nfields;
   if (blocks <= 0 || blocks > 0x7FFFFFFFLL) return cudaErrorInvalidConfiguration;
   if (forward_sign) k_strided<P, -1><<<(unsigned)blocks, threads, smem, st>>>(p, sp, tw);
@@ -291,12 +273,9 @@ cudaError_t launch_cheby(const ChebyParams& p, int nfields, cudaStream_t st) {
 template <class P>
 cudaError_t launch_strided_pipe(const CUtensorMap* map, const SPipeParams& p, const StagePlan* sp, const float4* tw,
                                 bool forward_sign, int E, int threads, size_t smem, int grid, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_strided_pipe<P, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_strided_pipe<P, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr = true;
-  }
+  cudaError_t ea = opt_in_smem((const void*)k_strided_pipe<P, -1>, 227 * 1024);
+  if (ea == cudaSuccess) ea = opt_in_smem((const void*)k_strided_pipe<P, 1>, 227 * 1024);
+  if (ea != cudaSuccess) return ea;
   (void)E;
   if (forward_sign) k_strided_pipe<P, -1><<<grid, threads, smem, st>>>(*map, p, sp, tw);
   else k_strided_pipe<P, 1><<<grid, threads, smem, st>>>(*map, p, sp, tw);
@@ -305,11 +284,8 @@ cudaError_t launch_strided_pipe(const CUtensorMap* map, const SPipeParams& p, co
 template <class P>
 cudaError_t launch_xr2c_pipe(const XPipeParams& p, const StagePlan* sp, const float4* tw, int E, int threads,
                              size_t smem, int grid, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_xr2c_pipe<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr = true;
-  }
+  cudaError_t ea = opt_in_smem((const void*)k_xr2c_pipe<P>, 227 * 1024);
+  if (ea != cudaSuccess) return ea;
   (void)E;
   k_xr2c_pipe<P><<<grid, threads, smem, st>>>(p, sp, tw);
   return cudaGetLastError();
@@ -317,11 +293,8 @@ cudaError_t launch_xr2c_pipe(const XPipeParams& p, const StagePlan* sp, const fl
 template <class P>
 cudaError_t launch_xc2r_pipe(const XPipeParams& p, const StagePlan* sp, const float4* tw, int E, int threads,
                              size_t smem, int grid, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_xc2r_pipe<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr = true;
-  }
+  cudaError_t ea = opt_in_smem((const void*)k_xc2r_pipe<P>, 227 * 1024);
+  if (ea != cudaSuccess) return ea;
   (void)E;
   k_xc2r_pipe<P><<<grid, threads, smem, st>>>(p, sp, tw);
   return cudaGetLastError();
@@ -333,9 +306,9 @@ template <class P>
 int pipe_blocks_per_sm(int kind, int threads, size_t smem) {
   const void* f = kind == 0 ? (const void*)k_strided_pipe<P, -1>
                             : (kind == 1 ? (const void*)k_xr2c_pipe<P> : (const void*)k_xc2r_pipe<P>);
-  cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem) != cudaSuccess || n < 1) {
+  if (opt_in_smem(f, 227 * 1024) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem) != cudaSuccess || n < 1) {
     cudaGetLastError();
     return 1;
   }

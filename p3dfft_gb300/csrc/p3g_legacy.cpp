@@ -282,6 +282,14 @@ void p3dfft_btran_c2r_many(real_t* A, int* dim_in, real_t* B, int* dim_out, int*
       [&](const void* i, void* out) { return p3g_btran_c2r(g_plan, i, out, o, n, di, dout, g_stream); });
 }
 
+// ftran.F90:787-814: X r2c alone into (nx/2+1, ny, nz) complexes
+void p3dfft_ftran_r2c_1d(real_t* A, real_t* B) {
+  if (!ready()) return;
+  const size_t cbytes = (size_t)(g_nx / 2 + 1) * g_ny * g_nz * 2 * sizeof(real_t);
+  run(A, rsize() * sizeof(real_t), true, B, cbytes, false,
+      [&](const void* i, void* out) { return p3g_ftran_r2c_1d(g_plan, i, out, g_stream); });
+}
+
 void p3dfft_cheby(real_t* A, real_t* B, real_t* Lz) {
   if (!ready()) return;
   const double lz = *Lz;

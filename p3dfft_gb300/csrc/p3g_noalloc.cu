@@ -55,89 +55,23 @@ int scratch_for_current_device(void** out) {
   return P3G_OK;
 }
 
+// The three forward passes on the single-tile kernels (one tile per CTA, no
+// persistent loop), with the pass parameters the allocating path builds.
 template <class P>
 int forward_passes(p3g_plan p, const void* in, void* out, int zi, bool fsign, void* wa, void* wb,
                    cudaStream_t st) {
   using namespace p3g;
-  const long long P_ = p->pitch;
-  void* ybuf = p->nyc < p->ny ? wb : wa;
-  // X r2c: user real -> wa (lines of pitch P, x modes 0..nxhpc-1)
-  {
-    XParams x{};
-    x.in = in;
-    x.out = wa;
-    x.in_field = (long long)p->nx * p->ny * p->nz;
-    x.out_field = (long long)p->nz * p->ny * P_;
-    x.in_line = p->nx;
-    x.out_line = (int)P_;
-    x.nlines = p->ny * p->nz;
-    x.nx = p->nx;
-    x.nkeep = p->nxhpc;
-    x.M = p->ax_x.M;
-    x.log2m = p->ax_x.log2m;
-    x.LS = p->ax_x.ls;
-    x.ps = p->ax_x.ps;
-    x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
-    cudaError_t e = launch_x_r2c<P>(x, p->d_sp + p->ax_x.sp_index, p->d_tw, p->ax_x.threads, p->ax_x.smem, 1, st);
-    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X r2c launch: ") + cudaGetErrorString(e));
-  }
-  // Y c2c: wa -> ybuf, y pruning on store
-  {
-    SParams s{};
-    s.in_xs = s.out_xs = 1;
-    s.in = wa;
-    s.out = ybuf;
-    s.in_axis = (int)P_;
-    s.in_o1 = (long long)p->ny * P_;
-    s.in_o2 = (long long)p->nz * p->ny * P_;
-    s.out_axis = (int)P_;
-    s.out_o1 = (long long)p->nyc * P_;
-    s.out_o2 = (long long)p->nz * p->nyc * P_;
-    s.X = p->nxhpc;
-    s.O1 = p->nz;
-    s.L = p->ny;
-    s.Lout = p->nyc;
-    s.lmap_a0 = s.lmap_a1 = p->ny;
-    s.smap_s0 = p->nycph;
-    s.smap_d = p->ny - p->nyc;
-    s.M = p->ax_y.M;
-    s.log2m = p->ax_y.log2m;
-    s.N = p->ax_y.n;
-    s.xtiles = (s.X + s.M - 1) / s.M;
-    cudaError_t e =
-        launch_strided<P>(s, p->d_sp + p->ax_y.sp_index, p->d_tw, true, p->ax_y.threads, p->ax_y.smem, 1, st);
-    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("Y pass launch: ") + cudaGetErrorString(e));
-  }
-  // Z op: ybuf -> user complex, z pruning on store
-  {
-    const AxisPlan& az = p->ax_z[zi];
-    SParams s{};
-    s.in_xs = s.out_xs = 1;
-    s.in = ybuf;
-    s.out = out;
-    s.out_user = 1;
-    s.in_axis = (int)(p->nyc * P_);
-    s.in_o1 = P_;
-    s.in_o2 = (long long)p->nz * p->nyc * P_;
-    s.out_axis = p->nxhpc * p->nyc;
-    s.out_o1 = p->nxhpc;
-    s.out_o2 = (long long)p->nxhpc * p->nyc * p->nzc;
-    s.X = p->nxhpc;
-    s.O1 = p->nyc;
-    s.L = p->nz;
-    s.Lout = p->nzc;
-    s.pre = zi == 1 ? 1 : (zi == 2 ? 2 : 0);
-    s.post = zi == 2 ? 1 : 0;
-    s.lmap_a0 = s.lmap_a1 = p->nz;
-    s.smap_s0 = p->nzcph;
-    s.smap_d = p->nz - p->nzc;
-    s.M = az.M;
-    s.log2m = az.log2m;
-    s.N = az.n;
-    s.xtiles = (s.X + s.M - 1) / s.M;
-    cudaError_t e = launch_strided<P>(s, p->d_sp + az.sp_index, p->d_tw, fsign, az.threads, az.smem, 1, st);
-    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("Z pass launch: ") + cudaGetErrorString(e));
-  }
+  XParams x;
+  SParams y, z;
+  make_forward_params(p, in, out, wa, wb, zi, (long long)p->nx * p->ny * p->nz,
+                      (long long)p->nxhpc * p->nyc * p->nzc, x, y, z);
+  cudaError_t e = launch_x_r2c<P>(x, p->d_sp + p->ax_x.sp_index, p->d_tw, p->ax_x.threads, p->ax_x.smem, 1, st);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X r2c launch: ") + cudaGetErrorString(e));
+  e = launch_strided<P>(y, p->d_sp + p->ax_y.sp_index, p->d_tw, true, p->ax_y.threads, p->ax_y.smem, 1, st);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("Y pass launch: ") + cudaGetErrorString(e));
+  const AxisPlan& az = p->ax_z[zi];
+  e = launch_strided<P>(z, p->d_sp + az.sp_index, p->d_tw, fsign, az.threads, az.smem, 1, st);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("Z pass launch: ") + cudaGetErrorString(e));
   p->launches += 3;
   return P3G_OK;
 }
@@ -161,7 +95,6 @@ extern "C" int p3g_ftran_r2c_noalloc(p3g_plan p, const void* in, void* out, cons
     default: return fail(P3G_E_ARG, std::string("Unknown transform type: ") + op[2]);
   }
   if (!p->z_ok[zi]) return fail(P3G_E_UNSUPPORTED, std::string("Z transform '") + op[2] + "' unsupported for nz");
-  if (p->layout != P3G_LAYOUT_XYZ) return fail(P3G_E_UNSUPPORTED, "allocation-free transform supports the XYZ layout");
   const size_t esize = p->esize();
   const size_t wa_bytes = ((size_t)p->nz * p->ny * p->pitch * esize + 255) / 256 * 256;
   const size_t wb_bytes = p->nyc < p->ny ? (size_t)p->nz * p->nyc * p->pitch * esize : 0;

@@ -10,6 +10,8 @@
 // format conversion fused in.
 #pragma once
 
+#include <type_traits>
+
 #include "p3g_async.cuh"
 #include "p3g_kernels.cuh"
 
@@ -435,13 +437,14 @@ P3G_D void xr2c_issue(const XPipeParams& q, int tile, int b) {
 }
 
 // X1[k] = (Z[k] + conj Z[N-k]) / 2, X2[k] = -i (Z[k] - conj Z[N-k]) / 2,
-// modes k < nkeep stored to the working layout.
-template <class P>
-P3G_D void xr2c_store(const XParams& x, const typename P::W* sm, int p0, int field) {
-  using W = typename P::W;
+// modes k < nkeep stored to the working layout (USER: the user complex
+// format, for the X-only transform).
+template <class P, bool USER>
+P3G_D void xr2c_store_t(const XParams& x, const typename P::W* sm, int p0, int field) {
   using C = typename P::C;
+  using O = typename std::conditional<USER, typename P::UC, typename P::W>::type;
   const int N = x.nx, nk = x.nkeep;
-  W* out = static_cast<W*>(x.out) + field * x.out_field;
+  O* out = static_cast<O*>(x.out) + field * x.out_field;
   const FastDiv fnk((uint32_t)nk);
   for (int e = threadIdx.x; e < x.M * nk; e += blockDim.x) {
     const int pr = (int)fnk.div((uint32_t)e);
@@ -450,10 +453,20 @@ P3G_D void xr2c_store(const XParams& x, const typename P::W* sm, int p0, int fie
     if (line >= x.nlines) continue;
     const C a = P::from_w(sm[pr * x.LS + pad_index(k, x.ps)]);
     const C bb = cconj(P::from_w(sm[pr * x.LS + pad_index(k == 0 ? 0 : N - k, x.ps)]));
-    out[(long long)line * x.out_line + k] = P::to_w(cscale2(a + bb, 0.5f));
-    if (line + 1 < x.nlines)
-      out[(long long)(line + 1) * x.out_line + k] = P::to_w(cscale2(rot<-1>(a - bb), 0.5f));
+    const C r1 = cscale2(a + bb, 0.5f), r2 = cscale2(rot<-1>(a - bb), 0.5f);
+    if constexpr (USER) {
+      out[(long long)line * x.out_line + k] = P::to_uc(r1);
+      if (line + 1 < x.nlines) out[(long long)(line + 1) * x.out_line + k] = P::to_uc(r2);
+    } else {
+      out[(long long)line * x.out_line + k] = P::to_w(r1);
+      if (line + 1 < x.nlines) out[(long long)(line + 1) * x.out_line + k] = P::to_w(r2);
+    }
   }
+}
+template <class P>
+P3G_D void xr2c_store(const XParams& x, const typename P::W* sm, int p0, int field) {
+  if (x.out_user) xr2c_store_t<P, true>(x, sm, p0, field);
+  else xr2c_store_t<P, false>(x, sm, p0, field);
 }
 
 template <class P>

@@ -16,7 +16,9 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <set>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <cudaTypedefs.h>
@@ -35,6 +37,19 @@ static thread_local std::string g_last_error;
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
   return code;
+}
+
+cudaError_t opt_in_smem(const void* func, int bytes) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done.count({func, dev})) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done.insert({func, dev});
+  return e;
 }
 #define P3G_CUDA_TRY(call)                                                                 \
   do {                                                                                     \
@@ -1060,7 +1075,9 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     delete p;
     return fail(P3G_E_UNSUPPORTED, m);
   };
-  // the kernels form per-element offsets within a plane in 32 bits
+  // single per-element strides (a plane's row pitch, the Z pass's axis stride
+  // nyc*pitch, the STRIDE1 column stride nyc*nzc) are 32-bit kernel parameters;
+  // offsets (their products with indices) are formed in 64 bits
   if ((long long)p->pitch * ny >= (1LL << 31) || (long long)p->nxhpc * p->nyc >= (1LL << 31) ||
       (long long)p->nyc * p->nzc >= (1LL << 31))
     return bad("a plane of more than 2^31 elements is not supported");
@@ -1271,6 +1288,30 @@ int p3g_btran_c2r(p3g_plan p, const void* in, void* out, const char* op, int nv,
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   return p->prec == P3G_F64 ? do_btran<PathF64>(p, in, out, op, nv, dim_in, dim_out, st)
                             : do_btran<PathF32>(p, in, out, op, nv, dim_in, dim_out, st);
+}
+
+int p3g_ftran_r2c_1d(p3g_plan p, const void* in, void* out, void* stream) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  if (!in || !out) return fail(P3G_E_ARG, "NULL array");
+  XParams x{};
+  x.in = in;
+  x.out = out;
+  x.in_field = (long long)p->nx * p->ny * p->nz;
+  x.out_field = (long long)p->nxhp * p->ny * p->nz;
+  x.in_line = p->nx;
+  x.out_line = p->nxhp;
+  x.nlines = p->ny * p->nz;
+  x.nx = p->nx;
+  x.nkeep = p->nxhp;  // every mode: the X transform alone is not pruned
+  x.M = p->ax_x.M;
+  x.log2m = p->ax_x.log2m;
+  x.LS = p->ax_x.ls;
+  x.ps = p->ax_x.ps;
+  x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
+  x.out_user = 1;
+  std::lock_guard<std::mutex> lk(p->mu);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  return p->prec == P3G_F64 ? run_x_r2c<PathF64>(p, x, 1, st) : run_x_r2c<PathF32>(p, x, 1, st);
 }
 
 int p3g_cheby(p3g_plan p, const void* in, void* out, double lz, int nv, long long dim_in, long long dim_out,

@@ -50,7 +50,7 @@ cudaError_t launch_spectrum(const SpecParams& prm, int nv, int sm_count, cudaStr
   int warps = kSpecThreads / 32;
   while (warps > 1 && (size_t)warps * nbins * sizeof(double) > kSpecMaxSmem) warps >>= 1;
   const size_t smem = (size_t)warps * nbins * sizeof(double);
-  cudaError_t e = cudaFuncSetAttribute(k_spectrum<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaError_t e = opt_in_smem((const void*)k_spectrum<P>, 227 * 1024);
   if (e != cudaSuccess) return e;
   int per_sm = 1;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spectrum<P>, warps * 32, smem);

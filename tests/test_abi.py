@@ -28,7 +28,7 @@ def test_libraries_export_declared_symbols(lib):
     legacy_syms = _declared("p3dfft.h")
     for name in ("p3dfft_setup", "p3dfft_get_dims", "p3dfft_ftran_r2c", "p3dfft_btran_c2r", "p3dfft_clean",
                  "p3dfft_ftran_r2c_many", "p3dfft_btran_c2r_many", "p3dfft_cheby", "p3dfft_cheby_many",
-                 "get_timers", "set_timers"):
+                 "get_timers", "set_timers", "p3dfft_ftran_r2c_1d"):
         assert name in legacy_syms, name
     for name in legacy_syms:
         assert hasattr(lib.legacy, name), name
@@ -50,7 +50,7 @@ def test_plan_rejects_bad_sizes_without_gpu(lib):
     assert lib.core.p3g_plan_create(ctypes.byref(h), 8, 8, 8, 10, 8, 8, 0, 0, 0) == -1
     assert lib.core.p3g_plan_create(ctypes.byref(h), 8, 8, 8, 8, 8, 8, 7, 0, 0) == -1
     # a plane of 2^31 or more elements (131072/2+1 modes x 32768 rows) is refused before any
-    # device work: the kernels form offsets within a plane in 32 bits
+    # device work: single per-element strides are 32-bit kernel parameters
     assert lib.core.p3g_plan_create(ctypes.byref(h), 131072, 32768, 2, 0, 0, 0, 0, 0, 0) == -4
     assert b"2^31" in lib.core.p3g_last_error()
 
@@ -94,5 +94,6 @@ def test_fortran_module_binds_exported_symbols(lib):
     # the reference module's public names are all there
     for name in ("p3dfft_type", "r8", "i8", "timers", "p3dfft_setup", "p3dfft_get_dims", "p3dfft_ftran_r2c",
                  "p3dfft_btran_c2r", "p3dfft_ftran_r2c_many", "p3dfft_btran_c2r_many", "p3dfft_cheby",
-                 "p3dfft_cheby_many", "p3dfft_clean", "get_timers", "set_timers", "p3dfft_get_mpi_info"):
+                 "p3dfft_cheby_many", "p3dfft_clean", "get_timers", "set_timers", "p3dfft_get_mpi_info",
+                 "p3dfft_ftran_r2c_1d"):
         assert re.search(r"public\s*::[^\n]*\b%s\b" % name, text), name

@@ -1,13 +1,18 @@
-"""Full-size checks through size-independent properties (the configured
-workloads are too large for the CPU oracle to finish in seconds):
+"""Full-size checks of the configured workloads.
 
-* 1024^3 and 768x1024x540 FP64: round trip within the samples' pass rule
-  (driver_rand.F90:264-276: max error <= 1e-14 N / 4 after the 1/N scaling)
-  and Parseval for the forward spectrum;
-* linearity of the forward transform (T(a x + b y) = a T x + b T y);
-* FP32 against FP64 on the same field (relative L2 <= 1e-6);
-* 512x512x257 with the Chebyshev (DCT-I) Z transform: 'ffc' / 'cff' round trip
-  scaled by 1/(nx ny 2 (nz - 1)).
+Against the CPU oracle on every host core (numpy/scipy FP64, a few seconds
+per direction at these sizes), with the workloads' own seeded fields:
+
+* 768x1024x540, 32 Fourier modes + N(0,1e-3) noise: F64 forward and backward
+  (normalised L-inf <= 1e-12), F32 forward and backward (relative L2 <= 1e-6),
+  the round trip under the samples' rule (driver_rand.F90:264-276) and every
+  seeded mode against its analytic amplitude;
+* 512x512x257 with the Chebyshev (DCT-I) Z transform: 'ffc' / 'cff' and
+  p3dfft_cheby (ftran.F90:383-464).
+
+Through size-independent properties at 1024^3 and 768x1024x540: Parseval,
+the round trip, linearity (T(a x + b y) = a T x + b T y), and FP32 against
+FP64 on the same field.
 """
 import math
 
@@ -114,3 +119,52 @@ def test_chebyshev_config_roundtrip(torch_cuda):
     err = float((r - f).abs().max()) / float(f.abs().max())
     assert err <= 1e-12
     plan.close()
+
+
+def _bench():
+    import os
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    import bench
+    return bench
+
+
+def _against_oracle(torch, name, seed):
+    import p3dfft_gb300 as pg
+    bench = _bench()
+    cfg = bench.CONFIGS[name]
+    grid, ops = cfg["grid"], cfg["ops"]
+    p64 = pg.Plan(*grid, precision=pg.F64)
+    p32 = pg.Plan(*grid, precision=pg.F32)
+    x = bench.make_input(torch, grid, seed, torch.device("cuda"), cfg["input"])
+    err = bench.accuracy(torch, grid, ops, cfg["input"], x, p64, p32, None,
+                         lz=2.0 if name == "cheby" else None, seed=seed)
+    p64.check()
+    p64.close()
+    p32.close()
+    return err
+
+
+def test_noncubic_config_against_oracle(torch_cuda):
+    err = _against_oracle(torch_cuda, "noncubic", 1234)
+    assert err["f64_forward_normalised_linf_vs_oracle"] <= 1e-12
+    assert err["f64_backward_normalised_linf_vs_oracle"] <= 1e-12
+    assert err["f64_roundtrip_max_abs"] <= err["roundtrip_rule_f64"]
+    assert err["f64_roundtrip_normalised_linf"] <= 1e-12
+    assert err["f32_forward_rel_l2_vs_oracle"] <= 1e-6
+    assert err["f32_backward_rel_l2_vs_oracle"] <= 1e-6
+    assert err["f32_roundtrip_max_abs"] <= err["roundtrip_rule_f32"]
+    # the noise adds ~1e-3 sqrt(N) ~ 20 to modes of amplitude ~N/2 ~ 1e8
+    assert err["modes_checked"] >= 30 and err["f64_modes_max_rel_err"] <= 1e-5
+
+
+def test_chebyshev_config_against_oracle(torch_cuda):
+    err = _against_oracle(torch_cuda, "cheby", 77)
+    assert err["f64_forward_normalised_linf_vs_oracle"] <= 1e-12
+    assert err["f64_backward_normalised_linf_vs_oracle"] <= 1e-12
+    assert err["f64_roundtrip_normalised_linf"] <= 1e-12
+    assert err["f64_cheby_normalised_linf_vs_oracle"] <= 1e-12
+    assert err["f32_forward_rel_l2_vs_oracle"] <= 1e-6
+    assert err["f32_backward_rel_l2_vs_oracle"] <= 1e-6
