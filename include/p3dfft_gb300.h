@@ -32,7 +32,8 @@ enum {
   P3G_E_CUDA = -2,      /* a CUDA runtime call failed */
   P3G_E_NOMEM = -3,     /* device allocation failed */
   P3G_E_UNSUPPORTED = -4, /* a size or option outside this build's limits */
-  P3G_E_STATE = -5      /* call out of order (no plan / plan already set up) */
+  P3G_E_STATE = -5,     /* call out of order (no plan / plan already set up) */
+  P3G_E_RANGE = -6      /* F64 path: input magnitudes outside the exponent window at the plan's bias */
 };
 
 enum { P3G_F64 = 0, P3G_F32 = 1 };               /* precision of data and arithmetic path */
@@ -192,8 +193,38 @@ long long p3g_plan_launches(p3g_plan plan);
  * All calls share the array: calls that overlap on the GPU race. */
 int p3g_ftran_r2c_noalloc(p3g_plan plan, const void* in, void* out, const char* op, void* stream);
 
+/* Binary64 range of the F64 path (no counterpart in the reference, whose
+ * FFTW arithmetic is binary64 throughout).  The F64 path computes in
+ * double-float, whose exponent range is binary32's, so every F64 transform
+ * scales its binary64 input by an exact power of two 2^-k and its output by
+ * 2^k.  Results equal the unscaled transform's as long as the largest input
+ * magnitude, scaled, lies in [2^-50, 2^(124 - ceil(log2(nx ny 2 (nz+1))))]
+ * (the window): k = 0 covers fields of largest magnitude ~1e-15 .. ~1e28 at
+ * 1024^3.  Error bounds are relative to the field's largest magnitude;
+ * values below 2^-126 of it flush to zero, as they would in any normwise
+ * accurate FFT.
+ *   P3G_RANGE_FIXED (default): k = bias for every call; the input passes
+ *     record the largest magnitude they convert, and p3g_plan_status /
+ *     p3g_plan_check_range report P3G_E_RANGE when it was outside the window
+ *     (the results of those calls are then invalid; no inf or zero is returned
+ *     silently).
+ *   P3G_RANGE_AUTO: each call first measures the largest magnitude of its
+ *     input on the device (one extra read of the input) and its passes pick k
+ *     from it, without a host round trip.
+ * The F32 path has binary32's range, as the reference's single-precision
+ * build, and ignores these settings. */
+enum { P3G_RANGE_FIXED = 0, P3G_RANGE_AUTO = 1 };
+int p3g_plan_set_range(p3g_plan plan, int mode, int bias);
+/* Synchronises; checks the binary64 inputs converted since the last check
+ * against the window at the plan's bias and clears the record.  Returns
+ * P3G_OK or P3G_E_RANGE; *bias (may be NULL) receives the bias that brings
+ * them into the window (0 when none is needed) and *emax (may be NULL) the
+ * largest binary64 exponent seen (-1075 when every input was zero). */
+int p3g_plan_check_range(p3g_plan plan, int* bias, int* emax);
+
 /* Synchronises and reports a kernel-side failure recorded on the plan's
- * device flag (a pipelined pass whose bounded wait for a tile copy expired). */
+ * device flag (a pipelined pass whose bounded wait for a tile copy expired),
+ * or P3G_E_RANGE as p3g_plan_check_range (whose record it clears). */
 int p3g_plan_status(p3g_plan plan);
 /* Kernel selection: use_pipe = persistent double-buffered passes (default 1),
  * use_tma = TMA tensor-tile copies where the layout allows (default 1).  With

@@ -40,6 +40,9 @@ JOB_FORWARD = 1
 JOB_BACKWARD = 2
 JOB_SPECTRUM = 3
 FLAG_TIMERS = 1
+RANGE_FIXED = 0
+RANGE_AUTO = 1
+E_RANGE = -6
 
 
 class P3DFFTError(RuntimeError):
@@ -203,8 +206,25 @@ class Plan:
         _check(_core().p3g_plan_set_options(self._h, int(pipe), int(tma)))
 
     def check(self):
-        """Synchronise and raise if a kernel recorded a failure."""
+        """Synchronise and raise if a kernel recorded a failure or an F64
+        transform's input was outside the exponent window (p3g_plan_status)."""
         _check(_core().p3g_plan_status(self._h))
+
+    def set_range(self, mode=RANGE_FIXED, bias=0):
+        """Exponent bias of the F64 path (p3g_plan_set_range): RANGE_FIXED
+        with inputs scaled by 2^-bias, or RANGE_AUTO (picked per call on the
+        device from the input's largest magnitude)."""
+        _check(_core().p3g_plan_set_range(self._h, int(mode), int(bias)))
+
+    def check_range(self):
+        """(rc, bias, emax) of p3g_plan_check_range: rc is 0 or E_RANGE, bias
+        the exponent bias that brings the inputs since the last check into the
+        window, emax their largest binary64 exponent."""
+        b, e = ctypes.c_int(), ctypes.c_int()
+        rc = _core().p3g_plan_check_range(self._h, ctypes.byref(b), ctypes.byref(e))
+        if rc not in (0, E_RANGE):
+            _check(rc)
+        return rc, b.value, e.value
 
     def timers(self):
         t = (ctypes.c_double * 12)()

@@ -37,6 +37,8 @@ CORE_SIGNATURES = {
     "p3g_ftran_r2c_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
                                              ctypes.c_void_p]),
     "p3g_plan_status": (ctypes.c_int, [ctypes.c_void_p]),
+    "p3g_plan_set_range": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "p3g_plan_check_range": (ctypes.c_int, [ctypes.c_void_p, _c_int_p, _c_int_p]),
     "p3g_plan_create_tuned": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),

@@ -249,6 +249,65 @@ P3G_HD double df2d(float hi, float lo) {
   return u2d(d + (uint64_t)(int64_t)k);
 }
 
+// -------------------------------------------- exponent bias (binary64 range)
+// The double-float pairs have binary32's exponent range, so the F64 path
+// scales a field by an exact power of two 2^-k on its way in (binary64 ->
+// double-float) and by 2^k on its way out, with k chosen from the field's
+// largest magnitude.  Scaling by a power of two only moves the exponent, so
+// the result is the same as the unscaled transform's wherever both exist.
+
+// x * 2^-k as double-float (k = 0: d2df).  Zeros, binary64 subnormals,
+// infinities and NaNs keep their class; a result below 2^-1022 flushes to a
+// signed zero and one at or above 2^1024 becomes a signed infinity.
+P3G_HD df d2df_scaled(double x, int k) {
+  if (k == 0) return d2df(x);
+  const uint64_t b = d2u(x);
+  const uint32_t hw = (uint32_t)(b >> 32);
+  const int e = (int)((hw >> 20) & 0x7FFu);
+  if (e == 0 || e == 2047) return d2df_edge(x);
+  const int e2 = e - k;
+  if (e2 < 1) return df{u2f(hw & 0x80000000u), 0.0f};
+  if (e2 > 2046) return df{u2f((hw & 0x80000000u) | 0x7F800000u), 0.0f};
+  const uint32_t hw2 = (hw & 0x800FFFFFu) | ((uint32_t)e2 << 20);
+  return d2df(u2d(((uint64_t)hw2 << 32) | (uint32_t)b));
+}
+
+// d * 2^k for a binary64 d (k = 0: d).  Zeros, infinities and NaNs keep their
+// class; a result below 2^-1022 flushes to a signed zero, one at or above
+// 2^1024 becomes a signed infinity.
+P3G_HD double scale_pow2(double d, int k) {
+  if (k == 0) return d;
+  const uint64_t b = d2u(d);
+  const uint32_t hw = (uint32_t)(b >> 32);
+  const int e = (int)((hw >> 20) & 0x7FFu);
+  if (e == 0 || e == 2047) return d;
+  const int e2 = e + k;
+  if (e2 < 1) return u2d((uint64_t)(hw & 0x80000000u) << 32);
+  if (e2 > 2046) return u2d((uint64_t)((hw & 0x80000000u) | 0x7FF00000u) << 32);
+  return u2d(((uint64_t)((hw & 0x800FFFFFu) | ((uint32_t)e2 << 20)) << 32) | (uint32_t)b);
+}
+
+// The window of largest magnitudes the F64 path transforms without a bias:
+// 2^kRangeLo <= max |x| < 2^(kRangeTop - log2n + 1), where 2^log2n bounds the
+// transform's gain (nx ny 2 (nz + 1) covers the DCT-I/DST-I extensions).
+// Above it a partial sum could reach binary32's 2^128; below it the low words
+// of the pairs (2^-48 of the largest value) would fall out of binary32's
+// normal range.
+constexpr int kRangeLo = -50;
+constexpr int kRangeTop = 124;
+
+// Exponent bias for a field whose largest |high word| (sign cleared) is amax:
+// 0 inside the window, else the unbiased exponent E of the largest magnitude
+// (which scales it into [1, 2)).  Fields of zeros and binary64 subnormals
+// only, and fields holding an infinity or a NaN, are not scaled.
+P3G_HD int range_bias(uint32_t amax, int log2n) {
+  const int e = (int)(amax >> 20);
+  if (e == 0 || e >= 2047) return 0;
+  const int E = e - 1023;
+  if (E >= kRangeLo && E <= kRangeTop - log2n) return 0;
+  return E;
+}
+
 // ------------------------------------------------------- double-float ops
 // The ops keep (hi, lo) unnormalised: hi is always a rounded partial result and
 // lo collects exact error terms and the low-order parts.  The absolute error
@@ -373,6 +432,21 @@ struct PathF64 {
   P3G_D static double2 to_uc(C c) { return make_double2(df2d(c.re.hi, c.re.lo), df2d(c.im.hi, c.im.lo)); }
   P3G_D static df from_ur(double v) { return d2df(v); }
   P3G_D static double to_ur(df v) { return df2d(v.hi, v.lo); }
+  // with the exponent bias k: inputs times 2^-k, outputs times 2^k
+  P3G_D static C from_uc(double2 v, int k) { return cdf{d2df_scaled(v.x, k), d2df_scaled(v.y, k)}; }
+  P3G_D static double2 to_uc(C c, int k) {
+    return make_double2(scale_pow2(df2d(c.re.hi, c.re.lo), k), scale_pow2(df2d(c.im.hi, c.im.lo), k));
+  }
+  P3G_D static df from_ur(double v, int k) { return d2df_scaled(v, k); }
+  P3G_D static double to_ur(df v, int k) { return scale_pow2(df2d(v.hi, v.lo), k); }
+  // largest |high word| seen (the binary64 exponent window's input)
+  P3G_D static void track(uint32_t& amax, double v) {
+    amax = max(amax, (uint32_t)__double2hiint(v) & 0x7FFFFFFFu);
+  }
+  P3G_D static void track(uint32_t& amax, double2 v) {
+    track(amax, v.x);
+    track(amax, v.y);
+  }
   P3G_D static C make(df re, df im) { return cdf{re, im}; }
   P3G_D static C zero() { return cdf{df{0.f, 0.f}, df{0.f, 0.f}}; }
   P3G_D static df re(C c) { return c.re; }
@@ -390,6 +464,14 @@ struct PathF32 {
   P3G_D static float2 to_uc(C c) { return make_float2(c.re, c.im); }
   P3G_D static float from_ur(float v) { return v; }
   P3G_D static float to_ur(float v) { return v; }
+  // binary32 data has binary32's range, as the reference's single-precision
+  // build: no exponent bias and nothing to track
+  P3G_D static C from_uc(float2 v, int) { return cf{v.x, v.y}; }
+  P3G_D static float2 to_uc(C c, int) { return make_float2(c.re, c.im); }
+  P3G_D static float from_ur(float v, int) { return v; }
+  P3G_D static float to_ur(float v, int) { return v; }
+  P3G_D static void track(uint32_t&, float) {}
+  P3G_D static void track(uint32_t&, float2) {}
   P3G_D static C make(float re, float im) { return cf{re, im}; }
   P3G_D static C zero() { return cf{0.f, 0.f}; }
   P3G_D static float re(C c) { return c.re; }

@@ -127,6 +127,7 @@ struct p3g_batch_s {
   int prec = P3G_F64;
   int sm_count = 0;
   std::vector<BatchPass> host;
+  std::vector<p3g_plan> plans;  // the jobs' plans (their range records)
   BatchPass* d_pass = nullptr;
   size_t pass_cap = 0;
   int* d_ctl = nullptr;
@@ -249,6 +250,8 @@ static int build_chains(p3g_batch b, int njobs, const p3g_job* jobs, int threads
       SParams y, z;
       void* fout = jb.kind == P3G_JOB_FORWARD ? jb.out : cplx;
       make_forward_params(p, jb.in, fout, wa, wb, 0, rsize, csize, x, y, z);
+      x.range = range_params(p, true, false);
+      z.range = range_params(p, false, false);
       x_pass(kBXr2c, x);
       s_pass(kBFwd, y, p->ax_y);
       s_pass(kBFwd, z, p->ax_z[0]);
@@ -258,6 +261,8 @@ static int build_chains(p3g_batch b, int njobs, const p3g_job* jobs, int threads
       XParams x;
       const void* bin = jb.kind == P3G_JOB_BACKWARD ? jb.in : cplx;
       make_backward_params(p, bin, jb.out, wa, wb, 0, csize, rsize, z, y, x);
+      if (jb.kind == P3G_JOB_BACKWARD) z.range = range_params(p, true, false);  // user input
+      x.range = range_params(p, false, false);
       s_pass(kBBwd, z, p->ax_z[0]);
       s_pass(kBBwd, y, p->ax_y);
       x_pass(kBXc2r, x);
@@ -399,6 +404,9 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->upload);
   if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch table upload: ") + cudaGetErrorString(e));
   b->host = std::move(table);
+  b->plans.clear();
+  for (int j = 0; j < njobs; ++j)
+    if (std::find(b->plans.begin(), b->plans.end(), jobs[j].plan) == b->plans.end()) b->plans.push_back(jobs[j].plan);
   b->npass = (int)b->host.size();
   b->nitems = (int)items;
   b->smem = smem;
@@ -477,6 +485,11 @@ int p3g_batch_status(p3g_batch b, void* stream) {
   e = cudaMemcpy(&err, b->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch status: ") + cudaGetErrorString(e));
   if (err) return fail(P3G_E_CUDA, "batch kernel: a dependency wait timed out");
+  // the F64 jobs' binary64 inputs against the exponent window at their plans' biases
+  for (p3g_plan p : b->plans) {
+    const int rc = p3g_plan_check_range(p, nullptr, nullptr);
+    if (rc) return rc;
+  }
   return P3G_OK;
 }
 

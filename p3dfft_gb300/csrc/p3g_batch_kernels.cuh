@@ -72,24 +72,30 @@ P3G_D void batch_process_pipe(const BatchPass& bp, int tile, typename P::W* buf)
   constexpr int E = batch_pipe_elems<P::kF64>();
   switch (bp.kind) {
     case kBXr2c: {  // the first FFT stage reads the raw line pairs
-      Tile<P> t{buf, nullptr, bp.x.M, bp.x.log2m, bp.x.LS, 1, bp.x.ps};
+      const int k = range_k(bp.x.range);
+      uint32_t amax = 0;
+      Tile<P> t{buf, nullptr, bp.x.M, bp.x.log2m, bp.x.LS, 1, bp.x.ps, k, &amax};
       cta_fft<P, -1, E, kLineMajor, kRawR2C>(t, bp.sp, bp.tw);
-      xr2c_store<P>(bp.x, buf, tile * bp.x.M, 0);
+      xr2c_store<P>(bp.x, buf, tile * bp.x.M, 0, k);
+      range_flush(bp.x.range, amax);
       break;
     }
     case kBXc2r: {  // the first FFT stage reads the raw half spectra
       Tile<P> t{buf, nullptr, bp.x.M, bp.x.log2m, bp.x.LS, 1, bp.x.ps};
       cta_fft<P, 1, E, kLineMajor, kRawC2R>(t, bp.sp, bp.tw);
-      xc2r_store<P>(bp.x, buf, tile * bp.x.M, 0);
+      xc2r_store<P>(bp.x, buf, tile * bp.x.M, 0, range_k(bp.x.range));
       break;
     }
     default: {
       const int o1 = tile / bp.s.xtiles;
-      strided_fix<P>(bp.s, false, buf);
+      const int k = range_k(bp.s.range);
+      uint32_t amax = 0;
+      strided_fix<P>(bp.s, false, buf, k, amax);
       Tile<P> t{buf, nullptr, bp.s.M, bp.s.log2m, 1, bp.s.M};
       if (bp.kind == kBFwd) cta_fft<P, -1, E, kPointMajor>(t, bp.sp, bp.tw);
       else cta_fft<P, 1, E, kPointMajor>(t, bp.sp, bp.tw);
-      strided_store<P>(bp.s, buf, tile - o1 * bp.s.xtiles, o1, 0);
+      strided_store<P>(bp.s, buf, tile - o1 * bp.s.xtiles, o1, 0, k);
+      range_flush(bp.s.range, amax);
       break;
     }
   }
@@ -101,9 +107,20 @@ P3G_D void batch_process_pipe(const BatchPass& bp, int tile, typename P::W* buf)
 template <class P>
 __device__ __noinline__ void batch_process_single(const BatchPass& bp, int tile, typename P::W* sm) {
   switch (bp.kind) {
-    case kBXr2c: x_r2c_tile<P, true>(bp.x, bp.sp, bp.tw, sm, tile, 0); break;
-    case kBFwd: strided_tile<P, -1, true>(bp.s, bp.sp, bp.tw, sm, tile); break;
-    case kBBwd: strided_tile<P, 1, true>(bp.s, bp.sp, bp.tw, sm, tile); break;
+    case kBXr2c: {
+      uint32_t amax = 0;
+      x_r2c_tile<P, true>(bp.x, bp.sp, bp.tw, sm, tile, 0, amax);
+      range_flush(bp.x.range, amax);
+      break;
+    }
+    case kBFwd:
+    case kBBwd: {
+      uint32_t amax = 0;
+      if (bp.kind == kBFwd) strided_tile<P, -1, true>(bp.s, bp.sp, bp.tw, sm, tile, amax);
+      else strided_tile<P, 1, true>(bp.s, bp.sp, bp.tw, sm, tile, amax);
+      range_flush(bp.s.range, amax);
+      break;
+    }
     case kBXc2r: x_c2r_tile<P, true>(bp.x, bp.sp, bp.tw, sm, tile, 0); break;
     case kBSpec: {
       double* hist = reinterpret_cast<double*>(sm);

@@ -105,6 +105,10 @@ struct Tile {
   typename P::W* scratch;  // same size, generic stages only
   int M, log2m, LS, JS;    // point-major tiles (LS = 1) always have JS = M
   int ps = 0;              // line-major padding shift (0: none)
+  // kRawR2C first stage only: the binary64 exponent bias of the conversion
+  // and the thread's running largest |high word| (null: not tracked)
+  int ebias = 0;
+  uint32_t* amax = nullptr;
   P3G_D int addr(int line, int j) const { return line * LS + (LS == 1 ? j * JS : pad_index(j, ps)); }
   P3G_D uint32_t saddr(int line, int j) const {
     return (uint32_t)__cvta_generic_to_shared(sm) + (uint32_t)((line * LS + j * JS) * (int)sizeof(typename P::W));
@@ -223,9 +227,14 @@ __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const
         const uint32_t ra = sbase + (uint32_t)((2 * line * N + j) * (int)kU);
         const uint32_t rstep = (uint32_t)per_line * kU, lstep = (uint32_t)N * kU;
 #pragma unroll
-        for (int q = 0; q < R; ++q)
-          v[i][q] = P::make(P::from_ur(lds1(ra + q * rstep, (UR*)nullptr)),
-                            P::from_ur(lds1(ra + lstep + q * rstep, (UR*)nullptr)));
+        for (int q = 0; q < R; ++q) {
+          const UR x1 = lds1(ra + q * rstep, (UR*)nullptr), x2 = lds1(ra + lstep + q * rstep, (UR*)nullptr);
+          if (t.amax) {
+            P::track(*t.amax, x1);
+            P::track(*t.amax, x2);
+          }
+          v[i][q] = P::make(P::from_ur(x1, t.ebias), P::from_ur(x2, t.ebias));
+        }
       } else if constexpr (RAW == kRawC2R) {
         const int nh = N / 2 + 1;
         const int rs = sizeof(W) == 8 ? (nh + 1) & ~1 : nh;  // raw line stride (xc2r_raw_stride)

@@ -8,6 +8,29 @@
 
 namespace p3g {
 
+// Exponent window of the F64 path (range_bias in p3g_arith.cuh).  A pass
+// that converts binary64 user data in records the largest |high word| it saw
+// (track, atomicMax, null = off) and scales by 2^-k; a pass that converts to
+// binary64 user data scales by 2^k.  k is `bias`, or, with auto_max set, the
+// range_bias of the largest |high word| a reduction kernel measured on the
+// call's input just before.
+struct RangeParams {
+  unsigned* track;
+  const unsigned* auto_max;
+  int bias;
+  int log2n;
+};
+P3G_D int range_k(const RangeParams& r) {
+  return r.auto_max ? range_bias(__ldcg(r.auto_max), r.log2n) : r.bias;
+}
+// Adds a thread's largest |high word| to the pass's record: one atomic per
+// warp (every lane of the warp must call it).
+P3G_D void range_flush(const RangeParams& r, uint32_t amax) {
+  if (!r.track) return;
+  const uint32_t w = __reduce_max_sync(0xFFFFFFFFu, amax);
+  if ((threadIdx.x & 31) == 0 && w != 0u) atomicMax(r.track, w);
+}
+
 // X passes: lines along x (contiguous).  Two real lines travel as the real and
 // imaginary parts of one complex line of length nx.
 struct XParams {
@@ -23,6 +46,7 @@ struct XParams {
   int LS;                         // shared-memory stride between line pairs (>= padded N)
   int ps;                         // line padding shift (see pad_index), 0 = none
   int out_user;                   // r2c: 1 stores the user complex format (X-only transform)
+  RangeParams range;              // r2c: binary64 input; c2r (and X-only r2c): binary64 output
 };
 
 // Strided Y/Z passes: a tile is M consecutive x columns of one (o1, o2) row
@@ -58,6 +82,7 @@ struct SParams {
   // column 0), so that full tiles start on a 16-byte boundary and load two
   // columns per copy.
   int xphase;
+  RangeParams range;  // user-format input (Z backward) or output (Z forward) of the F64 path
 };
 
 // First column of tile xt of row (o1, o2) and the row's phase: 0, or 1 when
@@ -76,8 +101,8 @@ struct ChebyParams {
   long long zstride;   // element stride along z
   int npencil;         // nxhpc * nyc
   int nzc;
-  float sc_hi, sc_lo;  // 1/(nx*ny*(nzc-1)) as double-float
-  float l_hi, l_lo;    // 4/Lz as double-float
+  double sc;           // 1/(nx*ny*(nzc-1))
+  double lfac;         // 4/Lz
 };
 
 // Global loads.  CG = true reads through L2 only (ld.global.cg): the batch
@@ -88,14 +113,20 @@ P3G_D T gload(const T* p) {
   if constexpr (CG) return __ldcg(p);
   else return *p;
 }
+// User-format elements are converted with the exponent bias k (inputs
+// times 2^-k, outputs times 2^k) and inputs are tracked into amax.
 template <class P, bool CG = false>
-P3G_D typename P::C load_elem(const void* base, int user, long long idx) {
-  if (user) return P::from_uc(gload<CG>(static_cast<const typename P::UC*>(base) + idx));
+P3G_D typename P::C load_elem(const void* base, int user, long long idx, int k, uint32_t& amax) {
+  if (user) {
+    const typename P::UC v = gload<CG>(static_cast<const typename P::UC*>(base) + idx);
+    P::track(amax, v);
+    return P::from_uc(v, k);
+  }
   return P::from_w(gload<CG>(static_cast<const typename P::W*>(base) + idx));
 }
 template <class P>
-P3G_D void store_elem(void* base, int user, long long idx, typename P::C v) {
-  if (user) static_cast<typename P::UC*>(base)[idx] = P::to_uc(v);
+P3G_D void store_elem(void* base, int user, long long idx, typename P::C v, int k) {
+  if (user) static_cast<typename P::UC*>(base)[idx] = P::to_uc(v, k);
   else static_cast<typename P::W*>(base)[idx] = P::to_w(v);
 }
 

@@ -26,7 +26,8 @@ struct PathLimits<PathF32> {
 // One tile (M line pairs) of field `field`; sm = the tile's shared memory.
 template <class P, bool CG>
 P3G_D void x_r2c_tile(const XParams& prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw,
-                      typename P::W* sm, int tile, int field) {
+                      typename P::W* sm, int tile, int field, uint32_t& amax) {
+  const int kb = range_k(prm.range);
   using W = typename P::W;
   using C = typename P::C;
   const int N = prm.nx;
@@ -44,7 +45,12 @@ P3G_D void x_r2c_tile(const XParams& prm, const StagePlan* __restrict__ sp, cons
     const int c = lt & 1;
     float* f = smf + ((lt >> 1) * LS + pad_index(x, ps)) * kW;
     if constexpr (P::kF64) {
-      const df v = line < prm.nlines ? P::from_ur(gload<CG>(in + (long long)line * prm.in_line + x)) : df{0.f, 0.f};
+      df v{0.f, 0.f};
+      if (line < prm.nlines) {
+        const double u = gload<CG>(in + (long long)line * prm.in_line + x);
+        P::track(amax, u);
+        v = P::from_ur(u, kb);
+      }
       f[c] = v.hi;
       f[2 + c] = v.lo;
     } else {
@@ -54,13 +60,15 @@ P3G_D void x_r2c_tile(const XParams& prm, const StagePlan* __restrict__ sp, cons
   __syncthreads();
   Tile<P> t{sm, sm + M * LS, M, prm.log2m, LS, 1, ps};
   cta_fft<P, -1, kElemsPerThread, kLineMajor>(t, sp, tw);
-  xr2c_store<P>(prm, sm, p0, field);
+  xr2c_store<P>(prm, sm, p0, field, kb);
 }
 
 template <class P>
 __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
     k_x_r2c(const XParams prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw) {
-  x_r2c_tile<P, false>(prm, sp, tw, reinterpret_cast<typename P::W*>(p3g_smem), blockIdx.x, blockIdx.y);
+  uint32_t amax = 0;
+  x_r2c_tile<P, false>(prm, sp, tw, reinterpret_cast<typename P::W*>(p3g_smem), blockIdx.x, blockIdx.y, amax);
+  range_flush(prm.range, amax);
 }
 
 // ---------------------------------------------------------------- X c2r
@@ -70,6 +78,7 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
 template <class P, bool CG>
 P3G_D void x_c2r_tile(const XParams& prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw,
                       typename P::W* sm, int tile, int field) {
+  const int kb = range_k(prm.range);
   using W = typename P::W;
   using C = typename P::C;
   const int N = prm.nx;
@@ -108,7 +117,7 @@ P3G_D void x_c2r_tile(const XParams& prm, const StagePlan* __restrict__ sp, cons
     const int c = lt & 1;
     const float* f = smf + ((lt >> 1) * LS + pad_index(n, ps)) * kW;
     if constexpr (P::kF64) {
-      out[(long long)line * prm.out_line + n] = P::to_ur(df{f[c], f[2 + c]});
+      out[(long long)line * prm.out_line + n] = P::to_ur(df{f[c], f[2 + c]}, kb);
     } else {
       out[(long long)line * prm.out_line + n] = f[c];
     }
@@ -126,7 +135,8 @@ __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMi
 // One tile (M columns x L rows); `bid` enumerates (x tile, o1, o2 = field).
 template <class P, int DIR, bool CG>
 P3G_D void strided_tile(const SParams& prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw,
-                        typename P::W* sm, long long bid) {
+                        typename P::W* sm, long long bid, uint32_t& amax) {
+  const int kb = range_k(prm.range);
   using W = typename P::W;
   using C = typename P::C;
   const int M = prm.M;
@@ -162,7 +172,8 @@ P3G_D void strided_tile(const SParams& prm, const StagePlan* __restrict__ sp, co
     const int src = j >= prm.lmap_a1 ? j - prm.lmap_d : (j < prm.lmap_a0 ? j : -1);
     C v = P::zero();
     if (x0 + m < prm.X && src >= 0)
-      v = load_elem<P, CG>(prm.in, prm.in_user, ibase + (long long)m * prm.in_xs + (long long)src * prm.in_axis);
+      v = load_elem<P, CG>(prm.in, prm.in_user, ibase + (long long)m * prm.in_xs + (long long)src * prm.in_axis, kb,
+                           amax);
     if (prm.pre == 0) {
       sm[j * M + m] = P::to_w(v);
     } else if (prm.pre == 1) {
@@ -192,46 +203,56 @@ P3G_D void strided_tile(const SParams& prm, const StagePlan* __restrict__ sp, co
     C v;
     if (prm.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
     else v = P::from_w(sm[k * M + m]);
-    store_elem<P>(prm.out, prm.out_user, obase + (long long)m * prm.out_xs + (long long)jo * prm.out_axis, v);
+    store_elem<P>(prm.out, prm.out_user, obase + (long long)m * prm.out_xs + (long long)jo * prm.out_axis, v, kb);
   }
 }
 
 template <class P, int DIR>
 __global__ void __launch_bounds__(PathLimits<P>::kMaxThreads, PathLimits<P>::kMinBlocks)
     k_strided(const SParams prm, const StagePlan* __restrict__ sp, const float4* __restrict__ tw) {
-  strided_tile<P, DIR, false>(prm, sp, tw, reinterpret_cast<typename P::W*>(p3g_smem), blockIdx.x);
+  uint32_t amax = 0;
+  strided_tile<P, DIR, false>(prm, sp, tw, reinterpret_cast<typename P::W*>(p3g_smem), blockIdx.x, amax);
+  range_flush(prm.range, amax);
 }
 
 // ------------------------------------------------------------- Chebyshev
-// out(k) = L k old + out(k+2), ftran.F90:412-451, one thread per (x, y) pencil.
+// out(k) = L k old + out(k+2), ftran.F90:412-451, one thread per (x, y)
+// pencil.  The F64 path runs this recurrence in binary64 itself (a few
+// multiply-adds per mode on a pass bound by its 2 x 16 bytes per mode), so
+// it has binary64's range and rounding like the reference; the F32 path in
+// binary32.
 template <class P>
 __global__ void k_cheby(const ChebyParams prm) {
-  using C = typename P::C;
   using UC = typename P::UC;
+  using R = typename std::conditional<P::kF64, double, float>::type;
   const int pcl = blockIdx.x * blockDim.x + threadIdx.x;
   if (pcl >= prm.npencil) return;
   UC* d = static_cast<UC*>(prm.data) + blockIdx.y * prm.field + pcl * prm.pstride;
   const int n = prm.nzc;
   const long long zs = prm.zstride;
-  auto scaled = [&](int k) { return mulr(P::from_uc(d[k * zs]), prm.sc_hi, prm.sc_lo); };
-  auto lk = [&](int k, C v) {  // (4/Lz) * k * v
-    const df f = dmulc(df{(float)k, 0.0f}, prm.l_hi, prm.l_lo);
-    return mulr(v, f.hi, f.lo);
+  const R sc = (R)prm.sc, lf = (R)prm.lfac;
+  auto scaled = [&](int k) {
+    const UC v = d[k * zs];
+    return UC{(R)v.x * sc, (R)v.y * sc};
   };
-  C old = scaled(n - 2);
-  C o1 = cscale2(lk(n - 1, scaled(n - 1)), 0.5f);  // out(nzc-1)
-  C o2 = P::zero();                                // out(nzc)
-  d[(n - 2) * zs] = P::to_uc(o1);
-  d[(n - 1) * zs] = P::to_uc(o2);
+  UC old = scaled(n - 2);
+  const UC top = scaled(n - 1);
+  const R f1 = lf * (R)(n - 1) * (R)0.5;
+  UC o1{f1 * top.x, f1 * top.y};  // out(nzc-1)
+  UC o2{(R)0, (R)0};               // out(nzc)
+  d[(n - 2) * zs] = o1;
+  d[(n - 1) * zs] = o2;
   for (int k = n - 3; k >= 0; --k) {
-    const C nw = scaled(k);
-    const C val = lk(k + 1, old) + o2;
-    d[k * zs] = P::to_uc(val);
+    const UC nw = scaled(k);
+    const R f = lf * (R)(k + 1);
+    const UC val{f * old.x + o2.x, f * old.y + o2.y};
+    d[k * zs] = val;
     o2 = o1;
     o1 = val;
     old = nw;
   }
-  d[0] = P::to_uc(cscale2(P::from_uc(d[0]), 0.5f));
+  const UC v0 = d[0];
+  d[0] = UC{v0.x * (R)0.5, v0.y * (R)0.5};
 }
 
 // ---------------------------------------------------------------- launchers

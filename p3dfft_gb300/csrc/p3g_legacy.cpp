@@ -126,13 +126,57 @@ bool ready() {
   return true;
 }
 
+// The F64 path's binary64 exponent window (p3g_plan_set_range): every call
+// runs at the exponent bias its direction needed last (fields of a
+// simulation keep their magnitudes from call to call).  A call whose input
+// turns out to lie outside the window runs again at the bias that brings it
+// in, so no call returns infinities or flushed zeros that the reference's
+// binary64 arithmetic would not; a call whose output overwrites its input
+// (in place) cannot run again and picks its bias on the device instead (one
+// extra read of the input).  The binary32 library has binary32's range, as
+// the reference's single-precision build, and the checks return at once.
+enum { kFwd = 0, kBwd = 1 };
+int g_bias[2] = {0, 0};
+
+// Runs `call` (which enqueues the transform on g_stream) under the range
+// policy above; finish synchronises every stream the call used.  Returns false
+// after recording an error.
+template <class F, class S>
+bool ranged(int dir, bool in_place, F&& call, S&& finish) {
+  p3g_plan_set_range(g_plan, in_place ? P3G_RANGE_AUTO : P3G_RANGE_FIXED, g_bias[dir]);
+  int rc = call();
+  const bool synced = finish();
+  if (!check(rc)) return false;
+  if (!synced) {
+    error(P3G_E_CUDA, "P3DFFT error: transform failed");
+    return false;
+  }
+  int need = 0;
+  rc = p3g_plan_check_range(g_plan, &need, nullptr);
+  if (rc == P3G_E_RANGE) {
+    g_bias[dir] = need;
+    p3g_plan_set_range(g_plan, P3G_RANGE_FIXED, need);
+    rc = call();
+    const bool ok = finish();
+    if (!check(rc)) return false;
+    if (!ok) {
+      error(P3G_E_CUDA, "P3DFFT error: transform failed");
+      return false;
+    }
+    rc = p3g_plan_check_range(g_plan, nullptr, nullptr);
+  }
+  if (in_place) p3g_plan_set_range(g_plan, P3G_RANGE_FIXED, g_bias[dir]);
+  return check(rc);
+}
+
 // Runs one transform call with host or device arrays.  in_bytes/out_bytes
 // cover all nv fields.  Host arrays are used in place only on the real-space
 // side (in_real / out_real): the X passes read and write whole contiguous
 // lines there, while the Z passes reach the wavenumber-space array in short
 // strided runs that cross the host link far slower than one bulk copy.
 template <class F>
-void run(const void* in, size_t in_bytes, bool in_real, void* out, size_t out_bytes, bool out_real, F&& call) {
+void run(int dir, const void* in, size_t in_bytes, bool in_real, void* out, size_t out_bytes, bool out_real,
+         F&& call) {
   const bool din = on_device(in) || (in_real && host_direct(in));
   const bool dout = on_device(out) || (out_real && host_direct(out));
   const void* dev_in = in;
@@ -148,11 +192,24 @@ void run(const void* in, size_t in_bytes, bool in_real, void* out, size_t out_by
     dev_out = stage(1, out_bytes);
     if (!dev_out) return error(P3G_E_NOMEM, "P3DFFT error: staging allocation failed");
   }
-  if (!check(call(dev_in, dev_out))) return;
+  const bool in_place = dev_in == dev_out;
+  if (!ranged(dir, in_place, [&] { return call(dev_in, dev_out); },
+              [&] { return cudaStreamSynchronize(g_stream) == cudaSuccess; }))
+    return;
   if (!dout && cudaMemcpyAsync(out, dev_out, out_bytes, cudaMemcpyDeviceToHost, g_stream) != cudaSuccess)
     return error(P3G_E_CUDA, "P3DFFT error: device to host copy failed");
   if (cudaStreamSynchronize(g_stream) != cudaSuccess) return error(P3G_E_CUDA, "P3DFFT error: transform failed");
   g_status = 0;
+}
+
+// Runs an overlapped call (both streams) under the range policy.
+template <class F>
+void run_overlapped(int dir, F&& call) {
+  if (ranged(dir, false, call, [] {
+        const cudaError_t a = cudaStreamSynchronize(g_stream), b = cudaStreamSynchronize(g_copy);
+        return a == cudaSuccess && b == cudaSuccess;
+      }))
+    g_status = 0;
 }
 
 size_t rsize() { return (size_t)g_nx * g_ny * g_nz; }
@@ -195,6 +252,7 @@ void p3dfft_setup(int* dims, int* nx, int* ny, int* nz, int* comm, int* nxc, int
   if (!g_stream) cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
   if (!g_copy) cudaStreamCreateWithFlags(&g_copy, cudaStreamNonBlocking);
   std::memset(g_timers, 0, sizeof(g_timers));
+  g_bias[kFwd] = g_bias[kBwd] = 0;
   g_comm = comm ? *comm : 0;
   g_nx = *nx;
   g_ny = *ny;
@@ -222,13 +280,6 @@ void p3dfft_get_mpi_info(int* taskid, int* ntasks, int* comm) {
   g_status = 0;
 }
 
-// Waits for both streams of an overlapped call and records the outcome.
-void finish_overlapped(int rc) {
-  const cudaError_t a = cudaStreamSynchronize(g_stream), b = cudaStreamSynchronize(g_copy);
-  if (!check(rc)) return;
-  if (a != cudaSuccess || b != cudaSuccess) return error(P3G_E_CUDA, "P3DFFT error: transform failed");
-  g_status = 0;
-}
 
 void p3dfft_ftran_r2c(real_t* A, real_t* B, unsigned char* op) {
   if (!ready()) return;
@@ -238,9 +289,9 @@ void p3dfft_ftran_r2c(real_t* A, real_t* B, unsigned char* op) {
   if (g_layout == P3G_LAYOUT_XYZ && !on_device(B) && (on_device(A) || host_direct(A))) {
     void* st = stage(1, csize() * 2 * sizeof(real_t));
     if (!st) return error(P3G_E_NOMEM, "P3DFFT error: staging allocation failed");
-    return finish_overlapped(p3g_ftran_r2c_to_host(g_plan, A, B, st, o, kRowBlocks, g_stream, g_copy));
+    return run_overlapped(kFwd, [&] { return p3g_ftran_r2c_to_host(g_plan, A, B, st, o, kRowBlocks, g_stream, g_copy); });
   }
-  run(A, rsize() * sizeof(real_t), true, B, csize() * 2 * sizeof(real_t), false,
+  run(kFwd, A, rsize() * sizeof(real_t), true, B, csize() * 2 * sizeof(real_t), false,
       [&](const void* i, void* out) { return p3g_ftran_r2c(g_plan, i, out, o, 1, 0, 0, g_stream); });
 }
 
@@ -252,9 +303,10 @@ void p3dfft_btran_c2r(real_t* A, real_t* B, unsigned char* op) {
   if (g_layout == P3G_LAYOUT_XYZ && !on_device(A) && (on_device(B) || host_direct(B))) {
     void* st = stage(0, csize() * 2 * sizeof(real_t));
     if (!st) return error(P3G_E_NOMEM, "P3DFFT error: staging allocation failed");
-    return finish_overlapped(p3g_btran_c2r_from_host(g_plan, A, st, B, o, kRowBlocks, g_stream, g_copy));
+    return run_overlapped(kBwd,
+                          [&] { return p3g_btran_c2r_from_host(g_plan, A, st, B, o, kRowBlocks, g_stream, g_copy); });
   }
-  run(A, csize() * 2 * sizeof(real_t), false, B, rsize() * sizeof(real_t), true,
+  run(kBwd, A, csize() * 2 * sizeof(real_t), false, B, rsize() * sizeof(real_t), true,
       [&](const void* i, void* out) { return p3g_btran_c2r(g_plan, i, out, o, 1, 0, 0, g_stream); });
 }
 
@@ -266,7 +318,7 @@ void p3dfft_ftran_r2c_many(real_t* A, int* dim_in, real_t* B, int* dim_out, int*
   const char* o = reinterpret_cast<const char*>(op);
   const long long di = *dim_in, dout = *dim_out;
   const int n = *nv;
-  run(A, (size_t)di * n * sizeof(real_t), true, B, (size_t)dout * n * 2 * sizeof(real_t), false,
+  run(kFwd, A, (size_t)di * n * sizeof(real_t), true, B, (size_t)dout * n * 2 * sizeof(real_t), false,
       [&](const void* i, void* out) { return p3g_ftran_r2c(g_plan, i, out, o, n, di, dout, g_stream); });
 }
 
@@ -278,7 +330,7 @@ void p3dfft_btran_c2r_many(real_t* A, int* dim_in, real_t* B, int* dim_out, int*
   const char* o = reinterpret_cast<const char*>(op);
   const long long di = *dim_in, dout = *dim_out;
   const int n = *nv;
-  run(A, (size_t)di * n * 2 * sizeof(real_t), false, B, (size_t)dout * n * sizeof(real_t), true,
+  run(kBwd, A, (size_t)di * n * 2 * sizeof(real_t), false, B, (size_t)dout * n * sizeof(real_t), true,
       [&](const void* i, void* out) { return p3g_btran_c2r(g_plan, i, out, o, n, di, dout, g_stream); });
 }
 
@@ -286,14 +338,14 @@ void p3dfft_btran_c2r_many(real_t* A, int* dim_in, real_t* B, int* dim_out, int*
 void p3dfft_ftran_r2c_1d(real_t* A, real_t* B) {
   if (!ready()) return;
   const size_t cbytes = (size_t)(g_nx / 2 + 1) * g_ny * g_nz * 2 * sizeof(real_t);
-  run(A, rsize() * sizeof(real_t), true, B, cbytes, false,
+  run(kFwd, A, rsize() * sizeof(real_t), true, B, cbytes, false,
       [&](const void* i, void* out) { return p3g_ftran_r2c_1d(g_plan, i, out, g_stream); });
 }
 
 void p3dfft_cheby(real_t* A, real_t* B, real_t* Lz) {
   if (!ready()) return;
   const double lz = *Lz;
-  run(A, rsize() * sizeof(real_t), true, B, csize() * 2 * sizeof(real_t), false,
+  run(kFwd, A, rsize() * sizeof(real_t), true, B, csize() * 2 * sizeof(real_t), false,
       [&](const void* i, void* out) { return p3g_cheby(g_plan, i, out, lz, 1, 0, 0, g_stream); });
 }
 
@@ -304,7 +356,7 @@ void p3dfft_cheby_many(real_t* A, int* dim_in, real_t* B, int* dim_out, int* nv,
   const double lz = *Lz;
   const long long di = *dim_in, dout = *dim_out;
   const int n = *nv;
-  run(A, (size_t)di * n * sizeof(real_t), true, B, (size_t)dout * n * 2 * sizeof(real_t), false,
+  run(kFwd, A, (size_t)di * n * sizeof(real_t), true, B, (size_t)dout * n * 2 * sizeof(real_t), false,
       [&](const void* i, void* out) { return p3g_cheby(g_plan, i, out, lz, n, di, dout, g_stream); });
 }
 

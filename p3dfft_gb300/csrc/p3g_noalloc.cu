@@ -63,8 +63,12 @@ int forward_passes(p3g_plan p, const void* in, void* out, int zi, bool fsign, vo
   using namespace p3g;
   XParams x;
   SParams y, z;
-  make_forward_params(p, in, out, wa, wb, zi, (long long)p->nx * p->ny * p->nz,
-                      (long long)p->nxhpc * p->nyc * p->nzc, x, y, z);
+  const long long rsize = (long long)p->nx * p->ny * p->nz;
+  make_forward_params(p, in, out, wa, wb, zi, rsize, (long long)p->nxhpc * p->nyc * p->nzc, x, y, z);
+  x.range = range_params(p, true, true);
+  z.range = range_params(p, false, true);
+  const int rc = launch_range_scan(p, in, rsize, rsize, 1, st);  // P3G_RANGE_AUTO only
+  if (rc) return rc;
   cudaError_t e = launch_x_r2c<P>(x, p->d_sp + p->ax_x.sp_index, p->d_tw, p->ax_x.threads, p->ax_x.smem, 1, st);
   if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X r2c launch: ") + cudaGetErrorString(e));
   e = launch_strided<P>(y, p->d_sp + p->ax_y.sp_index, p->d_tw, true, p->ax_y.threads, p->ax_y.smem, 1, st);

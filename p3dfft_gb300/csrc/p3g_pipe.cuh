@@ -227,7 +227,7 @@ P3G_D void strided_issue(const SPipeParams& q, const CUtensorMap* tin, int tile,
 // working format, DST-I negation, DCT-I mirror after a TMA load (tma).
 // Ends with a barrier when it changed anything.
 template <class P>
-P3G_D void strided_fix(const SParams& s, bool tma, typename P::W* sm) {
+P3G_D void strided_fix(const SParams& s, bool tma, typename P::W* sm, int k, uint32_t& amax) {
   using W = typename P::W;
   using C = typename P::C;
   const bool raw_user = s.in_user != 0 && P::kF64;  // binary32 user data is the working format
@@ -237,7 +237,14 @@ P3G_D void strided_fix(const SParams& s, bool tma, typename P::W* sm) {
     for (int e = threadIdx.x; e < M * rows; e += blockDim.x) {
       const int m = e & (M - 1);
       const int j = e >> s.log2m;
-      C v = raw_user ? P::from_uc(reinterpret_cast<const typename P::UC*>(sm)[j * M + m]) : P::from_w(sm[j * M + m]);
+      C v;
+      if (raw_user) {
+        const typename P::UC u = reinterpret_cast<const typename P::UC*>(sm)[j * M + m];
+        P::track(amax, u);
+        v = P::from_uc(u, k);
+      } else {
+        v = P::from_w(sm[j * M + m]);
+      }
       if (s.pre == 2 && j >= L + 2) v = cneg(v);
       const W w = P::to_w(v);
       sm[j * M + m] = w;
@@ -250,7 +257,7 @@ P3G_D void strided_fix(const SParams& s, bool tma, typename P::W* sm) {
 // Store of a transformed strided tile with the pruning map and the output
 // format (DST-I output rows k+1 times i).
 template <class P>
-P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int o1, int o2) {
+P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int o1, int o2, int k) {
   using C = typename P::C;
   const int M = s.M;
   const int ph = strided_phase(s, o1, o2);  // the tile's columns as loaded by strided_copy
@@ -263,7 +270,7 @@ P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int 
     C v;
     if (s.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
     else v = P::from_w(sm[k * M + m]);
-    store_elem<P>(s.out, s.out_user, obase + (long long)c * s.out_xs + (long long)jo * s.out_axis, v);
+    store_elem<P>(s.out, s.out_user, obase + (long long)c * s.out_xs + (long long)jo * s.out_axis, v, k);
   };
   const int T = blockDim.x;
   if (s.out_xs == 1 && s.post == 0 && (s.smap_s0 >= s.Lout || s.smap_d == 0) && (T & (M - 1)) == 0) {
@@ -282,7 +289,7 @@ P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int 
     if (s.out_user) {
       typename P::UC* d = static_cast<typename P::UC*>(s.out) + o;
 #pragma unroll 4
-      for (int jo = j0; jo < s.Lout; jo += js, a += astep, d += ostep) *d = P::to_uc(P::from_w(lds(a, (W*)nullptr)));
+      for (int jo = j0; jo < s.Lout; jo += js, a += astep, d += ostep) *d = P::to_uc(P::from_w(lds(a, (W*)nullptr)), k);
     } else {
       W* d = static_cast<W*>(s.out) + o;
 #pragma unroll 4
@@ -322,6 +329,8 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
     }
   }
   __syncthreads();
+  const int k = range_k(pp.s.range);
+  uint32_t amax = 0;
   int it = 0;
   int tile = blockIdx.x;
   bool next_pending = false;
@@ -340,7 +349,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       else cp_async_wait<1>();
     }
     if (__syncthreads_or(!ok)) break;
-    strided_fix<P>(pp.s, pp.use_tma != 0, strided_smem<P>(pp.c).buf0 + b * pp.c.buf_elems);
+    strided_fix<P>(pp.s, pp.use_tma != 0, strided_smem<P>(pp.c).buf0 + b * pp.c.buf_elems, k, amax);
     {
       const SPipeParams& q = pp;
       const StridedSmem<P> sm = strided_smem<P>(q.c);
@@ -350,7 +359,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
     {
       int xt, o1, o2;
       strided_decode(pp, tile, xt, o1, o2);
-      strided_store<P>(pp.s, strided_smem<P>(pp.c).buf0 + b * pp.c.buf_elems, xt, o1, o2);
+      strided_store<P>(pp.s, strided_smem<P>(pp.c).buf0 + b * pp.c.buf_elems, xt, o1, o2, k);
     }
     __syncthreads();
   }
@@ -364,6 +373,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
   } else {
     cp_async_wait<0>();
   }
+  range_flush(pp.s.range, amax);
 }
 
 // ---------------------------------------------------------------- X passes
@@ -440,7 +450,7 @@ P3G_D void xr2c_issue(const XPipeParams& q, int tile, int b) {
 // modes k < nkeep stored to the working layout (USER: the user complex
 // format, for the X-only transform).
 template <class P, bool USER>
-P3G_D void xr2c_store_t(const XParams& x, const typename P::W* sm, int p0, int field) {
+P3G_D void xr2c_store_t(const XParams& x, const typename P::W* sm, int p0, int field, int kb) {
   using C = typename P::C;
   using O = typename std::conditional<USER, typename P::UC, typename P::W>::type;
   const int N = x.nx, nk = x.nkeep;
@@ -455,24 +465,27 @@ P3G_D void xr2c_store_t(const XParams& x, const typename P::W* sm, int p0, int f
     const C bb = cconj(P::from_w(sm[pr * x.LS + pad_index(k == 0 ? 0 : N - k, x.ps)]));
     const C r1 = cscale2(a + bb, 0.5f), r2 = cscale2(rot<-1>(a - bb), 0.5f);
     if constexpr (USER) {
-      out[(long long)line * x.out_line + k] = P::to_uc(r1);
-      if (line + 1 < x.nlines) out[(long long)(line + 1) * x.out_line + k] = P::to_uc(r2);
+      out[(long long)line * x.out_line + k] = P::to_uc(r1, kb);
+      if (line + 1 < x.nlines) out[(long long)(line + 1) * x.out_line + k] = P::to_uc(r2, kb);
     } else {
       out[(long long)line * x.out_line + k] = P::to_w(r1);
       if (line + 1 < x.nlines) out[(long long)(line + 1) * x.out_line + k] = P::to_w(r2);
     }
   }
 }
+// kb: the exponent bias of the user-format output (X-only transform)
 template <class P>
-P3G_D void xr2c_store(const XParams& x, const typename P::W* sm, int p0, int field) {
-  if (x.out_user) xr2c_store_t<P, true>(x, sm, p0, field);
-  else xr2c_store_t<P, false>(x, sm, p0, field);
+P3G_D void xr2c_store(const XParams& x, const typename P::W* sm, int p0, int field, int kb) {
+  if (x.out_user) xr2c_store_t<P, true>(x, sm, p0, field, kb);
+  else xr2c_store_t<P, false>(x, sm, p0, field, kb);
 }
 
 template <class P>
 __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::kMinBlocks)
     k_xr2c_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
                 const float4* __restrict__ tw_g) {
+  const int k = range_k(pp.x.range);
+  uint32_t amax = 0;
   int it = 0;
   int tile = blockIdx.x;
   if (tile < pp.c.ntiles) xr2c_issue<P>(pp, tile, 0);
@@ -486,17 +499,18 @@ __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::k
     __syncthreads();
     {
       // the first FFT stage reads the raw line pairs (packing fused into it)
-      Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
+      Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps, k, &amax};
       cta_fft<P, -1, XPipeLimits<P>::kE, kLineMajor, kRawR2C>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;
       const int p0 = (tile - field * pp.c.tiles_per_field) * pp.x.M;
-      xr2c_store<P>(pp.x, xpipe_buf<P>(pp.c, b), p0, field);
+      xr2c_store<P>(pp.x, xpipe_buf<P>(pp.c, b), p0, field, k);
     }
     __syncthreads();
   }
   cp_async_wait<0>();
+  range_flush(pp.x.range, amax);
 }
 
 // c2r: complex lines 2p, 2p+1 of nh = N/2+1 modes copied raw (pair stride
@@ -583,7 +597,7 @@ P3G_D void xc2r_issue(const XPipeParams& q, int tile, int b) {
 // Even N: each thread takes positions n, n+1 of a line pair, reads the two
 // complex values once and writes two-element vectors to both lines.
 template <class P>
-P3G_D void xc2r_store(const XParams& x, const typename P::W* sm, int p0, int field) {
+P3G_D void xc2r_store(const XParams& x, const typename P::W* sm, int p0, int field, int k) {
   using W = typename P::W;
   using UR = typename P::UR;
   const int M = x.M, N = x.nx, LS = x.LS, ps = x.ps;
@@ -602,9 +616,10 @@ P3G_D void xc2r_store(const XParams& x, const typename P::W* sm, int p0, int fie
       const W b = sm[pr * LS + pad_index(n, ps) + 1];
       UR* o = out + (long long)line * x.out_line + n;
       if constexpr (P::kF64) {
-        *reinterpret_cast<double2*>(o) = make_double2(P::to_ur(df{a.x, a.z}), P::to_ur(df{b.x, b.z}));
+        *reinterpret_cast<double2*>(o) = make_double2(P::to_ur(df{a.x, a.z}, k), P::to_ur(df{b.x, b.z}, k));
         if (line + 1 < x.nlines)
-          *reinterpret_cast<double2*>(o + x.out_line) = make_double2(P::to_ur(df{a.y, a.w}), P::to_ur(df{b.y, b.w}));
+          *reinterpret_cast<double2*>(o + x.out_line) =
+              make_double2(P::to_ur(df{a.y, a.w}, k), P::to_ur(df{b.y, b.w}, k));
       } else {
         *reinterpret_cast<float2*>(o) = make_float2(a.x, b.x);
         if (line + 1 < x.nlines) *reinterpret_cast<float2*>(o + x.out_line) = make_float2(a.y, b.y);
@@ -622,7 +637,7 @@ P3G_D void xc2r_store(const XParams& x, const typename P::W* sm, int p0, int fie
     if (line >= x.nlines) continue;
     const int c = lt & 1;
     const float* f = smf + ((lt >> 1) * LS + pad_index(n, ps)) * kW;
-    if constexpr (P::kF64) out[(long long)line * x.out_line + n] = P::to_ur(df{f[c], f[2 + c]});
+    if constexpr (P::kF64) out[(long long)line * x.out_line + n] = P::to_ur(df{f[c], f[2 + c]}, k);
     else out[(long long)line * x.out_line + n] = f[c];
   }
 }
@@ -631,6 +646,7 @@ template <class P>
 __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::kMinBlocks)
     k_xc2r_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
                 const float4* __restrict__ tw_g) {
+  const int k = range_k(pp.x.range);
   int it = 0;
   int tile = blockIdx.x;
   if (tile < pp.c.ntiles) xc2r_issue<P>(pp, tile, 0);
@@ -650,7 +666,7 @@ __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::k
     {
       const int field = tile / pp.c.tiles_per_field;
       const int p0 = (tile - field * pp.c.tiles_per_field) * pp.x.M;
-      xc2r_store<P>(pp.x, xpipe_buf<P>(pp.c, b), p0, field);
+      xc2r_store<P>(pp.x, xpipe_buf<P>(pp.c, b), p0, field, k);
     }
     __syncthreads();
   }

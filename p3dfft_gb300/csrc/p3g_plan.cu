@@ -536,6 +536,53 @@ int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) 
 
 namespace p3g {
 
+// Largest |high word| (sign cleared) of nv binary64 fields into *out.
+__global__ void __launch_bounds__(256) k_range_scan(const double* __restrict__ in, long long n, long long field,
+                                                    unsigned* out) {
+  const double* f = in + blockIdx.y * field;
+  uint32_t m = 0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if ((reinterpret_cast<uintptr_t>(f) & 15) == 0) {
+    const double2* f2 = reinterpret_cast<const double2*>(f);
+    for (; i < n / 2; i += stride) {
+      const double2 v = __ldcs(f2 + i);
+      m = max(m, (uint32_t)__double2hiint(v.x) & 0x7FFFFFFFu);
+      m = max(m, (uint32_t)__double2hiint(v.y) & 0x7FFFFFFFu);
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) m = max(m, (uint32_t)__double2hiint(f[n - 1]) & 0x7FFFFFFFu);
+  } else {
+    for (; i < n; i += stride) m = max(m, (uint32_t)__double2hiint(__ldcs(f + i)) & 0x7FFFFFFFu);
+  }
+  m = __reduce_max_sync(0xFFFFFFFFu, m);
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+RangeParams range_params(p3g_plan p, bool input, bool allow_auto) {
+  RangeParams r{};
+  if (p->prec != P3G_F64) return r;
+  r.track = input ? reinterpret_cast<unsigned*>(p->d_err + 1) : nullptr;
+  r.auto_max = allow_auto && p->range_mode == P3G_RANGE_AUTO ? reinterpret_cast<const unsigned*>(p->d_err + 2)
+                                                             : nullptr;
+  r.bias = p->ebias;
+  r.log2n = p->log2n;
+  return r;
+}
+
+int launch_range_scan(p3g_plan p, const void* in, long long n, long long field, int nv, cudaStream_t st) {
+  if (p->prec != P3G_F64 || p->range_mode != P3G_RANGE_AUTO) return P3G_OK;
+  cudaError_t e = cudaMemsetAsync(p->d_err + 2, 0, sizeof(int), st);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("range scan: ") + cudaGetErrorString(e));
+  const long long want = (n / 2 + 255) / 256;
+  const int gx = (int)std::max(1LL, std::min(want, (long long)p->sm_count * 8 / std::max(1, nv) + 1));
+  k_range_scan<<<dim3(gx, nv), 256, 0, st>>>(static_cast<const double*>(in), n, field,
+                                               reinterpret_cast<unsigned*>(p->d_err + 2));
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("range scan launch: ") + cudaGetErrorString(e));
+  p->launches++;
+  return P3G_OK;
+}
+
 // Pass parameters of a forward transform: X r2c user real -> wa, Y wa ->
 // ybuf (wa, or wb when nyc < ny) keeping y modes 0..nycph-1 and the top
 // nyc-nycph (seg_copy_y, ftran.F90:736-738), Z ybuf -> user complex with the
@@ -723,6 +770,9 @@ int do_ftran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   XParams x;
   SParams y, z;
   make_forward_params(p, in, out, p->wa, p->wb, zi, dim_in, dim_out, x, y, z);
+  x.range = range_params(p, true, true);
+  z.range = range_params(p, false, true);
+  if ((rc = launch_range_scan(p, in, (long long)p->nx * p->ny * p->nz, dim_in, nv, st))) return rc;
   {
     PassTimer tm(p, 4, st);
     if ((rc = run_x_r2c<P>(p, x, nv, st))) return rc;
@@ -753,6 +803,9 @@ int do_btran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   SParams z, y;
   XParams x;
   make_backward_params(p, in, out, p->wa, p->wb, zi, dim_in, dim_out, z, y, x);
+  z.range = range_params(p, true, true);
+  x.range = range_params(p, false, true);
+  if ((rc = launch_range_scan(p, in, 2LL * p->nxhpc * p->nyc * p->nzc, 2 * dim_in, nv, st))) return rc;
   {
     PassTimer tm(p, 8, st);
     if ((rc = run_strided<P>(p, z, p->ax_z[zi], fsign, nv, st))) return rc;
@@ -854,6 +907,9 @@ int do_ftran_to_host(p3g_plan p, const void* in, void* out_host, void* stage, co
   XParams x;
   SParams y, z;
   make_forward_params(p, in, stage, p->wa, p->wb, zi, rsize, csize, x, y, z);
+  x.range = range_params(p, true, true);
+  z.range = range_params(p, false, true);
+  if ((rc = launch_range_scan(p, in, rsize, rsize, 1, st))) return rc;
   const size_t es = p->esize();
   if (!device_memory(in) && p->nz >= 2) {
     cudaStream_t aux;
@@ -933,6 +989,11 @@ int do_btran_from_host(p3g_plan p, const void* in_host, void* stage, void* out, 
   SParams z, y;
   XParams x;
   make_backward_params(p, stage, out, p->wa, p->wb, zi, csize, rsize, z, y, x);
+  z.range = range_params(p, true, true);
+  x.range = range_params(p, false, true);
+  // the auto bias needs the whole input's largest magnitude before the first
+  // block's Z pass: measured on the host array itself
+  if ((rc = launch_range_scan(p, in_host, 2 * csize, 2 * csize, 1, st))) return rc;
   const size_t es = p->esize();
   const auto blocks = row_blocks(p->nyc, chunks);
   EventSet evs(blocks.size());
@@ -998,11 +1059,6 @@ int do_btran_from_host(p3g_plan p, const void* in_host, void* stage, void* out, 
 }
 
 bool valid_op(const char* op) { return op && op[0] && op[1] && op[2]; }
-
-void split_df(long double v, float& hi, float& lo) {
-  hi = (float)v;
-  lo = (float)(v - (long double)hi);
-}
 
 }  // namespace
 
@@ -1156,10 +1212,16 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, dev);
   }
 
+  {
+    const long double gain = (long double)nx * (long double)ny * 2.0L * (long double)(nz + 1);
+    int l = 0;
+    while ((long double)std::ldexp(1.0, l) < gain) ++l;
+    p->log2n = l;
+  }
   p->tw_bytes = tw.v.size() * sizeof(float4);
   if (cudaMalloc(&p->d_tw, p->tw_bytes) != cudaSuccess ||
       cudaMalloc(&p->d_sp, sps.size() * sizeof(StagePlan)) != cudaSuccess ||
-      cudaMalloc(&p->d_err, sizeof(int)) != cudaSuccess || cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess) {
+      cudaMalloc(&p->d_err, 4 * sizeof(int)) != cudaSuccess || cudaMemset(p->d_err, 0, 4 * sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     if (p->d_tw) cudaFree(p->d_tw);
     delete p;
@@ -1309,8 +1371,11 @@ int p3g_ftran_r2c_1d(p3g_plan p, const void* in, void* out, void* stream) {
   x.ps = p->ax_x.ps;
   x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
   x.out_user = 1;
+  x.range = range_params(p, true, true);
   std::lock_guard<std::mutex> lk(p->mu);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int rc = launch_range_scan(p, in, x.in_field, x.in_field, 1, st);
+  if (rc) return rc;
   return p->prec == P3G_F64 ? run_x_r2c<PathF64>(p, x, 1, st) : run_x_r2c<PathF32>(p, x, 1, st);
 }
 
@@ -1336,8 +1401,8 @@ int p3g_cheby(p3g_plan p, const void* in, void* out, double lz, int nv, long lon
     c.pstride = 1;
     c.zstride = (long long)p->nxhpc * p->nyc;
   }
-  split_df(1.0L / ((long double)p->nx * (long double)p->ny * (long double)(p->nzc - 1)), c.sc_hi, c.sc_lo);
-  split_df(4.0L / (long double)lz, c.l_hi, c.l_lo);
+  c.sc = 1.0 / ((double)p->nx * (double)p->ny * (double)(p->nzc - 1));
+  c.lfac = 4.0 / lz;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   PassTimer tm(p, 7, st);
   cudaError_t e = p->prec == P3G_F64 ? launch_cheby<PathF64>(c, nv, st) : launch_cheby<PathF32>(c, nv, st);
@@ -1381,13 +1446,44 @@ long long p3g_plan_device_bytes(p3g_plan p) {
 
 long long p3g_plan_launches(p3g_plan p) { return p ? p->launches : 0; }
 
+int p3g_plan_set_range(p3g_plan p, int mode, int bias) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  if (mode != P3G_RANGE_FIXED && mode != P3G_RANGE_AUTO) return fail(P3G_E_ARG, "unknown range mode");
+  if (bias < -1100 || bias > 1100) return fail(P3G_E_ARG, "exponent bias out of range");
+  std::lock_guard<std::mutex> lk(p->mu);
+  p->range_mode = mode;
+  p->ebias = bias;
+  return P3G_OK;
+}
+
+int p3g_plan_check_range(p3g_plan p, int* bias, int* emax) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  int w[3] = {0, 0, 0};
+  cudaError_t e = cudaMemcpy(w, p->d_err, sizeof(w), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(p->d_err + 1, 0, sizeof(int));
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("range read: ") + cudaGetErrorString(e));
+  const uint32_t amax = (uint32_t)w[1];
+  const int ebits = (int)(amax >> 20);
+  if (emax) *emax = ebits == 0 ? -1075 : ebits - 1023;
+  const int need = range_bias(amax, p->log2n);
+  if (bias) *bias = need;
+  if (p->prec != P3G_F64 || p->range_mode == P3G_RANGE_AUTO || ebits == 0 || ebits == 2047) return P3G_OK;
+  // inside the window at the plan's bias?
+  const int E = ebits - 1023 - p->ebias;
+  if (E >= kRangeLo && E <= kRangeTop - p->log2n) return P3G_OK;
+  return fail(P3G_E_RANGE, "F64 transform input of largest magnitude 2^" + std::to_string(ebits - 1023) +
+                               " is outside the exponent window at bias " + std::to_string(p->ebias) +
+                               " (results invalid): call again after p3g_plan_set_range(plan, P3G_RANGE_FIXED, " +
+                               std::to_string(need) + ") or with P3G_RANGE_AUTO");
+}
+
 int p3g_plan_status(p3g_plan p) {
   if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
   int flag = 0;
   if (cudaMemcpy(&flag, p->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
     return fail(P3G_E_CUDA, std::string("status read: ") + cudaGetErrorString(cudaGetLastError()));
   if (flag) return fail(P3G_E_CUDA, "a pipelined pass timed out waiting for its tile copy (results invalid)");
-  return P3G_OK;
+  return p3g_plan_check_range(p, nullptr, nullptr);
 }
 
 int p3g_plan_set_options(p3g_plan p, int use_pipe, int use_tma) {

@@ -48,6 +48,13 @@ void make_forward_params(p3g_plan_s* p, const void* in, void* out, void* wa, voi
                          long long dim_out, XParams& x, SParams& y, SParams& z);
 void make_backward_params(p3g_plan_s* p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
                           long long dim_out, SParams& z, SParams& y, XParams& x);
+// Exponent-window parameters of a pass converting the plan's binary64 user
+// data in (input = true: tracked) or out; allow_auto = false ignores the
+// auto mode (callers that run no reduction first).  Zero on the F32 path.
+RangeParams range_params(p3g_plan_s* p, bool input, bool allow_auto);
+// Auto mode: clears the measured word and launches the reduction over nv
+// binary64 fields of n doubles spaced `field` doubles apart.
+int launch_range_scan(p3g_plan_s* p, const void* in, long long n, long long field, int nv, cudaStream_t st);
 }  // namespace p3g
 
 struct p3g_plan_s {
@@ -72,8 +79,14 @@ struct p3g_plan_s {
   cudaStream_t aux = nullptr;  // second compute stream of the host-array transforms
   std::mutex mu;
   int sm_count = 0;
-  int* d_err = nullptr;  // set by a kernel whose bounded wait timed out
+  // device words: [0] set by a kernel whose bounded wait timed out, [1] the
+  // largest |high word| of the binary64 inputs converted since the last range
+  // check, [2] the same measured by the auto-bias reduction of the current call
+  int* d_err = nullptr;
   bool use_pipe = true, use_tma = true;
+  int range_mode = P3G_RANGE_FIXED;  // F64 path: exponent bias fixed (ebias) or picked per call on the device
+  int ebias = 0;
+  int log2n = 0;  // ceil(log2(nx ny 2 (nz + 1))): bound of the transform's gain
 
   size_t esize() const { return prec == P3G_F64 ? 16 : 8; }
 };
