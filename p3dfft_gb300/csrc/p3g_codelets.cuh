@@ -1,4 +1,4 @@
-// Register-resident DFT codelets of radix 2, 3, 4, 5, 8 and 16.
+// Register-resident DFT codelets of radix 2, 3, 4, 5, 8, 16 and 32.
 //
 // DIR = -1 computes X_k = sum_n a_n exp(-2 pi i n k / R) (FFTW_FORWARD),
 // DIR = +1 the exp(+...) transform (FFTW_BACKWARD).  Inputs and outputs are in
@@ -124,6 +124,74 @@ P3G_D void dft16(C* a) {
     for (int k1 = 0; k1 < 4; ++k1) a[k2 + 4 * k1] = t[4 * k2 + k1];
 }
 
+// a * w32^E with w32 = exp(DIR 2 pi i / 32): w32^E = w32^(E mod 8) (DIR i)^(E / 8)
+// (cos/sin of 2 pi e / 32 for e = 1, 2, 3 as (hi, lo) binary32 pairs; the
+// sines are the cosines of 8 - e).
+#define P3G_C32_1 0x1.f6297cp-1f, 0x1.feeb96p-26f
+#define P3G_C32_2 0x1.d906bcp-1f, 0x1.e651a8p-26f
+#define P3G_C32_3 0x1.a9b662p-1f, 0x1.21d434p-26f
+#define P3G_C32_5 0x1.1c73b4p-1f, -0x1.9465cep-27f
+#define P3G_C32_6 0x1.87de2ap-2f, 0x1.abaa58p-28f
+#define P3G_C32_7 0x1.8f8b84p-3f, -0x1.cb2cfcp-30f
+template <int DIR, int E, class C>
+P3G_D C mul_w32(C a) {
+  constexpr int e8 = E % 8, q = (E / 8) % 4;
+  constexpr float S = DIR > 0 ? 1.0f : -1.0f;
+  C r;
+  if constexpr (e8 == 0) r = a;
+  else if constexpr (e8 == 4) r = mul_w8_1<DIR>(a);
+  else if constexpr (e8 == 1) r = mulcc(a, P3G_C32_1, S * 0x1.8f8b84p-3f, S * -0x1.cb2cfcp-30f);
+  else if constexpr (e8 == 2) r = mulcc(a, P3G_C32_2, S * 0x1.87de2ap-2f, S * 0x1.abaa58p-28f);
+  else if constexpr (e8 == 3) r = mulcc(a, P3G_C32_3, S * 0x1.1c73b4p-1f, S * -0x1.9465cep-27f);
+  else if constexpr (e8 == 5) r = mulcc(a, P3G_C32_5, S * 0x1.a9b662p-1f, S * 0x1.21d434p-26f);
+  else if constexpr (e8 == 6) r = mulcc(a, P3G_C32_6, S * 0x1.d906bcp-1f, S * 0x1.e651a8p-26f);
+  else r = mulcc(a, P3G_C32_7, S * 0x1.f6297cp-1f, S * 0x1.feeb96p-26f);
+  if constexpr (q >= 1) r = rot<DIR>(r);
+  if constexpr (q >= 2) r = rot<DIR>(r);
+  if constexpr (q >= 3) r = rot<DIR>(r);
+  return r;
+}
+
+// 32 = 8 x 4: inner DFT4 over n2 (inputs n1 + 8 n2), twiddle w32^(n1 k2),
+// outer DFT8 over n1 (contiguous after the inner step); output X[k2 + 4 k1].
+template <int DIR, class C>
+P3G_D void dft32(C* a) {
+#pragma unroll
+  for (int n1 = 0; n1 < 8; ++n1) dft4<DIR>(a[n1], a[n1 + 8], a[n1 + 16], a[n1 + 24]);
+  // b[n1][k2] lives in a[n1 + 8 k2]
+  a[1 + 8] = mul_w32<DIR, 1>(a[1 + 8]);
+  a[2 + 8] = mul_w32<DIR, 2>(a[2 + 8]);
+  a[3 + 8] = mul_w32<DIR, 3>(a[3 + 8]);
+  a[4 + 8] = mul_w32<DIR, 4>(a[4 + 8]);
+  a[5 + 8] = mul_w32<DIR, 5>(a[5 + 8]);
+  a[6 + 8] = mul_w32<DIR, 6>(a[6 + 8]);
+  a[7 + 8] = mul_w32<DIR, 7>(a[7 + 8]);
+  a[1 + 16] = mul_w32<DIR, 2>(a[1 + 16]);
+  a[2 + 16] = mul_w32<DIR, 4>(a[2 + 16]);
+  a[3 + 16] = mul_w32<DIR, 6>(a[3 + 16]);
+  a[4 + 16] = mul_w32<DIR, 8>(a[4 + 16]);
+  a[5 + 16] = mul_w32<DIR, 10>(a[5 + 16]);
+  a[6 + 16] = mul_w32<DIR, 12>(a[6 + 16]);
+  a[7 + 16] = mul_w32<DIR, 14>(a[7 + 16]);
+  a[1 + 24] = mul_w32<DIR, 3>(a[1 + 24]);
+  a[2 + 24] = mul_w32<DIR, 6>(a[2 + 24]);
+  a[3 + 24] = mul_w32<DIR, 9>(a[3 + 24]);
+  a[4 + 24] = mul_w32<DIR, 12>(a[4 + 24]);
+  a[5 + 24] = mul_w32<DIR, 15>(a[5 + 24]);
+  a[6 + 24] = mul_w32<DIR, 18>(a[6 + 24]);
+  a[7 + 24] = mul_w32<DIR, 21>(a[7 + 24]);
+#pragma unroll
+  for (int k2 = 0; k2 < 4; ++k2) dft8<DIR>(a + 8 * k2);
+  // now X[k2 + 4 k1] sits in a[8 k2 + k1]: transpose the 4x8 index
+  C t[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) t[i] = a[i];
+#pragma unroll
+  for (int k2 = 0; k2 < 4; ++k2)
+#pragma unroll
+    for (int k1 = 0; k1 < 8; ++k1) a[k2 + 4 * k1] = t[8 * k2 + k1];
+}
+
 template <int R, int DIR, class C>
 P3G_D void dft(C* a) {
   if constexpr (R == 2) dft2<DIR>(a);
@@ -132,6 +200,7 @@ P3G_D void dft(C* a) {
   else if constexpr (R == 5) dft5<DIR>(a);
   else if constexpr (R == 8) dft8<DIR>(a);
   else if constexpr (R == 16) dft16<DIR>(a);
+  else if constexpr (R == 32) dft32<DIR>(a);
 }
 
 }  // namespace p3g

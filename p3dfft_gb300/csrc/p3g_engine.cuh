@@ -13,7 +13,7 @@
 // butterflies of the stage in registers (at most ceil(E/R), E = elements per
 // thread, which the launch guarantees by using ceil(M N / E) threads).
 //
-// Radices 2, 3, 4, 5, 8, 16 are register codelets.  Any other prime p runs a
+// Radices 2, 3, 4, 5, 8, 16, 32 are register codelets.  Any other prime p runs a
 // generic direct-DFT stage through a second shared-memory buffer (O(N p) work).
 #pragma once
 
@@ -28,7 +28,7 @@ struct StagePlan {
   int n;                   // transform length (1 allowed: no stages)
   int nstages;
   int has_generic;         // a stage with a radix outside {2,3,4,5,8,16}
-  int cnt[6];              // number of stages of radix 16, 8, 4, 2, 3, 5 (stored in this order, then generic)
+  int cnt[7];              // number of stages of radix 32, 16, 8, 4, 2, 3, 5 (stored in this order, then generic)
   int radix[kMaxStages];
   int ns[kMaxStages];      // sub-transform length before the stage
   int tw_off[kMaxStages];  // float4 offset of this stage's twiddles [k < ns][q-1 < radix-1]
@@ -271,7 +271,7 @@ __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const
       oaddr[i] = sbase + (pm ? (uint32_t)(line + (jo << t.log2m)) * kW : (uint32_t)(t.addr(line, jo) * (int)kW));
     }
   }
-  cta_barrier<(R == 16 ? 1 : R)>();
+  cta_barrier<(R == 16 ? 1 : (R == 32 ? 6 : R))>();
 #pragma unroll
   for (int i = 0; i < MAXB; ++i) {
     if (live[i]) {
@@ -279,7 +279,7 @@ __device__ __forceinline__ void stage_reg(const Tile<P>& t, int N, int ns, const
       for (int q = 0; q < R; ++q) sts(oaddr[i] + q * ostride, P::to_w(v[i][q]));
     }
   }
-  cta_barrier<(R == 16 ? 1 : R)>();
+  cta_barrier<(R == 16 ? 1 : (R == 32 ? 6 : R))>();
 }
 
 // Generic prime radix p: twiddle the inputs into scratch, then each output is
@@ -362,20 +362,23 @@ template <class P, int DIR, int E = kElemsPerThread, int LAY = kAnyLayout, int R
 __device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __restrict__ sp,
                                         const float4* __restrict__ tw, int tw_base = 0) {
   const int N = __ldg(&sp->n);
-  int c[6];
+  int c[7];
 #pragma unroll
-  for (int i = 0; i < 6; ++i) c[i] = __ldg(&sp->cnt[i]);
+  for (int i = 0; i < 7; ++i) c[i] = __ldg(&sp->cnt[i]);
   const int nst = __ldg(&sp->nstages);
   int ns = 1;
   int off = __ldg(&sp->tw_off[0]) - tw_base;
   bool raw = RAW != kRawNone;
-  if constexpr (!P::kF64) run_family<P, DIR, 16, E, LAY, RAW>(t, tw, N, c[0], ns, off, raw);
-  run_family<P, DIR, 8, E, LAY, RAW>(t, tw, N, c[1], ns, off, raw);
-  run_family<P, DIR, 4, E, LAY, RAW>(t, tw, N, c[2], ns, off, raw);
-  run_family<P, DIR, 2, E, LAY, RAW>(t, tw, N, c[3], ns, off, raw);
-  run_family<P, DIR, 3, E, LAY, RAW>(t, tw, N, c[4], ns, off, raw);
-  run_family<P, DIR, 5, E, LAY, RAW>(t, tw, N, c[5], ns, off, raw);
-  const int sg = c[0] + c[1] + c[2] + c[3] + c[4] + c[5];
+  if constexpr (!P::kF64) {
+    run_family<P, DIR, 32, E, LAY, RAW>(t, tw, N, c[0], ns, off, raw);
+    run_family<P, DIR, 16, E, LAY, RAW>(t, tw, N, c[1], ns, off, raw);
+  }
+  run_family<P, DIR, 8, E, LAY, RAW>(t, tw, N, c[2], ns, off, raw);
+  run_family<P, DIR, 4, E, LAY, RAW>(t, tw, N, c[3], ns, off, raw);
+  run_family<P, DIR, 2, E, LAY, RAW>(t, tw, N, c[4], ns, off, raw);
+  run_family<P, DIR, 3, E, LAY, RAW>(t, tw, N, c[5], ns, off, raw);
+  run_family<P, DIR, 5, E, LAY, RAW>(t, tw, N, c[6], ns, off, raw);
+  const int sg = c[0] + c[1] + c[2] + c[3] + c[4] + c[5] + c[6];
 #pragma unroll 1
   for (int s = sg; s < nst; ++s)
     stage_generic<P, DIR>(t, N, __ldg(&sp->radix[s]), __ldg(&sp->ns[s]), tw + (__ldg(&sp->tw_off[s]) - tw_base),

@@ -47,25 +47,31 @@ P3G_D unsigned char* align1k(unsigned char* p) {
 
 // Tiles hold at most 4096 (F64) or 8192 (F32) elements; a thread holds
 // kE of them per stage (8 on the F64 path: 512 threads, 16 warps per SM to
-// hide the latency of the dependent double-float chains; 16 on F32).
+// hide the latency of the dependent double-float chains; 32 on F32, where one
+// radix-32 butterfly per thread and stage takes a 1024-point line through two
+// stages).
 template <class P>
 struct PipeLimits {
-  static constexpr int kE = P::kF64 ? 8 : 16;
+  static constexpr int kE = P::kF64 ? 8 : 32;
   static constexpr int kMaxThreads = (P::kF64 ? 4096 : 8192) / kE;
-  // caps registers at 128 per thread: with a larger budget the scheduler
-  // hoists shared-memory loads across codelets and spills
-  static constexpr int kMinBlocks = 65536 / 128 / kMaxThreads;
+  // F64: caps registers at 128 per thread (with a larger budget the scheduler
+  // hoists shared-memory loads across codelets and spills); F32: one
+  // 256-thread CTA per SM (its two 64 KB tiles fill shared memory) with up to
+  // 255 registers for the 32-point butterflies
+  static constexpr int kMinBlocks = P::kF64 ? 65536 / 128 / kMaxThreads : 1;
 };
 
-// X passes: 256-thread CTAs, three per SM (85 registers), with the twiddles
-// read from the global table through L1 instead of a shared-memory copy, which
-// leaves room for three double-buffered tiles per SM.  The X passes gain from
-// the extra resident warps; the strided passes, whose tiles must stay wide for
-// their long-stride DRAM rows, keep PipeLimits.
+// X passes: 256-thread CTAs, three per SM (85 registers) on the F64 path and
+// 128-thread CTAs, three per SM (170 registers, for the radix-32 stages) on
+// F32, with the twiddles read from the global table through L1 instead of a
+// shared-memory copy, which leaves room for three double-buffered tiles per
+// SM.  The X passes gain from the extra resident CTAs; the strided passes,
+// whose tiles must stay wide for their long-stride DRAM rows, keep
+// PipeLimits.
 template <class P>
 struct XPipeLimits {
   static constexpr int kE = PipeLimits<P>::kE;
-  static constexpr int kMaxThreads = 256;
+  static constexpr int kMaxThreads = P::kF64 ? 256 : 128;
   static constexpr int kMinBlocks = 3;
 };
 
@@ -257,7 +263,7 @@ P3G_D void strided_fix(const SParams& s, bool tma, typename P::W* sm, int k, uin
 // Store of a transformed strided tile with the pruning map and the output
 // format (DST-I output rows k+1 times i).
 template <class P>
-P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int o1, int o2, int k) {
+P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int o1, int o2, int kb) {
   using C = typename P::C;
   const int M = s.M;
   const int ph = strided_phase(s, o1, o2);  // the tile's columns as loaded by strided_copy
@@ -270,7 +276,7 @@ P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int 
     C v;
     if (s.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
     else v = P::from_w(sm[k * M + m]);
-    store_elem<P>(s.out, s.out_user, obase + (long long)c * s.out_xs + (long long)jo * s.out_axis, v, k);
+    store_elem<P>(s.out, s.out_user, obase + (long long)c * s.out_xs + (long long)jo * s.out_axis, v, kb);
   };
   const int T = blockDim.x;
   if (s.out_xs == 1 && s.post == 0 && (s.smap_s0 >= s.Lout || s.smap_d == 0) && (T & (M - 1)) == 0) {
@@ -289,7 +295,7 @@ P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int 
     if (s.out_user) {
       typename P::UC* d = static_cast<typename P::UC*>(s.out) + o;
 #pragma unroll 4
-      for (int jo = j0; jo < s.Lout; jo += js, a += astep, d += ostep) *d = P::to_uc(P::from_w(lds(a, (W*)nullptr)), k);
+      for (int jo = j0; jo < s.Lout; jo += js, a += astep, d += ostep) *d = P::to_uc(P::from_w(lds(a, (W*)nullptr)), kb);
     } else {
       W* d = static_cast<W*>(s.out) + o;
 #pragma unroll 4

@@ -58,10 +58,12 @@ cudaError_t opt_in_smem(const void* func, int bytes) {
   } while (0)
 
 // ------------------------------------------------------------ factorisation
-// Stage radices for length n, ordered by family (16, 8, 4, 2, 3, 5, other
-// primes) as cta_fft expects.  Powers of two use the largest radix allowed
-// (max_pow2: 16 only on the F32 path, 8 by default on F64, 4 or 2 when a
-// tuner asks) with a smaller remainder.
+// Stage radices for length n, ordered by family (32, 16, 8, 4, 2, 3, 5,
+// other primes) as cta_fft expects.  Powers of two use the largest radix
+// allowed (max_pow2: 32 or 16 only on the F32 path, 8 by default on F64, 4 or
+// 2 when a tuner asks) with a smaller remainder; with 32 the 2^a factor is
+// split into the fewest stages of at most 32, as evenly as possible
+// (1024 = 32 x 32, 512 = 32 x 16, 256 = 16 x 16, 128 = 16 x 8).
 static bool factor(int n, int max_pow2, std::vector<int>& radices) {
   radices.clear();
   int a = 0;
@@ -70,6 +72,14 @@ static bool factor(int n, int max_pow2, std::vector<int>& radices) {
     ++a;
   }
   std::vector<int> pow2;
+  if (max_pow2 >= 32 && a > 0) {
+    const int st = (a + 4) / 5;
+    for (int i = 0; i < st; ++i) {
+      const int bits = a / st + (i < a % st ? 1 : 0);
+      pow2.push_back(1 << bits);
+    }
+    a = 0;
+  }
   if (max_pow2 <= 4) {
     while (a >= 2 && max_pow2 == 4) {
       pow2.push_back(4);
@@ -100,7 +110,7 @@ static bool factor(int n, int max_pow2, std::vector<int>& radices) {
   } else if (a == 3) {
     pow2.push_back(8);
   }
-  for (int r : {16, 8, 4, 2})
+  for (int r : {32, 16, 8, 4, 2})
     for (int x : pow2)
       if (x == r) radices.push_back(r);
   for (int p : {3, 5}) {
@@ -152,12 +162,13 @@ static bool build_stages(int n, int max_pow2, HostTw& tw, StagePlan& sp) {
     sp.radix[s] = r;
     sp.ns[s] = ns;
     switch (r) {
-      case 16: sp.cnt[0]++; break;
-      case 8: sp.cnt[1]++; break;
-      case 4: sp.cnt[2]++; break;
-      case 2: sp.cnt[3]++; break;
-      case 3: sp.cnt[4]++; break;
-      case 5: sp.cnt[5]++; break;
+      case 32: sp.cnt[0]++; break;
+      case 16: sp.cnt[1]++; break;
+      case 8: sp.cnt[2]++; break;
+      case 4: sp.cnt[3]++; break;
+      case 2: sp.cnt[4]++; break;
+      case 3: sp.cnt[5]++; break;
+      case 5: sp.cnt[6]++; break;
       default: sp.has_generic = 1; break;
     }
     sp.tw_off[s] = (int)tw.v.size();
@@ -168,7 +179,7 @@ static bool build_stages(int n, int max_pow2, HostTw& tw, StagePlan& sp) {
       tw.push_root(0, 1);  // keep offsets valid
     }
     sp.root_off[s] = (int)tw.v.size();
-    if (r != 2 && r != 3 && r != 4 && r != 5 && r != 8 && r != 16)
+    if (r != 2 && r != 3 && r != 4 && r != 5 && r != 8 && r != 16 && r != 32)
       for (int m = 0; m < r; ++m) tw.push_root(m, r);
     ns *= r;
   }
@@ -238,7 +249,9 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
     const int t = threads_for(M);
     size_t bb;
     const size_t sm = smem_for(M, bb);
-    const int regs = xk ? 65536 / (XPipeLimits<PathF64>::kMaxThreads * XPipeLimits<PathF64>::kMinBlocks) : 128;
+    const int regs = !xk ? 128
+                     : (f64 ? 65536 / (XPipeLimits<PathF64>::kMaxThreads * XPipeLimits<PathF64>::kMinBlocks)
+                            : 65536 / (XPipeLimits<PathF32>::kMaxThreads * XPipeLimits<PathF32>::kMinBlocks));
     int b = 65536 / (regs * t);
     b = std::min(b, 2048 / t);
     b = std::min(b, (int)((228 * 1024) / sm));
@@ -1077,8 +1090,8 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
                           int layout, int flags, int max_radix, int max_lines) {
   if (!out) return fail(P3G_E_ARG, "plan pointer is NULL");
   if (max_radix != 0 && max_radix != 2 && max_radix != 4 && max_radix != 8 &&
-      !(max_radix == 16 && precision == P3G_F32))
-    return fail(P3G_E_ARG, "max_radix must be 0, 2, 4, 8 (or 16 on the F32 path)");
+      !((max_radix == 16 || max_radix == 32) && precision == P3G_F32))
+    return fail(P3G_E_ARG, "max_radix must be 0, 2, 4, 8 (or 16, 32 on the F32 path)");
   if (max_lines < 0 || (max_lines & (max_lines - 1)) != 0)
     return fail(P3G_E_ARG, "max_lines must be 0 or a power of two");
   *out = nullptr;
@@ -1117,7 +1130,7 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
   int strided_max_m = f64 ? 64 : 128;  // 256 words per TMA box row
   const int x_max_m = max_lines > 0 ? max_lines : (1 << 30);
   if (max_lines > 0 && max_lines < strided_max_m) strided_max_m = max_lines;
-  const int max_pow2 = max_radix > 0 ? max_radix : (f64 ? 8 : 16);
+  const int max_pow2 = max_radix > 0 ? max_radix : (f64 ? 8 : 32);
   auto add_axis = [&](AxisPlan& ap, int n, int lines) -> bool {
     if (!build_stages(n, max_pow2, tw, ap.sp)) return false;
     ap.tw_lo = tw.mark;
