@@ -163,7 +163,7 @@ template <class P>
 cudaError_t launch_xr2c_pipe(const XPipeParams& p, const StagePlan* sp, const float4* tw, int E, int threads,
                              size_t smem, int grid, cudaStream_t st);
 template <class P>
-int pipe_blocks_per_sm(int kind, int threads, size_t smem);
+int pipe_blocks_per_sm(int kind, int E, int threads, size_t smem);
 template <class P>
 cudaError_t launch_xc2r_pipe(const XPipeParams& p, const StagePlan* sp, const float4* tw, int E, int threads,
                              size_t smem, int grid, cudaStream_t st);

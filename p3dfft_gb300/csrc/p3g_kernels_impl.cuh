@@ -291,42 +291,75 @@ cudaError_t launch_cheby(const ChebyParams& p, int nfields, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// Pipelined launchers: E (elements per thread) selects the instantiation.
+template <class P, int E>
+cudaError_t launch_strided_pipe_e(const CUtensorMap* map, const SPipeParams& p, const StagePlan* sp,
+                                  const float4* tw, bool forward_sign, int threads, size_t smem, int grid,
+                                  cudaStream_t st) {
+  cudaError_t ea = opt_in_smem((const void*)k_strided_pipe<P, -1, E>, 227 * 1024);
+  if (ea == cudaSuccess) ea = opt_in_smem((const void*)k_strided_pipe<P, 1, E>, 227 * 1024);
+  if (ea != cudaSuccess) return ea;
+  if (forward_sign) k_strided_pipe<P, -1, E><<<grid, threads, smem, st>>>(*map, p, sp, tw);
+  else k_strided_pipe<P, 1, E><<<grid, threads, smem, st>>>(*map, p, sp, tw);
+  return cudaGetLastError();
+}
 template <class P>
 cudaError_t launch_strided_pipe(const CUtensorMap* map, const SPipeParams& p, const StagePlan* sp, const float4* tw,
                                 bool forward_sign, int E, int threads, size_t smem, int grid, cudaStream_t st) {
-  cudaError_t ea = opt_in_smem((const void*)k_strided_pipe<P, -1>, 227 * 1024);
-  if (ea == cudaSuccess) ea = opt_in_smem((const void*)k_strided_pipe<P, 1>, 227 * 1024);
+  if constexpr (P::kF64) {
+    if (E == 8) return launch_strided_pipe_e<P, 8>(map, p, sp, tw, forward_sign, threads, smem, grid, st);
+  } else {
+    if (E == 16) return launch_strided_pipe_e<P, 16>(map, p, sp, tw, forward_sign, threads, smem, grid, st);
+    if (E == 32) return launch_strided_pipe_e<P, 32>(map, p, sp, tw, forward_sign, threads, smem, grid, st);
+  }
+  return cudaErrorInvalidValue;
+}
+template <class P, int E>
+cudaError_t launch_xr2c_pipe_e(const XPipeParams& p, const StagePlan* sp, const float4* tw, int threads, size_t smem,
+                               int grid, cudaStream_t st) {
+  cudaError_t ea = opt_in_smem((const void*)k_xr2c_pipe<P, E>, 227 * 1024);
   if (ea != cudaSuccess) return ea;
-  (void)E;
-  if (forward_sign) k_strided_pipe<P, -1><<<grid, threads, smem, st>>>(*map, p, sp, tw);
-  else k_strided_pipe<P, 1><<<grid, threads, smem, st>>>(*map, p, sp, tw);
+  k_xr2c_pipe<P, E><<<grid, threads, smem, st>>>(p, sp, tw);
   return cudaGetLastError();
 }
 template <class P>
 cudaError_t launch_xr2c_pipe(const XPipeParams& p, const StagePlan* sp, const float4* tw, int E, int threads,
                              size_t smem, int grid, cudaStream_t st) {
-  cudaError_t ea = opt_in_smem((const void*)k_xr2c_pipe<P>, 227 * 1024);
+  if constexpr (P::kF64) {
+    if (E == 8) return launch_xr2c_pipe_e<P, 8>(p, sp, tw, threads, smem, grid, st);
+  } else {
+    if (E == 16) return launch_xr2c_pipe_e<P, 16>(p, sp, tw, threads, smem, grid, st);
+    if (E == 32) return launch_xr2c_pipe_e<P, 32>(p, sp, tw, threads, smem, grid, st);
+  }
+  return cudaErrorInvalidValue;
+}
+template <class P, int E>
+cudaError_t launch_xc2r_pipe_e(const XPipeParams& p, const StagePlan* sp, const float4* tw, int threads, size_t smem,
+                               int grid, cudaStream_t st) {
+  cudaError_t ea = opt_in_smem((const void*)k_xc2r_pipe<P, E>, 227 * 1024);
   if (ea != cudaSuccess) return ea;
-  (void)E;
-  k_xr2c_pipe<P><<<grid, threads, smem, st>>>(p, sp, tw);
+  k_xc2r_pipe<P, E><<<grid, threads, smem, st>>>(p, sp, tw);
   return cudaGetLastError();
 }
 template <class P>
 cudaError_t launch_xc2r_pipe(const XPipeParams& p, const StagePlan* sp, const float4* tw, int E, int threads,
                              size_t smem, int grid, cudaStream_t st) {
-  cudaError_t ea = opt_in_smem((const void*)k_xc2r_pipe<P>, 227 * 1024);
-  if (ea != cudaSuccess) return ea;
-  (void)E;
-  k_xc2r_pipe<P><<<grid, threads, smem, st>>>(p, sp, tw);
-  return cudaGetLastError();
+  if constexpr (P::kF64) {
+    if (E == 8) return launch_xc2r_pipe_e<P, 8>(p, sp, tw, threads, smem, grid, st);
+  } else {
+    if (E == 16) return launch_xc2r_pipe_e<P, 16>(p, sp, tw, threads, smem, grid, st);
+    if (E == 32) return launch_xc2r_pipe_e<P, 32>(p, sp, tw, threads, smem, grid, st);
+  }
+  return cudaErrorInvalidValue;
 }
 
 // Resident CTAs per SM of a pipelined kernel (kind 0 strided, 1 r2c, 2 c2r)
-// for the given block size and dynamic shared memory; 1 if the query fails.
-template <class P>
-int pipe_blocks_per_sm(int kind, int threads, size_t smem) {
-  const void* f = kind == 0 ? (const void*)k_strided_pipe<P, -1>
-                            : (kind == 1 ? (const void*)k_xr2c_pipe<P> : (const void*)k_xc2r_pipe<P>);
+// with E elements per thread for the given block size and dynamic shared
+// memory; 1 if the query fails.
+template <class P, int E>
+int pipe_blocks_per_sm_e(int kind, int threads, size_t smem) {
+  const void* f = kind == 0 ? (const void*)k_strided_pipe<P, -1, E>
+                            : (kind == 1 ? (const void*)k_xr2c_pipe<P, E> : (const void*)k_xc2r_pipe<P, E>);
   int n = 0;
   if (opt_in_smem(f, 227 * 1024) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem) != cudaSuccess || n < 1) {
@@ -334,6 +367,15 @@ int pipe_blocks_per_sm(int kind, int threads, size_t smem) {
     return 1;
   }
   return n;
+}
+template <class P>
+int pipe_blocks_per_sm(int kind, int E, int threads, size_t smem) {
+  if constexpr (P::kF64) {
+    return pipe_blocks_per_sm_e<P, 8>(kind, threads, smem);
+  } else {
+    return E == 32 ? pipe_blocks_per_sm_e<P, 32>(kind, threads, smem)
+                   : pipe_blocks_per_sm_e<P, 16>(kind, threads, smem);
+  }
 }
 
 #define P3G_INSTANTIATE(P)                                                                                          \
@@ -344,7 +386,7 @@ int pipe_blocks_per_sm(int kind, int threads, size_t smem) {
   template cudaError_t launch_strided<P>(const SParams&, const StagePlan*, const float4*, bool, int, size_t, int,  \
                                          cudaStream_t);                                                            \
   template cudaError_t launch_cheby<P>(const ChebyParams&, int, cudaStream_t);                                     \
-  template int pipe_blocks_per_sm<P>(int, int, size_t);                                                            \
+  template int pipe_blocks_per_sm<P>(int, int, int, size_t);                                                            \
   template cudaError_t launch_strided_pipe<P>(const CUtensorMap*, const SPipeParams&, const StagePlan*,             \
                                               const float4*, bool, int, int, size_t, int, cudaStream_t);          \
   template cudaError_t launch_xr2c_pipe<P>(const XPipeParams&, const StagePlan*, const float4*, int, int, size_t,  \

@@ -45,35 +45,38 @@ P3G_D unsigned char* align1k(unsigned char* p) {
   return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
 }
 
-// Tiles hold at most 4096 (F64) or 8192 (F32) elements; a thread holds
-// kE of them per stage (8 on the F64 path: 512 threads, 16 warps per SM to
-// hide the latency of the dependent double-float chains; 32 on F32, where one
-// radix-32 butterfly per thread and stage takes a 1024-point line through two
-// stages).
-template <class P>
+// Tiles hold at most 4096 (F64) or 8192 (F32) elements; a thread holds E
+// of them per stage: 8 on the F64 path (512 threads, 16 warps per SM to hide
+// the latency of the dependent double-float chains); on the F32 path 32 for
+// axes with radix-32 stages (one 32-point butterfly per thread and stage
+// takes a 1024-point line through two stages) and 16 otherwise.
+template <class P, int E>
 struct PipeLimits {
-  static constexpr int kE = P::kF64 ? 8 : 32;
-  static constexpr int kMaxThreads = (P::kF64 ? 4096 : 8192) / kE;
-  // F64: caps registers at 128 per thread (with a larger budget the scheduler
-  // hoists shared-memory loads across codelets and spills); F32: one
-  // 256-thread CTA per SM (its two 64 KB tiles fill shared memory) with up to
-  // 255 registers for the 32-point butterflies
-  static constexpr int kMinBlocks = P::kF64 ? 65536 / 128 / kMaxThreads : 1;
+  static constexpr int kMaxThreads = (P::kF64 ? 4096 : 8192) / E;
+  // 128 registers per thread (with a larger budget the scheduler hoists
+  // shared-memory loads across codelets and spills), except for the F32
+  // radix-32 kernel: one 256-thread CTA per SM (its two 64 KB tiles fill
+  // shared memory) with up to 255 registers for the 32-point butterflies
+  static constexpr int kMinBlocks = (!P::kF64 && E == 32) ? 1 : 65536 / 128 / kMaxThreads;
 };
 
-// X passes: 256-thread CTAs, three per SM (85 registers) on the F64 path and
-// 128-thread CTAs, three per SM (170 registers, for the radix-32 stages) on
-// F32, with the twiddles read from the global table through L1 instead of a
-// shared-memory copy, which leaves room for three double-buffered tiles per
-// SM.  The X passes gain from the extra resident CTAs; the strided passes,
-// whose tiles must stay wide for their long-stride DRAM rows, keep
-// PipeLimits.
-template <class P>
+// X passes: 256-thread CTAs, three per SM (85 registers; 128-thread CTAs
+// with up to 170 registers for the F32 radix-32 stages), with the twiddles
+// read from the global table through L1 instead of a shared-memory copy,
+// which leaves room for three double-buffered tiles per SM.  The X passes
+// gain from the extra resident CTAs; the strided passes, whose tiles must
+// stay wide for their long-stride DRAM rows, keep PipeLimits.
+template <class P, int E>
 struct XPipeLimits {
-  static constexpr int kE = PipeLimits<P>::kE;
-  static constexpr int kMaxThreads = P::kF64 ? 256 : 128;
+  static constexpr int kMaxThreads = (!P::kF64 && E == 32) ? 128 : 256;
   static constexpr int kMinBlocks = 3;
 };
+
+// Per-thread element counts the pipelined kernels are built for.
+template <class P>
+constexpr bool pipe_e_ok(int E) {
+  return P::kF64 ? E == 8 : (E == 16 || E == 32);
+}
 
 // ------------------------------------------------------------ strided Y/Z
 template <class P>
@@ -321,8 +324,8 @@ P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int 
   }
 }
 
-template <class P, int DIR>
-__global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMinBlocks)
+template <class P, int DIR, int E>
+__global__ void __launch_bounds__(PipeLimits<P, E>::kMaxThreads, PipeLimits<P, E>::kMinBlocks)
     k_strided_pipe(const __grid_constant__ CUtensorMap tin, const __grid_constant__ SPipeParams pp,
                    const StagePlan* __restrict__ sp, const float4* __restrict__ tw_g) {
   {
@@ -360,7 +363,7 @@ __global__ void __launch_bounds__(PipeLimits<P>::kMaxThreads, PipeLimits<P>::kMi
       const SPipeParams& q = pp;
       const StridedSmem<P> sm = strided_smem<P>(q.c);
       Tile<P> t{sm.buf0 + b * q.c.buf_elems, nullptr, q.s.M, q.s.log2m, 1, q.s.M};
-      cta_fft<P, DIR, PipeLimits<P>::kE, kPointMajor>(t, sp, sm.tw, q.c.tw_base);
+      cta_fft<P, DIR, E, kPointMajor>(t, sp, sm.tw, q.c.tw_base);
     }
     {
       int xt, o1, o2;
@@ -486,8 +489,8 @@ P3G_D void xr2c_store(const XParams& x, const typename P::W* sm, int p0, int fie
   else xr2c_store_t<P, false>(x, sm, p0, field, kb);
 }
 
-template <class P>
-__global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::kMinBlocks)
+template <class P, int E>
+__global__ void __launch_bounds__(XPipeLimits<P, E>::kMaxThreads, XPipeLimits<P, E>::kMinBlocks)
     k_xr2c_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
                 const float4* __restrict__ tw_g) {
   const int k = range_k(pp.x.range);
@@ -506,7 +509,7 @@ __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::k
     {
       // the first FFT stage reads the raw line pairs (packing fused into it)
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps, k, &amax};
-      cta_fft<P, -1, XPipeLimits<P>::kE, kLineMajor, kRawR2C>(t, sp, tw_g, 0);
+      cta_fft<P, -1, E, kLineMajor, kRawR2C>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;
@@ -648,8 +651,8 @@ P3G_D void xc2r_store(const XParams& x, const typename P::W* sm, int p0, int fie
   }
 }
 
-template <class P>
-__global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::kMinBlocks)
+template <class P, int E>
+__global__ void __launch_bounds__(XPipeLimits<P, E>::kMaxThreads, XPipeLimits<P, E>::kMinBlocks)
     k_xc2r_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
                 const float4* __restrict__ tw_g) {
   const int k = range_k(pp.x.range);
@@ -667,7 +670,7 @@ __global__ void __launch_bounds__(XPipeLimits<P>::kMaxThreads, XPipeLimits<P>::k
     {
       // the first FFT stage reads the raw half spectra (Hermitian merge fused into it)
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
-      cta_fft<P, 1, XPipeLimits<P>::kE, kLineMajor, kRawC2R>(t, sp, tw_g, 0);
+      cta_fft<P, 1, E, kLineMajor, kRawC2R>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;

@@ -218,16 +218,30 @@ static bool size_tile(AxisPlan& ap, int n, int lines_avail, bool f64, int max_m 
   return ap.smem <= 227 * 1024;
 }
 
+// Launch shape of a pipelined kernel with E elements per thread: the most
+// threads per CTA and the registers per thread its launch bounds allow.
+template <class P, int E>
+static void pipe_shape(bool xk, int& max_threads, int& regs) {
+  max_threads = xk ? XPipeLimits<P, E>::kMaxThreads : PipeLimits<P, E>::kMaxThreads;
+  const int blocks = xk ? XPipeLimits<P, E>::kMinBlocks : PipeLimits<P, E>::kMinBlocks;
+  regs = std::min(255, 65536 / (max_threads * blocks));
+}
+
 // Pipelined kernels: two tile buffers (1 KB aligned), the axis's twiddles
-// and two mbarriers in shared memory.  kind: 0 strided, 1 r2c, 2 c2r.
+// and two mbarriers in shared memory.  kind: 0 strided, 1 r2c, 2 c2r.  The
+// elements per thread follow the axis's stages: 8 on the F64 path; on F32, 32
+// when a radix-32 stage is present, else 16.
 static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   ap.pipe_ok = false;
   if (ap.sp.nstages < 1 || ap.sp.has_generic || ap.n < 2) return;
   const size_t esize = f64 ? 16 : 8;
   const bool xk = kind != 0;  // X kernels have their own launch shape (XPipeLimits)
-  const int max_threads = f64 ? (xk ? XPipeLimits<PathF64>::kMaxThreads : PipeLimits<PathF64>::kMaxThreads)
-                              : (xk ? XPipeLimits<PathF32>::kMaxThreads : PipeLimits<PathF32>::kMaxThreads);
-  const int E = f64 ? PipeLimits<PathF64>::kE : PipeLimits<PathF32>::kE;
+  const int E = f64 ? 8 : (ap.sp.cnt[0] > 0 ? 32 : 16);
+  ap.pipe_e = E;
+  int max_threads = 0, regs_max = 0;
+  if (f64) pipe_shape<PathF64, 8>(xk, max_threads, regs_max);
+  else if (E == 32) pipe_shape<PathF32, 32>(xk, max_threads, regs_max);
+  else pipe_shape<PathF32, 16>(xk, max_threads, regs_max);
   const bool tw_shared = !xk;  // the X kernels read the global table
   const int n = ap.n;
   const int nh = n / 2 + 1;
@@ -249,9 +263,7 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
     const int t = threads_for(M);
     size_t bb;
     const size_t sm = smem_for(M, bb);
-    const int regs = !xk ? 128
-                     : (f64 ? 65536 / (XPipeLimits<PathF64>::kMaxThreads * XPipeLimits<PathF64>::kMinBlocks)
-                            : 65536 / (XPipeLimits<PathF32>::kMaxThreads * XPipeLimits<PathF32>::kMinBlocks));
+    const int regs = regs_max;
     int b = 65536 / (regs * t);
     b = std::min(b, 2048 / t);
     b = std::min(b, (int)((228 * 1024) / sm));
@@ -468,7 +480,7 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
     }
     const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
     const int grid = pp.c.ntiles < slots ? pp.c.ntiles : slots;
-    cudaError_t e = launch_strided_pipe<P>(&map, pp, p->d_sp + ap.sp_index, p->d_tw, fwd_sign, kElemsPerThread,
+    cudaError_t e = launch_strided_pipe<P>(&map, pp, p->d_sp + ap.sp_index, p->d_tw, fwd_sign, ap.pipe_e,
                                            ap.pipe_threads, ap.pipe_smem, grid, st);
     if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("strided pass launch: ") + cudaGetErrorString(e));
     p->launches++;
@@ -503,7 +515,7 @@ int run_x_r2c(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) 
     xp.c.err = p->d_err;
     const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
     const int grid = xp.c.ntiles < slots ? xp.c.ntiles : slots;
-    cudaError_t e = launch_xr2c_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, kElemsPerThread, ap.pipe_threads,
+    cudaError_t e = launch_xr2c_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, ap.pipe_e, ap.pipe_threads,
                                         ap.pipe_smem, grid, st);
     if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X r2c launch: ") + cudaGetErrorString(e));
     p->launches++;
@@ -533,7 +545,7 @@ int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) 
     xp.c.err = p->d_err;
     const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
     const int grid = xp.c.ntiles < slots ? xp.c.ntiles : slots;
-    cudaError_t e = launch_xc2r_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, kElemsPerThread, ap.pipe_threads,
+    cudaError_t e = launch_xc2r_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, ap.pipe_e, ap.pipe_threads,
                                         ap.pipe_smem, grid, st);
     if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X c2r launch: ") + cudaGetErrorString(e));
     p->launches++;
@@ -1130,9 +1142,16 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
   int strided_max_m = f64 ? 64 : 128;  // 256 words per TMA box row
   const int x_max_m = max_lines > 0 ? max_lines : (1 << 30);
   if (max_lines > 0 && max_lines < strided_max_m) strided_max_m = max_lines;
-  const int max_pow2 = max_radix > 0 ? max_radix : (f64 ? 8 : 32);
+  // largest power-of-two radix: the tuner's cap, else 8 on the F64 path; on
+  // F32, 32 for power-of-two lengths (their radix-32 stages run with 32
+  // elements per thread) and 16 for the mixed-radix ones
+  auto axis_pow2 = [&](int n) {
+    if (max_radix > 0) return max_radix;
+    if (f64) return 8;
+    return (n & (n - 1)) == 0 ? 32 : 16;
+  };
   auto add_axis = [&](AxisPlan& ap, int n, int lines) -> bool {
-    if (!build_stages(n, max_pow2, tw, ap.sp)) return false;
+    if (!build_stages(n, axis_pow2(n), tw, ap.sp)) return false;
     ap.tw_lo = tw.mark;
     ap.tw_cnt = (int)tw.v.size() - tw.mark;
     if (!size_tile(ap, n, lines, f64, &ap == &p->ax_x ? x_max_m : strided_max_m)) return false;
@@ -1202,8 +1221,8 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
   {
     auto bps = [&](AxisPlan& ap, int kind) {
       if (ap.pipe_ok)
-        ap.pipe_bps = f64 ? pipe_blocks_per_sm<PathF64>(kind, ap.pipe_threads, ap.pipe_smem)
-                          : pipe_blocks_per_sm<PathF32>(kind, ap.pipe_threads, ap.pipe_smem);
+        ap.pipe_bps = f64 ? pipe_blocks_per_sm<PathF64>(kind, ap.pipe_e, ap.pipe_threads, ap.pipe_smem)
+                          : pipe_blocks_per_sm<PathF32>(kind, ap.pipe_e, ap.pipe_threads, ap.pipe_smem);
     };
     bps(p->ax_x, 2);
     bps(p->ax_y, 0);

@@ -29,6 +29,7 @@ struct AxisPlan {
   int buf_elems = 0;
   size_t pipe_smem = 0;
   int pipe_bps = 1;  // resident CTAs per SM of the pipelined kernel
+  int pipe_e = 8;    // elements per thread of the pipelined kernel (PipeLimits)
 };
 
 struct TimerRec {
