@@ -601,8 +601,11 @@ def run_serving(torch, pg, n_requests, plain_f64_gpts, slots=3):
     loop (all requests queued at once); the timed stream then arrives as a
     Poisson process at 70 % of that capacity."""
     from p3dfft_gb300 import serve
+    # every request brings its own host input and takes its result back to
+    # the host (views rotating through two 2 GiB page-locked arenas)
     cap_reqs = serve.make_requests(min(600, n_requests), seed=50)
     reqs = serve.poisson_arrivals(serve.make_requests(n_requests, seed=5), rate=1.0)  # rate set below
+    serve.attach_host_data(cap_reqs + reqs, arena_bytes=2 << 30)
     srv = serve.Server(budget_bytes=150e9, slots=slots, max_jobs=64, window=4, keep_outputs=False,
                        launch_work=40e6, age_limit=0.008)
     t = time.time()
@@ -629,6 +632,9 @@ def run_serving(torch, pg, n_requests, plain_f64_gpts, slots=3):
                                                             or [0])), 2),
                 "slots": len(srv.slots), "plans_resident": len(srv.plans), "plan_setup_s": round(plan_s, 1),
                 "mix": "forward:backward:spectrum 4:4:2, 10% FP64",
+                "data": "per request: H2D of its own input and D2H of its result on its launch's stream, "
+                        "inside the latency",
+                "fallbacks": sum(1 for r in reqs if r.fallback),
                 "schedule": "least estimated work first, launches bounded at 40M point-equivalents, "
                             "requests waiting 8 ms first"})
     if plain_f64_gpts:

@@ -23,6 +23,7 @@ struct PipeCommon {
   int tiles_per_field;
   int tw_base, tw_count;    // this pass's slice of the twiddle table (float4)
   int buf_elems;            // elements (W) per buffer
+  int nbuf;                 // tile buffers (2 or 3): loads run nbuf - 1 tiles ahead
   int* err;                 // device error flag
 };
 
@@ -39,6 +40,10 @@ struct XPipeParams {
   XParams x;
   PipeCommon c;
   int chunk;                // r2c: cp.async bytes per copy (4, 8 or 16)
+  // 1: thread 0 loads tiles with 1-D bulk copies on an mbarrier (r2c: the
+  // tile's 2M contiguous real lines in one copy, full tiles only; c2r: one
+  // copy per line of every mode), else every thread issues cp.async
+  int bulk;
 };
 
 P3G_D unsigned char* align1k(unsigned char* p) {
@@ -90,7 +95,7 @@ P3G_D StridedSmem<P> strided_smem(const PipeCommon& pc) {
   extern __shared__ unsigned char p3g_pipe_smem[];
   StridedSmem<P> r;
   r.buf0 = reinterpret_cast<typename P::W*>(align1k(p3g_pipe_smem));
-  r.tw = reinterpret_cast<float4*>(r.buf0 + 2 * pc.buf_elems);
+  r.tw = reinterpret_cast<float4*>(r.buf0 + pc.nbuf * pc.buf_elems);
   r.mbar = reinterpret_cast<uint64_t*>(r.tw + pc.tw_count);
   return r;
 }
@@ -324,16 +329,23 @@ P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int 
   }
 }
 
+// Waits for the copies of tile slot it (buffer it % nbuf): cp.async groups
+// (nbuf - 1 may stay in flight) or the TMA mbarrier; false after a time-out.
+P3G_D void cp_async_wait_ahead(int nbuf) {
+  if (nbuf >= 3) cp_async_wait<2>();
+  else cp_async_wait<1>();
+}
+
 template <class P, int DIR, int E>
 __global__ void __launch_bounds__(PipeLimits<P, E>::kMaxThreads, PipeLimits<P, E>::kMinBlocks)
     k_strided_pipe(const __grid_constant__ CUtensorMap tin, const __grid_constant__ SPipeParams pp,
                    const StagePlan* __restrict__ sp, const float4* __restrict__ tw_g) {
+  const int nb = pp.c.nbuf;
   {
     const StridedSmem<P> sm = strided_smem<P>(pp.c);
     for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) sm.tw[i] = __ldg(tw_g + pp.c.tw_base + i);
     if (threadIdx.x == 0 && pp.use_tma) {
-      mbar_init(&sm.mbar[0], 1);
-      mbar_init(&sm.mbar[1], 1);
+      for (int i = 0; i < nb; ++i) mbar_init(&sm.mbar[i], 1);
       mbar_fence_init();
     }
   }
@@ -342,20 +354,23 @@ __global__ void __launch_bounds__(PipeLimits<P, E>::kMaxThreads, PipeLimits<P, E
   uint32_t amax = 0;
   int it = 0;
   int tile = blockIdx.x;
-  bool next_pending = false;
-  if (tile < pp.c.ntiles) strided_issue<P>(pp, &tin, tile, 0);
+  // tiles of the first nb - 1 iterations in flight before the loop
+  for (int j = 0; j < nb - 1; ++j) {
+    const int t = tile + j * (int)gridDim.x;
+    if (t < pp.c.ntiles) strided_issue<P>(pp, &tin, t, j);
+    else if (!pp.use_tma) cp_async_commit();
+  }
+  int b = 0, ph = 0;  // buffer of iteration it and the parity of its use
 #pragma unroll 1
   for (; tile < pp.c.ntiles; tile += gridDim.x, ++it) {
-    const int b = it & 1;
     bool ok = true;
     {
       const SPipeParams& q = pp;
-      const int next = tile + gridDim.x;
-      next_pending = next < q.c.ntiles;
-      if (next_pending) strided_issue<P>(q, &tin, next, b ^ 1);
+      const int ahead = tile + (nb - 1) * (int)gridDim.x;  // into the buffer the last iteration released
+      if (ahead < q.c.ntiles) strided_issue<P>(q, &tin, ahead, b == 0 ? nb - 1 : b - 1);
       else if (!q.use_tma) cp_async_commit();  // one group per iteration
-      if (q.use_tma) ok = mbar_wait_bounded(&strided_smem<P>(q.c).mbar[b], (it >> 1) & 1, q.c.err);
-      else cp_async_wait<1>();
+      if (q.use_tma) ok = mbar_wait_bounded(&strided_smem<P>(q.c).mbar[b], ph, q.c.err);
+      else cp_async_wait_ahead(nb);
     }
     if (__syncthreads_or(!ok)) break;
     strided_fix<P>(pp.s, pp.use_tma != 0, strided_smem<P>(pp.c).buf0 + b * pp.c.buf_elems, k, amax);
@@ -371,13 +386,19 @@ __global__ void __launch_bounds__(PipeLimits<P, E>::kMaxThreads, PipeLimits<P, E
       strided_store<P>(pp.s, strided_smem<P>(pp.c).buf0 + b * pp.c.buf_elems, xt, o1, o2, k);
     }
     __syncthreads();
+    if (++b == nb) {
+      b = 0;
+      ph ^= 1;
+    }
   }
-  // early exit after a timed-out wait: wait (bounded) for copies in flight
+  // early exit after a timed-out wait: wait (bounded) for the copies of the
+  // tiles issued and not yet consumed
   if (pp.use_tma) {
-    if (threadIdx.x == 0 && tile < pp.c.ntiles) {
+    if (threadIdx.x == 0) {
       const StridedSmem<P> sm = strided_smem<P>(pp.c);
-      mbar_wait_bounded(&sm.mbar[it & 1], (it >> 1) & 1, nullptr);
-      if (next_pending) mbar_wait_bounded(&sm.mbar[(it + 1) & 1], ((it + 1) >> 1) & 1, nullptr);
+      for (int j = 0; j < nb; ++j)
+        if (tile + j * (int)gridDim.x < pp.c.ntiles)
+          mbar_wait_bounded(&sm.mbar[(it + j) % nb], ((it + j) / nb) & 1, nullptr);
     }
   } else {
     cp_async_wait<0>();
@@ -390,6 +411,11 @@ template <class P>
 P3G_D typename P::W* xpipe_buf(const PipeCommon& pc, int b) {
   extern __shared__ unsigned char p3g_pipe_smem[];
   return reinterpret_cast<typename P::W*>(align1k(p3g_pipe_smem)) + b * pc.buf_elems;
+}
+// the bulk copies' mbarriers, one per buffer, after the buffers
+template <class P>
+P3G_D uint64_t* xpipe_mbar(const PipeCommon& pc) {
+  return reinterpret_cast<uint64_t*>(xpipe_buf<P>(pc, pc.nbuf));
 }
 
 // cp.async of CH bytes (16, 8 or 4)
@@ -447,13 +473,37 @@ P3G_D void xr2c_copy(const XParams& x, int chunk, typename P::W* dst_w, int p0, 
   }
 }
 
-template <class P>
-P3G_D void xr2c_issue(const XPipeParams& q, int tile, int b) {
+// r2c tiles that arrive by one bulk copy: bulk loads on and the tile's 2M
+// lines all inside the field (a partial tile is zero-filled by cp.async)
+P3G_D bool xr2c_tile_bulk(const XPipeParams& q, int tile) {
+  if (!q.bulk) return false;
   const int field = tile / q.c.tiles_per_field;
   const int p0 = (tile - field * q.c.tiles_per_field) * q.x.M;
-  xr2c_copy<P>(q.x, q.chunk, xpipe_buf<P>(q.c, b), p0, field);
+  return 2 * (p0 + q.x.M) <= q.x.nlines;
+}
+
+// Copies of one r2c tile into buffer b: one bulk copy by thread 0 (with an
+// empty commit group so that every tile counts one group) or cp.async.
+template <class P>
+P3G_D void xr2c_issue(const XPipeParams& q, int tile, int b) {
+  using UR = typename P::UR;
+  const int field = tile / q.c.tiles_per_field;
+  const int p0 = (tile - field * q.c.tiles_per_field) * q.x.M;
+  if (xr2c_tile_bulk(q, tile)) {
+    if (threadIdx.x == 0) {
+      uint64_t* bar = xpipe_mbar<P>(q.c) + b;
+      const uint32_t bytes = (uint32_t)(2 * q.x.M * q.x.nx) * (uint32_t)sizeof(UR);
+      const UR* src = static_cast<const UR*>(q.x.in) + field * q.x.in_field + (long long)2 * p0 * q.x.nx;
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(bar, bytes);
+      bulk_load(xpipe_buf<P>(q.c, b), src, bytes, bar);
+    }
+  } else {
+    xr2c_copy<P>(q.x, q.chunk, xpipe_buf<P>(q.c, b), p0, field);
+  }
   cp_async_commit();
 }
+
 
 // X1[k] = (Z[k] + conj Z[N-k]) / 2, X2[k] = -i (Z[k] - conj Z[N-k]) / 2,
 // modes k < nkeep stored to the working layout (USER: the user complex
@@ -494,18 +544,29 @@ __global__ void __launch_bounds__(XPipeLimits<P, E>::kMaxThreads, XPipeLimits<P,
     k_xr2c_pipe(const __grid_constant__ XPipeParams pp, const StagePlan* __restrict__ sp,
                 const float4* __restrict__ tw_g) {
   const int k = range_k(pp.x.range);
+  const int nb = pp.c.nbuf;
   uint32_t amax = 0;
   int it = 0;
   int tile = blockIdx.x;
-  if (tile < pp.c.ntiles) xr2c_issue<P>(pp, tile, 0);
+  if (pp.bulk && threadIdx.x == 0) {
+    for (int i = 0; i < nb; ++i) mbar_init(xpipe_mbar<P>(pp.c) + i, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  for (int j = 0; j < nb - 1; ++j) {
+    const int t = tile + j * (int)gridDim.x;
+    if (t < pp.c.ntiles) xr2c_issue<P>(pp, t, j);
+    else cp_async_commit();
+  }
+  int b = 0, ph = 0;  // buffer of iteration it and the parity of its use
 #pragma unroll 1
   for (; tile < pp.c.ntiles; tile += gridDim.x, ++it) {
-    const int b = it & 1;
-    const int next = tile + gridDim.x;
-    if (next < pp.c.ntiles) xr2c_issue<P>(pp, next, b ^ 1);
+    const int ahead = tile + (nb - 1) * (int)gridDim.x;
+    if (ahead < pp.c.ntiles) xr2c_issue<P>(pp, ahead, b == 0 ? nb - 1 : b - 1);
     else cp_async_commit();
-    cp_async_wait<1>();
-    __syncthreads();
+    cp_async_wait_ahead(nb);
+    const bool ok = !xr2c_tile_bulk(pp, tile) || mbar_wait_bounded(xpipe_mbar<P>(pp.c) + b, ph, pp.c.err);
+    if (__syncthreads_or(!ok)) break;
     {
       // the first FFT stage reads the raw line pairs (packing fused into it)
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps, k, &amax};
@@ -517,8 +578,19 @@ __global__ void __launch_bounds__(XPipeLimits<P, E>::kMaxThreads, XPipeLimits<P,
       xr2c_store<P>(pp.x, xpipe_buf<P>(pp.c, b), p0, field, k);
     }
     __syncthreads();
+    if (++b == nb) {
+      b = 0;
+      ph ^= 1;
+    }
   }
   cp_async_wait<0>();
+  // early exit after a timed-out wait: wait (bounded) for bulk copies in flight
+  if (threadIdx.x == 0)
+    for (int j = 0; j < nb; ++j) {
+      const int t = tile + j * (int)gridDim.x;
+      if (t < pp.c.ntiles && xr2c_tile_bulk(pp, t))
+        mbar_wait_bounded(xpipe_mbar<P>(pp.c) + (it + j) % nb, ((it + j) / nb) & 1, nullptr);
+    }
   range_flush(pp.x.range, amax);
 }
 
@@ -594,11 +666,30 @@ P3G_D void xc2r_copy(const XParams& x, typename P::W* dst, int p0, int field) {
   }
 }
 
+// Copies of one c2r tile into buffer b: one bulk copy per line (the nh
+// modes rounded up to 16 bytes, into the raw line stride) by thread 0, with an
+// empty commit group, or cp.async.
 template <class P>
 P3G_D void xc2r_issue(const XPipeParams& q, int tile, int b) {
+  using W = typename P::W;
   const int field = tile / q.c.tiles_per_field;
   const int p0 = (tile - field * q.c.tiles_per_field) * q.x.M;
-  xc2r_copy<P>(q.x, xpipe_buf<P>(q.c, b), p0, field);
+  if (q.bulk) {
+    if (threadIdx.x == 0) {
+      const int nh = q.x.nx / 2 + 1;
+      const int rs = xc2r_raw_stride(nh, (int)sizeof(W));
+      const uint32_t lbytes = ((uint32_t)nh * (uint32_t)sizeof(W) + 15u) & ~15u;
+      const int nl = min(2 * q.x.M, q.x.nlines - 2 * p0);
+      uint64_t* bar = xpipe_mbar<P>(q.c) + b;
+      const W* in = static_cast<const W*>(q.x.in) + field * q.x.in_field;
+      W* dst = xpipe_buf<P>(q.c, b);
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(bar, lbytes * (uint32_t)nl);
+      for (int lt = 0; lt < nl; ++lt) bulk_load(dst + lt * rs, in + (long long)(2 * p0 + lt) * q.x.in_line, lbytes, bar);
+    }
+  } else {
+    xc2r_copy<P>(q.x, xpipe_buf<P>(q.c, b), p0, field);
+  }
   cp_async_commit();
 }
 
@@ -657,16 +748,27 @@ __global__ void __launch_bounds__(XPipeLimits<P, E>::kMaxThreads, XPipeLimits<P,
                 const float4* __restrict__ tw_g) {
   const int k = range_k(pp.x.range);
   int it = 0;
+  const int nb = pp.c.nbuf;
   int tile = blockIdx.x;
-  if (tile < pp.c.ntiles) xc2r_issue<P>(pp, tile, 0);
+  if (pp.bulk && threadIdx.x == 0) {
+    for (int i = 0; i < nb; ++i) mbar_init(xpipe_mbar<P>(pp.c) + i, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  for (int j = 0; j < nb - 1; ++j) {
+    const int t = tile + j * (int)gridDim.x;
+    if (t < pp.c.ntiles) xc2r_issue<P>(pp, t, j);
+    else cp_async_commit();
+  }
+  int b = 0, ph = 0;  // buffer of iteration it and the parity of its use
 #pragma unroll 1
   for (; tile < pp.c.ntiles; tile += gridDim.x, ++it) {
-    const int b = it & 1;
-    const int next = tile + gridDim.x;
-    if (next < pp.c.ntiles) xc2r_issue<P>(pp, next, b ^ 1);
+    const int ahead = tile + (nb - 1) * (int)gridDim.x;
+    if (ahead < pp.c.ntiles) xc2r_issue<P>(pp, ahead, b == 0 ? nb - 1 : b - 1);
     else cp_async_commit();
-    cp_async_wait<1>();
-    __syncthreads();
+    cp_async_wait_ahead(nb);
+    const bool ok = !pp.bulk || mbar_wait_bounded(xpipe_mbar<P>(pp.c) + b, ph, pp.c.err);
+    if (__syncthreads_or(!ok)) break;
     {
       // the first FFT stage reads the raw half spectra (Hermitian merge fused into it)
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
@@ -678,8 +780,17 @@ __global__ void __launch_bounds__(XPipeLimits<P, E>::kMaxThreads, XPipeLimits<P,
       xc2r_store<P>(pp.x, xpipe_buf<P>(pp.c, b), p0, field, k);
     }
     __syncthreads();
+    if (++b == nb) {
+      b = 0;
+      ph ^= 1;
+    }
   }
   cp_async_wait<0>();
+  // early exit after a timed-out wait: wait (bounded) for bulk copies in flight
+  if (pp.bulk && threadIdx.x == 0)
+    for (int j = 0; j < nb; ++j)
+      if (tile + j * (int)gridDim.x < pp.c.ntiles)
+        mbar_wait_bounded(xpipe_mbar<P>(pp.c) + (it + j) % nb, ((it + j) / nb) & 1, nullptr);
 }
 
 }  // namespace p3g

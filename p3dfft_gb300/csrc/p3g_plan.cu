@@ -250,19 +250,19 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
     t = (t + 31) / 32 * 32;
     return t < 32 ? 32 : t;
   };
-  auto smem_for = [&](int M, size_t& buf_bytes) {
-    // buffer stride rounded to 1 KB so both buffers (TMA destinations) stay aligned
+  auto smem_for = [&](int M, size_t& buf_bytes, int nbuf = 2) {
+    // buffer stride rounded to 1 KB so every buffer (TMA destinations) stays aligned
     const int raw = 2 * xc2r_raw_stride(nh, (int)esize);  // c2r raw line pair
     const size_t need = (size_t)(kind == 0 ? M * n : M * (ap.ls > raw ? ap.ls : raw)) * esize;
     buf_bytes = (need + 1023) / 1024 * 1024;
-    return 1024 + 2 * buf_bytes + (tw_shared ? (size_t)ap.tw_cnt * 16 : 0) + 16;
+    return 1024 + nbuf * buf_bytes + (tw_shared ? (size_t)ap.tw_cnt * 16 : 0) + 8 * nbuf + 16;
   };
   // resident warps per SM for tile width M: registers per thread from the
   // kernel's launch bounds, 2048 threads and ~228 KB of shared memory per SM
-  auto warps_for = [&](int M) {
+  auto warps_for = [&](int M, int nbuf = 2) {
     const int t = threads_for(M);
     size_t bb;
-    const size_t sm = smem_for(M, bb);
+    const size_t sm = smem_for(M, bb, nbuf);
     const int regs = regs_max;
     int b = 65536 / (regs * t);
     b = std::min(b, 2048 / t);
@@ -281,8 +281,12 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   ap.pipe_threads = threads_for(M);
   ap.pipe_m = M;
   ap.pipe_log2m = ilog2(M);
+  // a third tile buffer (loads two tiles ahead) where it fits without
+  // costing resident warps: the strided kernels run one CTA per SM
   size_t buf_bytes = 0;
-  ap.pipe_smem = smem_for(M, buf_bytes);
+  ap.pipe_nbuf = 2;
+  if (smem_for(M, buf_bytes, 3) <= 227 * 1024 && warps_for(M, 3) >= warps_for(M, 2)) ap.pipe_nbuf = 3;
+  ap.pipe_smem = smem_for(M, buf_bytes, ap.pipe_nbuf);
   ap.buf_elems = (int)(buf_bytes / esize);
   ap.pipe_ok = ap.pipe_smem <= 227 * 1024;
 }
@@ -459,6 +463,7 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
     pp.c.tw_base = ap.tw_lo;
     pp.c.tw_count = ap.tw_cnt;
     pp.c.buf_elems = ap.buf_elems;
+    pp.c.nbuf = ap.pipe_nbuf;
     pp.c.err = p->d_err;
     pp.chunk = esize;
     CUtensorMap map;
@@ -512,7 +517,11 @@ int run_x_r2c(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) 
     xp.c.tw_base = ap.tw_lo;
     xp.c.tw_count = ap.tw_cnt;
     xp.c.buf_elems = ap.buf_elems;
+    xp.c.nbuf = ap.pipe_nbuf;
     xp.c.err = p->d_err;
+    // the tile's 2M real lines are one contiguous run of device memory
+    xp.bulk = x.in_line == x.nx && (x.nx * us) % 16 == 0 && (x.in_field * us) % 16 == 0 && aligned_to(x.in, 16) &&
+              device_memory(x.in);
     const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
     const int grid = xp.c.ntiles < slots ? xp.c.ntiles : slots;
     cudaError_t e = launch_xr2c_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, ap.pipe_e, ap.pipe_threads,
@@ -542,7 +551,17 @@ int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) 
     xp.c.tw_base = ap.tw_lo;
     xp.c.tw_count = ap.tw_cnt;
     xp.c.buf_elems = ap.buf_elems;
+    xp.c.nbuf = ap.pipe_nbuf;
     xp.c.err = p->d_err;
+    {
+      // every mode of a line arrives by one bulk copy of its nh complexes
+      // rounded up to 16 bytes, which the line pitch and the raw stride hold
+      const long long es = (long long)sizeof(typename P::W);
+      const int nh = x.nx / 2 + 1;
+      xp.bulk = x.nkeep == nh && (x.in_line * es) % 16 == 0 && (x.in_field * es) % 16 == 0 &&
+                (long long)x.in_line * es >= ((nh * es + 15) / 16) * 16 && aligned_to(x.in, 16) &&
+                device_memory(x.in);
+    }
     const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
     const int grid = xp.c.ntiles < slots ? xp.c.ntiles : slots;
     cudaError_t e = launch_xc2r_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, ap.pipe_e, ap.pipe_threads,
@@ -1214,6 +1233,7 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
       p->ax_x.pipe_ok = false;
     p->ax_x.buf_elems = c2r.buf_elems;
     p->ax_x.pipe_smem = c2r.pipe_smem;
+    p->ax_x.pipe_nbuf = c2r.pipe_nbuf;
   }
   size_pipe(p->ax_y, 0, f64);
   for (int i = 0; i < 4; ++i)

@@ -30,6 +30,7 @@ struct AxisPlan {
   size_t pipe_smem = 0;
   int pipe_bps = 1;  // resident CTAs per SM of the pipelined kernel
   int pipe_e = 8;    // elements per thread of the pipelined kernel (PipeLimits)
+  int pipe_nbuf = 2; // tile buffers of the pipelined kernel
 };
 
 struct TimerRec {

@@ -32,6 +32,25 @@ used first out.
 Precision per request: the FP32 path (compensated twiddles; relative L2
 error ~2e-7 against the FP64 oracle) unless the request asks for a tighter
 tolerance than ``F32_TOL``, then the FP64 path (double-float; ~1e-14).
+Fallback at run time: an FP32 result that is not finite (a field beyond
+binary32's range) is computed again on the FP64 path, and an FP64 batch
+whose inputs left the double-float exponent window (p3g_batch_status
+reports P3G_E_RANGE) has its FP64 requests computed again through the plain
+API with the exponent bias picked on the device; ``Request.fallback``
+records it.
+
+Request data: a request either names a device tensor (``inp``), or brings
+host memory (``host_in``, page-locked for asynchronous copies) that is copied
+to a device buffer of its own on the slot's stream just before its launch;
+with ``host_out`` the result is copied back on the same stream, so the
+request's latency includes its own data movement.  Without either the
+request uses the shape's resident input grid.
+
+Failures stay per request: a device buffer that cannot be allocated fails
+only its request (``status`` "failed", ``error`` the message) and frees its
+share of the budget; ``cancel(rid)`` drops a pending request at once and
+discards an in-flight one's result when its launch retires.  ``alloc`` is
+the one place buffers come from, so a test can make it fail on the host.
 
 There is no counterpart in the reference (one blocking transform per call);
 the transforms themselves are the reference's (ftran.F90:489-780,
@@ -63,8 +82,15 @@ class Request:
     t_done: float = math.nan
     out: object = None        # result tensor
     inp: object = None        # input tensor (resident per shape unless given)
+    host_in: object = None    # host input copied to a device buffer of its own
+    host_out: object = None   # host tensor the result is copied back to
     nbytes: int = 0           # device bytes held while in flight
     slot: int = -1
+    status: str = "pending"   # pending, done, cancelled, failed
+    error: str = ""
+    cancelled: bool = False
+    fallback: bool = False    # computed again on the FP64 path
+    resident: bool = False    # inp is the shape's resident grid (counted in use)
 
     @property
     def latency(self) -> float:
@@ -87,6 +113,7 @@ class _Slot:
     event: object = None
     reqs: list = field(default_factory=list)
     busy: bool = False
+    finite: object = None  # per FP32 request of the launch: result finite
 
 
 class Server:
@@ -243,66 +270,182 @@ class Server:
             self.pending = collections.deque(r for r in self.pending if id(r) not in chosen)
         return take
 
+    def alloc(self, shape, dtype):
+        """Every device buffer of a request comes from here (a test replaces
+        it to make allocations fail)."""
+        return self.torch.empty(shape, dtype=dtype, device="cuda")
+
     # ------------------------------------------------------------ the loop
     def submit(self, req: Request) -> None:
         req.precision = F64 if req.tol < F32_TOL else F32
+        req.status = "pending"
         self.pending.append(req)
+
+    def cancel(self, rid: int) -> bool:
+        """Cancels request rid: a pending one leaves the queue now, an
+        in-flight one's result is discarded when its launch retires.  False
+        when no such request is pending or in flight."""
+        for r in self.pending:
+            if r.rid == rid:
+                self.pending.remove(r)
+                r.cancelled = True
+                r.status = "cancelled"
+                r.t_done = self.now()
+                self.done.append(r)
+                return True
+        for s in self.slots:
+            for r in s.reqs:
+                if r.rid == rid:
+                    r.cancelled = True
+                    return True
+        return False
+
+    def _release(self, r: Request) -> None:
+        self.in_flight_bytes -= r.nbytes
+        if r.resident:
+            key = self._input_key(r)
+            if self.in_use[key] > 0:
+                self.in_use[key] -= 1
+            r.resident = False
+
+    def _fail(self, r: Request, err: Exception) -> None:
+        r.status = "failed"
+        r.error = str(err)
+        r.t_done = self.now()
+        r.out = None
+        r.inp = None
+        self._release(r)
+        self.done.append(r)
+
+    def _job(self, r: Request, inp):
+        """Output buffer and batch job of a request (allocations through alloc)."""
+        t = self.torch
+        p = self.plan(r.shape, r.precision)
+        rdt, cdt = self._dtypes(r.precision)
+        nx, ny, nz = r.shape
+        work = self.alloc(p.work_bytes(KINDS[r.kind]), t.uint8)
+        if r.kind == "forward":
+            r.out = self.alloc(p.complex_shape, cdt)
+            return {"plan": p, "kind": JOB_FORWARD, "in": inp, "out": r.out, "work": work}
+        if r.kind == "backward":
+            r.out = self.alloc((nz, ny, nx), rdt)
+            return {"plan": p, "kind": JOB_BACKWARD, "in": inp, "out": r.out, "work": work}
+        r.out = self.alloc(kmax_of(r.shape) + 1, t.float64)
+        return {"plan": p, "kind": JOB_SPECTRUM, "in": inp, "out": r.out, "work": work,
+                "kmax": kmax_of(r.shape), "scale": 1.0 / (nx * ny * nz), "flags": SPEC_HERMITIAN}
 
     def _launch(self, slot: _Slot, reqs) -> None:
         t = self.torch
         groups = {F32: [], F64: []}
+        live, copies = [], []
         for r in reqs:
-            p = self.plan(r.shape, r.precision)
-            rdt, cdt = self._dtypes(r.precision)
-            nx, ny, nz = r.shape
-            if r.inp is None:
-                r.inp = self.resident_input(r.shape, r.precision, r.kind)
-                self.in_use[self._input_key(r)] += 1
-            work = t.empty(p.work_bytes(KINDS[r.kind]), dtype=t.uint8, device="cuda")
-            if r.kind == "forward":
-                r.out = t.empty(p.complex_shape, dtype=cdt, device="cuda")
-                job = {"plan": p, "kind": JOB_FORWARD, "in": r.inp, "out": r.out, "work": work}
-            elif r.kind == "backward":
-                r.out = t.empty((nz, ny, nx), dtype=rdt, device="cuda")
-                job = {"plan": p, "kind": JOB_BACKWARD, "in": r.inp, "out": r.out, "work": work}
-            else:
-                r.out = t.empty(kmax_of(r.shape) + 1, dtype=t.float64, device="cuda")
-                job = {"plan": p, "kind": JOB_SPECTRUM, "in": r.inp, "out": r.out, "work": work,
-                       "kmax": kmax_of(r.shape), "scale": 1.0 / (nx * ny * nz), "flags": SPEC_HERMITIAN}
+            try:
+                if r.host_in is not None:
+                    # the request's own data: a device buffer filled on the slot's stream
+                    rdt, cdt = self._dtypes(r.precision)
+                    r.inp = self.alloc(tuple(r.host_in.shape), cdt if r.kind == "backward" else rdt)
+                    copies.append((r.inp, r.host_in))
+                elif r.inp is None:
+                    r.inp = self.resident_input(r.shape, r.precision, r.kind)
+                    r.resident = True
+                    self.in_use[self._input_key(r)] += 1
+                job = self._job(r, r.inp)
+            except (RuntimeError, MemoryError) as e:  # torch's out-of-memory error is a RuntimeError
+                self._fail(r, e)
+                continue
             groups[r.precision].append(job)
+            live.append(r)
         # the slot's launch follows everything queued on the current stream
         # (input grids generated there, allocations of the buffers above)
         slot.stream.wait_stream(t.cuda.current_stream())
         with t.cuda.stream(slot.stream):
+            for dev, host in copies:
+                dev.copy_(host.to(dev.dtype) if host.dtype != dev.dtype else host, non_blocking=True)
             for prec, jobs in groups.items():
                 if jobs:
                     b = slot.batches[prec]
                     b.set_jobs(jobs, window=self.window)
                     b.launch(slot.stream)
                     self.launches += 1
+            # finiteness of the FP32 results (read at retire, no extra wait) and
+            # the copies back to the host
+            f32 = [r for r in live if r.precision == F32]
+            slot.finite = t.stack([t.isfinite(r.out).all() for r in f32]) if f32 else None
+            for r in live:
+                if r.host_out is not None:
+                    r.host_out.copy_(r.out, non_blocking=True)
             slot.event = t.cuda.Event()
             slot.event.record(slot.stream)
-        slot.reqs = list(reqs)
+        slot.reqs = live
         slot.busy = True
-        self.batch_sizes.append(len(reqs))
+        self.batch_sizes.append(len(live))
+
+
+    def _rerun(self, r: Request, precision) -> None:
+        """Computes r again through the plain API on `precision` (FP64 with the
+        exponent bias picked on the device) on the current stream."""
+        from . import RANGE_AUTO
+        t = self.torch
+        p = self.plan(r.shape, precision)
+        rdt, cdt = self._dtypes(precision)
+        src = r.host_in if r.host_in is not None else r.inp
+        inp = src.to(device="cuda", dtype=cdt if r.kind == "backward" else rdt)
+        nx, ny, nz = r.shape
+        if precision == F64:
+            p.set_range(RANGE_AUTO)
+        try:
+            if r.kind == "forward":
+                r.out = p.ftran_r2c(inp)
+            elif r.kind == "backward":
+                r.out = p.btran_c2r(inp)
+            else:
+                b = p.ftran_r2c(inp)
+                r.out = p.spectrum(b, kmax=kmax_of(r.shape), scale=1.0 / (nx * ny * nz), flags=SPEC_HERMITIAN)
+            t.cuda.synchronize()
+        finally:
+            if precision == F64:
+                p.set_range()
+        r.precision = precision
 
     def _retire(self, slot: _Slot) -> None:
-        now = self.now()
+        from . import P3DFFTError
         for prec, b in slot.batches.items():
             if any(r.precision == prec for r in slot.reqs):
-                b.check(slot.stream)
+                try:
+                    b.check(slot.stream)
+                except P3DFFTError as e:
+                    if prec != F64 or "exponent window" not in str(e):
+                        raise
+                    for r in slot.reqs:  # FP64 inputs outside the window: again, biased
+                        if r.precision == F64 and not r.cancelled:
+                            r.fallback = True
+                            self._rerun(r, F64)
             b._keep = []  # release the work buffers
+        finite = slot.finite.cpu().tolist() if slot.finite is not None else []
+        i32 = 0
         for r in slot.reqs:
-            r.t_done = now
-            self.in_flight_bytes -= r.nbytes
-            key = self._input_key(r)
-            if self.in_use[key] > 0:
-                self.in_use[key] -= 1
+            ok = True
+            if r.precision == F32:
+                ok = bool(finite[i32])
+                i32 += 1
+            if r.cancelled:
+                r.status = "cancelled"
+                r.out = None
+            else:
+                if not ok:  # an FP32 result beyond binary32's range: FP64 fallback
+                    r.fallback = True
+                    self._rerun(r, F64)
+                    if r.host_out is not None:
+                        r.host_out = r.out.cpu()
+                r.status = "done"
+            r.t_done = self.now()
+            self._release(r)
             if not self.keep_outputs:
                 r.out = None
                 r.inp = None
             self.done.append(r)
         slot.reqs = []
+        slot.finite = None
         slot.busy = False
 
     def poll(self) -> bool:
@@ -401,6 +544,50 @@ def make_requests(n: int, seed: int = 5, lo: int = 32, hi: int = 512, mix=(4, 4,
         kind = str(rng.choice(kinds, p=p))
         tol = 1e-12 if rng.random() < f64_fraction else F32_TOL
         reqs.append(Request(rid=i, kind=kind, shape=shape, tol=tol))
+    return reqs
+
+
+def attach_host_data(reqs, seed: int = 7, outputs: bool = True, arena_bytes: int = 1 << 30):
+    """Gives every request host data of its own: an input view of a
+    page-locked arena (real field, or complex spectrum for backward
+    requests, in the request's precision) and, with outputs, a view of a
+    second arena for its result.  Views rotate through the arenas, so the
+    bytes repeat but each request's copies are its own."""
+    import numpy as np
+    import torch
+    arena_in = torch.empty(arena_bytes, dtype=torch.uint8).pin_memory()
+    rng = np.random.default_rng(seed)
+    arena_in.view(torch.float32)[:] = torch.from_numpy(rng.uniform(-1, 1, arena_bytes // 4).astype(np.float32))
+    arena_out = torch.empty(arena_bytes, dtype=torch.uint8).pin_memory() if outputs else None
+    off_in = off_out = 0
+
+    def take(arena, off, n):
+        if off + n > arena_bytes:
+            off = 0
+        return arena[off:off + n], (off + n + 255) // 256 * 256
+
+    for r in reqs:
+        nx, ny, nz = r.shape
+        f64 = r.tol < F32_TOL
+        rdt = torch.float64 if f64 else torch.float32
+        cdt = torch.complex128 if f64 else torch.complex64
+        if r.kind == "backward":
+            shape_in, dt_in = (nz, ny, nx // 2 + 1), cdt
+        else:
+            shape_in, dt_in = (nz, ny, nx), rdt
+        n_in = int(np.prod(shape_in)) * dt_in.itemsize
+        v, off_in = take(arena_in, off_in, n_in)
+        r.host_in = v.view(dt_in).view(shape_in)
+        if outputs:
+            if r.kind == "forward":
+                shape_out, dt_out = (nz, ny, nx // 2 + 1), cdt
+            elif r.kind == "backward":
+                shape_out, dt_out = (nz, ny, nx), rdt
+            else:
+                shape_out, dt_out = (kmax_of(r.shape) + 1,), torch.float64
+            n_out = int(np.prod(shape_out)) * dt_out.itemsize
+            v, off_out = take(arena_out, off_out, n_out)
+            r.host_out = v.view(dt_out).view(shape_out)
     return reqs
 
 

@@ -106,3 +106,95 @@ def test_serve_poisson_stream_reports_latency(torch_cuda):
     assert s["requests"] == 40 and 0 <= s["p50_ms"] <= s["p99_ms"]
     assert all(r.out is None for r in reqs)
     srv.close()
+
+
+def test_serve_requests_with_their_own_host_data(torch_cuda):
+    # each request's input is copied from host memory of its own and its
+    # result copied back: the host results match the oracle
+    from p3dfft_gb300 import serve
+    reqs = serve.attach_host_data(_small_requests(16, seed=14), seed=3, arena_bytes=64 << 20)
+    srv = serve.Server(budget_bytes=8e9, slots=2, max_jobs=6)
+    srv.run(reqs)
+    for r in reqs:
+        assert r.status == "done"
+        r.inp = r.host_in
+        r.out = r.host_out
+        _oracle_check(r)
+    srv.close()
+
+
+def test_serve_allocation_failure_fails_only_its_request(torch_cuda):
+    # failure injected on the host: the work buffer of every fourth request
+    # fails to allocate; the others complete and the budget is freed
+    from p3dfft_gb300 import serve
+    torch = torch_cuda
+    reqs = _small_requests(12, seed=15)
+    victims = {r.rid for r in reqs[::4]}
+    srv = serve.Server(budget_bytes=8e9, slots=2, max_jobs=4)
+    real_alloc = srv.alloc
+    current = {}
+
+    def alloc(shape, dtype):
+        if current.get("rid") in victims:
+            raise RuntimeError("CUDA out of memory (injected)")
+        return real_alloc(shape, dtype)
+
+    def job(r, inp, _orig=srv._job):
+        current["rid"] = r.rid
+        return _orig(r, inp)
+
+    srv.alloc = alloc
+    srv._job = job
+    srv.run(reqs)
+    for r in reqs:
+        if r.rid in victims:
+            assert r.status == "failed" and "injected" in r.error and r.out is None
+        else:
+            assert r.status == "done"
+            _oracle_check(r)
+    assert srv.in_flight_bytes == 0
+    srv.close()
+    del torch
+
+
+def test_serve_cancellation(torch_cuda):
+    from p3dfft_gb300 import serve
+    reqs = _small_requests(10, seed=16)
+    srv = serve.Server(budget_bytes=8e9, slots=1, max_jobs=2, launch_work=None)
+    for r in reqs:
+        srv.submit(r)
+    assert srv.cancel(reqs[9].rid)           # pending: leaves the queue
+    srv.poll()                               # launches the first two
+    assert srv.cancel(reqs[0].rid)           # in flight: result discarded at retire
+    srv.drain()
+    assert reqs[9].status == "cancelled" and reqs[0].status == "cancelled" and reqs[0].out is None
+    for r in reqs[1:9]:
+        assert r.status == "done"
+        _oracle_check(r)
+    assert srv.in_flight_bytes == 0
+    srv.close()
+
+
+def test_serve_fp64_fallbacks(torch_cuda):
+    # an FP32 request whose sums pass binary32's range is computed again on
+    # the FP64 path; an FP64 request beyond the double-float window is
+    # computed again with the bias picked on the device
+    import torch as _t
+
+    from p3dfft_gb300 import F64, serve
+    big32 = serve.Request(rid=0, kind="forward", shape=(32, 32, 32),
+                          host_in=_t.full((32, 32, 32), 3e37, dtype=_t.float32).pin_memory())
+    rng = np.random.default_rng(17)
+    big64 = serve.Request(rid=1, kind="backward", shape=(24, 20, 18), tol=1e-12,
+                          host_in=_t.from_numpy(rng.standard_normal((18, 20, 13)) * 1e200
+                                                + 1j * rng.standard_normal((18, 20, 13)) * 1e200).pin_memory())
+    small = serve.Request(rid=2, kind="forward", shape=(16, 16, 16),
+                          host_in=_t.from_numpy(rng.uniform(-1, 1, (16, 16, 16)).astype(np.float32)).pin_memory())
+    srv = serve.Server(budget_bytes=8e9, slots=1, max_jobs=4)
+    srv.run([big32, big64, small])
+    assert big32.fallback and big32.precision == F64 and bool(_t.isfinite(big32.out).all())
+    assert big64.fallback and small.status == "done" and not small.fallback
+    for r in (big32, big64, small):
+        r.inp = r.host_in
+        _oracle_check(r)
+    srv.close()

@@ -75,3 +75,17 @@ def test_budget_limits_admission():
     srv2.pending.append(_req(0, 32))
     with pytest.raises(RuntimeError, match="budget"):
         srv2._select(0)
+
+
+def test_cancel_pending_request_on_the_host():
+    srv = _server(launch_work=1e12, now=0.002)
+    srv.slots = []
+    srv.done = []
+    for i, s in enumerate([32, 48, 64]):
+        srv.pending.append(_req(i, s))
+    assert srv.cancel(1) is True
+    assert [r.rid for r in srv.pending] == [0, 2]
+    assert srv.done[0].rid == 1 and srv.done[0].status == "cancelled" and srv.done[0].t_done == 0.002
+    assert srv.cancel(7) is False
+    took = srv._select(0)
+    assert [r.rid for r in took] == [0, 2]
