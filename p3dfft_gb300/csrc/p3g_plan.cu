@@ -281,11 +281,12 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   ap.pipe_threads = threads_for(M);
   ap.pipe_m = M;
   ap.pipe_log2m = ilog2(M);
-  // a third tile buffer (loads two tiles ahead) where it fits without
-  // costing resident warps: the strided kernels run one CTA per SM
+  // a third tile buffer (loads two tiles ahead) for the X kernels where it
+  // fits without costing resident warps; the strided kernels keep two (with
+  // three in flight per SM their scattered rows ran 3-15 % slower)
   size_t buf_bytes = 0;
   ap.pipe_nbuf = 2;
-  if (smem_for(M, buf_bytes, 3) <= 227 * 1024 && warps_for(M, 3) >= warps_for(M, 2)) ap.pipe_nbuf = 3;
+  if (xk && smem_for(M, buf_bytes, 3) <= 227 * 1024 && warps_for(M, 3) >= warps_for(M, 2)) ap.pipe_nbuf = 3;
   ap.pipe_smem = smem_for(M, buf_bytes, ap.pipe_nbuf);
   ap.buf_elems = (int)(buf_bytes / esize);
   ap.pipe_ok = ap.pipe_smem <= 227 * 1024;
@@ -661,8 +662,11 @@ void make_forward_params(p3g_plan p, const void* in, void* out, void* wa, void* 
   y.in_axis = (int)P_;
   y.in_o1 = (long long)p->ny * P_;
   y.in_o2 = wa_field;
-  y.out_axis = (int)P_;
-  y.out_o1 = (long long)p->nyc * P_;
+  // the Y output (Z input) is stored [y][z][x]: the Z pass then reads its
+  // lines at a stride of one row (pitch) instead of a whole plane, and the
+  // scattered accesses move to the Y pass's stores
+  y.out_axis = (int)(p->nz * P_);
+  y.out_o1 = P_;
   y.out_o2 = y_field;
   y.X = p->nxhpc;
   y.O1 = p->nz;
@@ -683,8 +687,8 @@ void make_forward_params(p3g_plan p, const void* in, void* out, void* wa, void* 
   z.in = ybuf;
   z.out = out;
   z.out_user = 1;
-  z.in_axis = (int)(p->nyc * P_);
-  z.in_o1 = P_;
+  z.in_axis = (int)P_;
+  z.in_o1 = (long long)p->nz * P_;
   z.in_o2 = y_field;
   if (p->layout == P3G_LAYOUT_STRIDE1) {  // (nzc, nyc, nxhpc), z fastest (module.F90:245-254)
     z.out_axis = 1;
@@ -1182,10 +1186,10 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     delete p;
     return fail(P3G_E_UNSUPPORTED, m);
   };
-  // single per-element strides (a plane's row pitch, the Z pass's axis stride
-  // nyc*pitch, the STRIDE1 column stride nyc*nzc) are 32-bit kernel parameters;
+  // single per-element strides (a plane's row pitch, the Y output's row
+  // stride nz*pitch, the STRIDE1 column stride nyc*nzc) are 32-bit kernel parameters;
   // offsets (their products with indices) are formed in 64 bits
-  if ((long long)p->pitch * ny >= (1LL << 31) || (long long)p->nxhpc * p->nyc >= (1LL << 31) ||
+  if ((long long)p->pitch * std::max(ny, nz) >= (1LL << 31) || (long long)p->nxhpc * p->nyc >= (1LL << 31) ||
       (long long)p->nyc * p->nzc >= (1LL << 31))
     return bad("a plane of more than 2^31 elements is not supported");
   if (!add_axis(p->ax_x, nx, (ny * nz + 1) / 2)) return bad("x length " + std::to_string(nx) + " is too long");
