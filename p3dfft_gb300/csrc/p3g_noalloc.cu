@@ -101,7 +101,7 @@ extern "C" int p3g_ftran_r2c_noalloc(p3g_plan p, const void* in, void* out, cons
   if (!p->z_ok[zi]) return fail(P3G_E_UNSUPPORTED, std::string("Z transform '") + op[2] + "' unsupported for nz");
   const size_t esize = p->esize();
   const size_t wa_bytes = ((size_t)p->nz * p->ny * p->pitch * esize + 255) / 256 * 256;
-  const size_t wb_bytes = p->nyc < p->ny ? (size_t)p->nz * p->nyc * p->pitch * esize : 0;
+  const size_t wb_bytes = (size_t)p->nz * p->nyc * p->pitch * esize;
   if (wa_bytes + wb_bytes > kNoAllocScratchBytes)
     return fail(P3G_E_UNSUPPORTED, "allocation-free transform: the grid needs " + std::to_string(wa_bytes + wb_bytes) +
                                        " bytes of workspace, more than its fixed " +

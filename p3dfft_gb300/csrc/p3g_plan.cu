@@ -314,7 +314,7 @@ int ensure_workspace(p3g_plan p, int nv) {
     p->wa = nullptr;
     return fail(P3G_E_NOMEM, "workspace allocation failed (" + std::to_string(na) + " bytes)");
   }
-  if (p->nyc < p->ny) {
+  {  // the forward Y pass writes wb ([y][z][x], a layout it cannot write in place)
     const size_t nb = (size_t)p->nz * p->nyc * p->pitch * nv * p->esize();
     if (cudaMalloc(&p->wb, nb) != cudaSuccess) {
       cudaGetLastError();
@@ -629,7 +629,7 @@ int launch_range_scan(p3g_plan p, const void* in, long long n, long long field, 
 }
 
 // Pass parameters of a forward transform: X r2c user real -> wa, Y wa ->
-// ybuf (wa, or wb when nyc < ny) keeping y modes 0..nycph-1 and the top
+// wb ([y][z][x]) keeping y modes 0..nycph-1 and the top
 // nyc-nycph (seg_copy_y, ftran.F90:736-738), Z ybuf -> user complex with the
 // Z op and z pruning (seg_copy_z, ftran.F90:705-706).
 void make_forward_params(p3g_plan p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
@@ -637,8 +637,8 @@ void make_forward_params(p3g_plan p, const void* in, void* out, void* wa, void* 
   const long long P_ = p->pitch;
   const long long wa_field = (long long)p->nz * p->ny * P_;
   const long long wb_field = (long long)p->nz * p->nyc * P_;
-  void* ybuf = p->nyc < p->ny ? wb : wa;
-  const long long y_field = p->nyc < p->ny ? wb_field : wa_field;
+  void* ybuf = wb;
+  const long long y_field = wb_field;
   x = XParams{};
   x.in = in;
   x.out = wa;

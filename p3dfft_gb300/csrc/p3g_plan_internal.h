@@ -72,7 +72,7 @@ struct p3g_plan_s {
   StagePlan* d_sp = nullptr;
   size_t tw_bytes = 0;
   void* wa = nullptr;  // nz*ny*pitch*nv elements
-  void* wb = nullptr;  // nz*nyc*pitch*nv elements (only if nyc < ny)
+  void* wb = nullptr;  // nz*nyc*pitch*nv elements: the forward Y output ([y][z][x]), pruned-y backward
   size_t w_fields = 0;
   double timers[12];
   std::vector<TimerRec> pending;
