@@ -22,6 +22,8 @@ def main(argv=None):
     ap.add_argument("--mode", choices=sorted(MODES), default="pipe_tma")
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--max-radix", type=int, default=0, help="largest power-of-two radix (plan tuning knob)")
+    ap.add_argument("--max-lines", type=int, default=0, help="most lines per tile (plan tuning knob)")
     args = ap.parse_args(argv)
 
     import torch
@@ -30,7 +32,8 @@ def main(argv=None):
 
     nx, ny, nz = args.grid
     f64 = args.precision == "f64"
-    plan = pg.Plan(nx, ny, nz, precision=pg.F64 if f64 else pg.F32, timers=True)
+    plan = pg.Plan(nx, ny, nz, precision=pg.F64 if f64 else pg.F32, timers=True, max_radix=args.max_radix,
+                   max_lines=args.max_lines)
     plan.set_options(*MODES[args.mode])
     g = torch.Generator(device="cuda")
     g.manual_seed(args.seed)
@@ -55,6 +58,7 @@ def main(argv=None):
     else:
         err = None
     print(json.dumps({"grid": [nx, ny, nz], "precision": args.precision, "mode": args.mode,
+                      "max_radix": args.max_radix, "max_lines": args.max_lines,
                       "ms_per_round_trip": round(ms, 4),
                       "passes_ms": {name: round(t[i] * 1e3 / args.steps, 4) for name, i in
                                     (("x_r2c", 4), ("y_fwd", 6), ("z_fwd", 7), ("z_bwd", 8), ("y_bwd", 9),
