@@ -346,7 +346,10 @@ __device__ __forceinline__ void run_family(const Tile<P>& t, const float4* __res
 }
 
 // Runs all stages of the plan on the tile (sm must be filled and
-// synchronised).  The plan orders its stages by radix family (16, 8, 4, 2, 3,
+// synchronised).  MAXR is the largest power-of-two radix compiled in: 32 on
+// the F32 path; 8 on F64, 16 in the F64 wide pipelined kernels (a
+// double-float radix-16 codelet needs ~200 registers, so only kernels that
+// may use them carry it; their plans' stages never exceed MAXR).  The plan orders its stages by radix family (16, 8, 4, 2, 3,
 // 5, then generic primes) and each family runs in its own loop: a single loop
 // with a switch over the radix makes the register allocator keep the live
 // ranges of every codelet at once and spill.  Radix 16 is compiled only for
@@ -358,7 +361,8 @@ __device__ __forceinline__ void run_family(const Tile<P>& t, const float4* __res
 // tile layout when the caller knows it (kPointMajor, kLineMajor).  RAW: the
 // tile still holds the raw line pairs of an X r2c or c2r tile (kRawR2C,
 // kRawC2R; plans without generic stages only), read by the first stage.
-template <class P, int DIR, int E = kElemsPerThread, int LAY = kAnyLayout, int RAW = kRawNone>
+template <class P, int DIR, int E = kElemsPerThread, int LAY = kAnyLayout, int RAW = kRawNone,
+          int MAXR = P::kF64 ? 8 : 32>
 __device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __restrict__ sp,
                                         const float4* __restrict__ tw, int tw_base = 0) {
   const int N = __ldg(&sp->n);
@@ -369,10 +373,8 @@ __device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __res
   int ns = 1;
   int off = __ldg(&sp->tw_off[0]) - tw_base;
   bool raw = RAW != kRawNone;
-  if constexpr (!P::kF64) {
-    run_family<P, DIR, 32, E, LAY, RAW>(t, tw, N, c[0], ns, off, raw);
-    run_family<P, DIR, 16, E, LAY, RAW>(t, tw, N, c[1], ns, off, raw);
-  }
+  if constexpr (MAXR >= 32) run_family<P, DIR, 32, E, LAY, RAW>(t, tw, N, c[0], ns, off, raw);
+  if constexpr (MAXR >= 16) run_family<P, DIR, 16, E, LAY, RAW>(t, tw, N, c[1], ns, off, raw);
   run_family<P, DIR, 8, E, LAY, RAW>(t, tw, N, c[2], ns, off, raw);
   run_family<P, DIR, 4, E, LAY, RAW>(t, tw, N, c[3], ns, off, raw);
   run_family<P, DIR, 2, E, LAY, RAW>(t, tw, N, c[4], ns, off, raw);

@@ -308,6 +308,7 @@ cudaError_t launch_strided_pipe(const CUtensorMap* map, const SPipeParams& p, co
                                 bool forward_sign, int E, int threads, size_t smem, int grid, cudaStream_t st) {
   if constexpr (P::kF64) {
     if (E == 8) return launch_strided_pipe_e<P, 8>(map, p, sp, tw, forward_sign, threads, smem, grid, st);
+    if (E == 16) return launch_strided_pipe_e<P, 16>(map, p, sp, tw, forward_sign, threads, smem, grid, st);
   } else {
     if (E == 16) return launch_strided_pipe_e<P, 16>(map, p, sp, tw, forward_sign, threads, smem, grid, st);
     if (E == 32) return launch_strided_pipe_e<P, 32>(map, p, sp, tw, forward_sign, threads, smem, grid, st);
@@ -327,6 +328,7 @@ cudaError_t launch_xr2c_pipe(const XPipeParams& p, const StagePlan* sp, const fl
                              size_t smem, int grid, cudaStream_t st) {
   if constexpr (P::kF64) {
     if (E == 8) return launch_xr2c_pipe_e<P, 8>(p, sp, tw, threads, smem, grid, st);
+    if (E == 16) return launch_xr2c_pipe_e<P, 16>(p, sp, tw, threads, smem, grid, st);
   } else {
     if (E == 16) return launch_xr2c_pipe_e<P, 16>(p, sp, tw, threads, smem, grid, st);
     if (E == 32) return launch_xr2c_pipe_e<P, 32>(p, sp, tw, threads, smem, grid, st);
@@ -346,6 +348,7 @@ cudaError_t launch_xc2r_pipe(const XPipeParams& p, const StagePlan* sp, const fl
                              size_t smem, int grid, cudaStream_t st) {
   if constexpr (P::kF64) {
     if (E == 8) return launch_xc2r_pipe_e<P, 8>(p, sp, tw, threads, smem, grid, st);
+    if (E == 16) return launch_xc2r_pipe_e<P, 16>(p, sp, tw, threads, smem, grid, st);
   } else {
     if (E == 16) return launch_xc2r_pipe_e<P, 16>(p, sp, tw, threads, smem, grid, st);
     if (E == 32) return launch_xc2r_pipe_e<P, 32>(p, sp, tw, threads, smem, grid, st);
@@ -371,7 +374,7 @@ int pipe_blocks_per_sm_e(int kind, int threads, size_t smem) {
 template <class P>
 int pipe_blocks_per_sm(int kind, int E, int threads, size_t smem) {
   if constexpr (P::kF64) {
-    return pipe_blocks_per_sm_e<P, 8>(kind, threads, smem);
+    return E == 16 ? pipe_blocks_per_sm_e<P, 16>(kind, threads, smem) : pipe_blocks_per_sm_e<P, 8>(kind, threads, smem);
   } else {
     return E == 32 ? pipe_blocks_per_sm_e<P, 32>(kind, threads, smem)
                    : pipe_blocks_per_sm_e<P, 16>(kind, threads, smem);

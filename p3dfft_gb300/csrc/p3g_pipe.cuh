@@ -51,18 +51,22 @@ P3G_D unsigned char* align1k(unsigned char* p) {
 }
 
 // Tiles hold at most 4096 (F64) or 8192 (F32) elements; a thread holds E
-// of them per stage: 8 on the F64 path (512 threads, 16 warps per SM to hide
-// the latency of the dependent double-float chains); on the F32 path 32 for
-// axes with radix-32 stages (one 32-point butterfly per thread and stage
-// takes a 1024-point line through two stages) and 16 otherwise.
+// of them per stage: on the F64 path 16 for axes with radix-16 stages (one
+// 16-point butterfly per thread and stage: 1024 = 16 x 16 x 4) and 8
+// otherwise (512 threads, 16 warps per SM to hide the latency of the
+// dependent double-float chains); on the F32 path 32 for axes with radix-32
+// stages (one 32-point butterfly per thread and stage takes a 1024-point line
+// through two stages) and 16 otherwise.
 template <class P, int E>
 struct PipeLimits {
+  // one radix-32 (F32) or radix-16 (F64) butterfly per thread and stage
+  static constexpr bool kWide = P::kF64 ? E == 16 : E == 32;
   static constexpr int kMaxThreads = (P::kF64 ? 4096 : 8192) / E;
   // 128 registers per thread (with a larger budget the scheduler hoists
-  // shared-memory loads across codelets and spills), except for the F32
-  // radix-32 kernel: one 256-thread CTA per SM (its two 64 KB tiles fill
-  // shared memory) with up to 255 registers for the 32-point butterflies
-  static constexpr int kMinBlocks = (!P::kF64 && E == 32) ? 1 : 65536 / 128 / kMaxThreads;
+  // shared-memory loads across codelets and spills), except for the wide
+  // kernels: one 256-thread CTA per SM (its two 64 KB tiles fill shared
+  // memory) with up to 255 registers for the 32- or 16-point butterflies
+  static constexpr int kMinBlocks = kWide ? 1 : 65536 / 128 / kMaxThreads;
 };
 
 // X passes: 256-thread CTAs, three per SM (85 registers; 128-thread CTAs
@@ -73,15 +77,17 @@ struct PipeLimits {
 // stay wide for their long-stride DRAM rows, keep PipeLimits.
 template <class P, int E>
 struct XPipeLimits {
-  static constexpr int kMaxThreads = (!P::kF64 && E == 32) ? 128 : 256;
+  static constexpr int kMaxThreads = PipeLimits<P, E>::kWide ? 128 : 256;
   static constexpr int kMinBlocks = 3;
 };
 
-// Per-thread element counts the pipelined kernels are built for.
-template <class P>
-constexpr bool pipe_e_ok(int E) {
-  return P::kF64 ? E == 8 : (E == 16 || E == 32);
-}
+// Largest radix compiled into a pipelined kernel (cta_fft's MAXR).
+template <class P, int E>
+struct PipeMaxR {
+  static constexpr int value = P::kF64 ? (E == 16 ? 16 : 8) : (E == 32 ? 32 : 16);
+};
+
+
 
 // ------------------------------------------------------------ strided Y/Z
 template <class P>
@@ -378,7 +384,7 @@ __global__ void __launch_bounds__(PipeLimits<P, E>::kMaxThreads, PipeLimits<P, E
       const SPipeParams& q = pp;
       const StridedSmem<P> sm = strided_smem<P>(q.c);
       Tile<P> t{sm.buf0 + b * q.c.buf_elems, nullptr, q.s.M, q.s.log2m, 1, q.s.M};
-      cta_fft<P, DIR, E, kPointMajor>(t, sp, sm.tw, q.c.tw_base);
+      cta_fft<P, DIR, E, kPointMajor, kRawNone, PipeMaxR<P, E>::value>(t, sp, sm.tw, q.c.tw_base);
     }
     {
       int xt, o1, o2;
@@ -570,7 +576,7 @@ __global__ void __launch_bounds__(XPipeLimits<P, E>::kMaxThreads, XPipeLimits<P,
     {
       // the first FFT stage reads the raw line pairs (packing fused into it)
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps, k, &amax};
-      cta_fft<P, -1, E, kLineMajor, kRawR2C>(t, sp, tw_g, 0);
+      cta_fft<P, -1, E, kLineMajor, kRawR2C, PipeMaxR<P, E>::value>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;
@@ -772,7 +778,7 @@ __global__ void __launch_bounds__(XPipeLimits<P, E>::kMaxThreads, XPipeLimits<P,
     {
       // the first FFT stage reads the raw half spectra (Hermitian merge fused into it)
       Tile<P> t{xpipe_buf<P>(pp.c, b), nullptr, pp.x.M, pp.x.log2m, pp.x.LS, 1, pp.x.ps};
-      cta_fft<P, 1, E, kLineMajor, kRawC2R>(t, sp, tw_g, 0);
+      cta_fft<P, 1, E, kLineMajor, kRawC2R, PipeMaxR<P, E>::value>(t, sp, tw_g, 0);
     }
     {
       const int field = tile / pp.c.tiles_per_field;

@@ -236,11 +236,13 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   if (ap.sp.nstages < 1 || ap.sp.has_generic || ap.n < 2) return;
   const size_t esize = f64 ? 16 : 8;
   const bool xk = kind != 0;  // X kernels have their own launch shape (XPipeLimits)
-  const int E = f64 ? 8 : (ap.sp.cnt[0] > 0 ? 32 : 16);
+  const int E = f64 ? (ap.spw_index >= 0 ? 16 : 8) : (ap.sp.cnt[0] > 0 ? 32 : 16);
   ap.pipe_e = E;
   int max_threads = 0, regs_max = 0;
-  if (f64) pipe_shape<PathF64, 8>(xk, max_threads, regs_max);
-  else if (E == 32) pipe_shape<PathF32, 32>(xk, max_threads, regs_max);
+  if (f64) {
+    if (E == 16) pipe_shape<PathF64, 16>(xk, max_threads, regs_max);
+    else pipe_shape<PathF64, 8>(xk, max_threads, regs_max);
+  } else if (E == 32) pipe_shape<PathF32, 32>(xk, max_threads, regs_max);
   else pipe_shape<PathF32, 16>(xk, max_threads, regs_max);
   const bool tw_shared = !xk;  // the X kernels read the global table
   const int n = ap.n;
@@ -253,9 +255,10 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   auto smem_for = [&](int M, size_t& buf_bytes, int nbuf = 2) {
     // buffer stride rounded to 1 KB so every buffer (TMA destinations) stays aligned
     const int raw = 2 * xc2r_raw_stride(nh, (int)esize);  // c2r raw line pair
-    const size_t need = (size_t)(kind == 0 ? M * n : M * (ap.ls > raw ? ap.ls : raw)) * esize;
+    const int ls = ap.pipe_ls();
+    const size_t need = (size_t)(kind == 0 ? M * n : M * (ls > raw ? ls : raw)) * esize;
     buf_bytes = (need + 1023) / 1024 * 1024;
-    return 1024 + nbuf * buf_bytes + (tw_shared ? (size_t)ap.tw_cnt * 16 : 0) + 8 * nbuf + 16;
+    return 1024 + nbuf * buf_bytes + (tw_shared ? (size_t)ap.pipe_tw_cnt() * 16 : 0) + 8 * nbuf + 16;
   };
   // resident warps per SM for tile width M: registers per thread from the
   // kernel's launch bounds, 2048 threads and ~228 KB of shared memory per SM
@@ -461,8 +464,8 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
     pp.s = s;
     pp.c.tiles_per_field = s.xtiles * s.O1;
     pp.c.ntiles = pp.c.tiles_per_field * nv;
-    pp.c.tw_base = ap.tw_lo;
-    pp.c.tw_count = ap.tw_cnt;
+    pp.c.tw_base = ap.pipe_tw_lo();
+    pp.c.tw_count = ap.pipe_tw_cnt();
     pp.c.buf_elems = ap.buf_elems;
     pp.c.nbuf = ap.pipe_nbuf;
     pp.c.err = p->d_err;
@@ -486,7 +489,7 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
     }
     const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
     const int grid = pp.c.ntiles < slots ? pp.c.ntiles : slots;
-    cudaError_t e = launch_strided_pipe<P>(&map, pp, p->d_sp + ap.sp_index, p->d_tw, fwd_sign, ap.pipe_e,
+    cudaError_t e = launch_strided_pipe<P>(&map, pp, p->d_sp + ap.pipe_sp(), p->d_tw, fwd_sign, ap.pipe_e,
                                            ap.pipe_threads, ap.pipe_smem, grid, st);
     if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("strided pass launch: ") + cudaGetErrorString(e));
     p->launches++;
@@ -509,14 +512,16 @@ int run_x_r2c(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) 
     else if ((x.nx * us) % 8 == 0 && (x.in_field * us) % 8 == 0 && aligned_to(x.in, 8)) chunk = 8;
     x.M = ap.pipe_m;
     x.log2m = ap.pipe_log2m;
+    x.LS = ap.pipe_ls();
+    x.ps = ap.pipe_ps();
     x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
     XPipeParams xp{};
     xp.x = x;
     xp.chunk = chunk;
     xp.c.tiles_per_field = x.tiles;
     xp.c.ntiles = x.tiles * nv;
-    xp.c.tw_base = ap.tw_lo;
-    xp.c.tw_count = ap.tw_cnt;
+    xp.c.tw_base = ap.pipe_tw_lo();
+    xp.c.tw_count = ap.pipe_tw_cnt();
     xp.c.buf_elems = ap.buf_elems;
     xp.c.nbuf = ap.pipe_nbuf;
     xp.c.err = p->d_err;
@@ -525,7 +530,7 @@ int run_x_r2c(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) 
               device_memory(x.in);
     const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
     const int grid = xp.c.ntiles < slots ? xp.c.ntiles : slots;
-    cudaError_t e = launch_xr2c_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, ap.pipe_e, ap.pipe_threads,
+    cudaError_t e = launch_xr2c_pipe<P>(xp, p->d_sp + ap.pipe_sp(), p->d_tw, ap.pipe_e, ap.pipe_threads,
                                         ap.pipe_smem, grid, st);
     if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X r2c launch: ") + cudaGetErrorString(e));
     p->launches++;
@@ -543,14 +548,16 @@ int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) 
   if (p->use_pipe && ap.pipe_ok) {
     x.M = ap.pipe_m;
     x.log2m = ap.pipe_log2m;
+    x.LS = ap.pipe_ls();
+    x.ps = ap.pipe_ps();
     x.tiles = ((x.nlines + 1) / 2 + x.M - 1) / x.M;
     XPipeParams xp{};
     xp.x = x;
     xp.chunk = (int)sizeof(typename P::W);
     xp.c.tiles_per_field = x.tiles;
     xp.c.ntiles = x.tiles * nv;
-    xp.c.tw_base = ap.tw_lo;
-    xp.c.tw_count = ap.tw_cnt;
+    xp.c.tw_base = ap.pipe_tw_lo();
+    xp.c.tw_count = ap.pipe_tw_cnt();
     xp.c.buf_elems = ap.buf_elems;
     xp.c.nbuf = ap.pipe_nbuf;
     xp.c.err = p->d_err;
@@ -565,7 +572,7 @@ int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) 
     }
     const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
     const int grid = xp.c.ntiles < slots ? xp.c.ntiles : slots;
-    cudaError_t e = launch_xc2r_pipe<P>(xp, p->d_sp + ap.sp_index, p->d_tw, ap.pipe_e, ap.pipe_threads,
+    cudaError_t e = launch_xc2r_pipe<P>(xp, p->d_sp + ap.pipe_sp(), p->d_tw, ap.pipe_e, ap.pipe_threads,
                                         ap.pipe_smem, grid, st);
     if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("X c2r launch: ") + cudaGetErrorString(e));
     p->launches++;
@@ -1124,9 +1131,9 @@ int p3g_plan_create(p3g_plan* out, int nx, int ny, int nz, int nxc, int nyc, int
 int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int nyc, int nzc, int precision,
                           int layout, int flags, int max_radix, int max_lines) {
   if (!out) return fail(P3G_E_ARG, "plan pointer is NULL");
-  if (max_radix != 0 && max_radix != 2 && max_radix != 4 && max_radix != 8 &&
-      !((max_radix == 16 || max_radix == 32) && precision == P3G_F32))
-    return fail(P3G_E_ARG, "max_radix must be 0, 2, 4, 8 (or 16, 32 on the F32 path)");
+  if (max_radix != 0 && max_radix != 2 && max_radix != 4 && max_radix != 8 && max_radix != 16 &&
+      !(max_radix == 32 && precision == P3G_F32))
+    return fail(P3G_E_ARG, "max_radix must be 0, 2, 4, 8, 16 (or 32 on the F32 path)");
   if (max_lines < 0 || (max_lines & (max_lines - 1)) != 0)
     return fail(P3G_E_ARG, "max_lines must be 0 or a power of two");
   *out = nullptr;
@@ -1173,15 +1180,29 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     if (f64) return 8;
     return (n & (n - 1)) == 0 ? 32 : 16;
   };
+  auto wide_ok = [&](int n) { return f64 && (max_radix == 0 || max_radix >= 16) && n >= 256 && (n & (n - 1)) == 0; };
   auto add_axis = [&](AxisPlan& ap, int n, int lines) -> bool {
-    if (!build_stages(n, axis_pow2(n), tw, ap.sp)) return false;
+    if (!build_stages(n, f64 ? std::min(axis_pow2(n), 8) : axis_pow2(n), tw, ap.sp)) return false;
     ap.tw_lo = tw.mark;
     ap.tw_cnt = (int)tw.v.size() - tw.mark;
     if (!size_tile(ap, n, lines, f64, &ap == &p->ax_x ? x_max_m : strided_max_m)) return false;
     ap.sp_index = (int)sps.size();
     sps.push_back(ap.sp);
+    // F64 power-of-two lines of at least 256 points: radix-16 stages for
+    // the wide pipelined kernels (1024 = 16 x 16 x 4 against 8 x 8 x 4 x 4)
+    if (wide_ok(n)) {
+      StagePlan w;
+      if (build_stages(n, 16, tw, w) && w.cnt[1] > 0) {
+        ap.spw = w;
+        ap.tw_lo_w = tw.mark;
+        ap.tw_cnt_w = (int)tw.v.size() - tw.mark;
+        ap.spw_index = (int)sps.size();
+        sps.push_back(w);
+      }
+    }
     return true;
   };
+
   auto bad = [&](const std::string& m) {
     delete p;
     return fail(P3G_E_UNSUPPORTED, m);
@@ -1197,20 +1218,23 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     // line padding for the X tiles (pad_index in p3g_engine.cuh): only for
     // all-power-of-two plans whose every N/R is a multiple of the first radix
     AxisPlan& ax = p->ax_x;
-    int ps = 0;
-    if (ax.sp.nstages > 0 && !ax.sp.has_generic) {
-      const int r0 = ax.sp.radix[0];
-      bool ok = (r0 & (r0 - 1)) == 0 && r0 >= 4;
-      for (int i = 0; ok && i < ax.sp.nstages; ++i) {
-        const int r = ax.sp.radix[i];
-        ok = (r & (r - 1)) == 0 && (nx / r) % r0 == 0;
-      }
-      if (ok) ps = ilog2(r0);
-    }
     const int nh2 = 2 * (nx / 2 + 1);
-    ax.ps = ps;
-    ax.ls = nx + (ps ? nx >> ps : 0);
-    if (ax.ls < nh2) ax.ls = nh2;
+    auto pad_of = [&](const StagePlan& sp, int& ps, int& ls) {
+      ps = 0;
+      if (sp.nstages > 0 && !sp.has_generic) {
+        const int r0 = sp.radix[0];
+        bool ok = (r0 & (r0 - 1)) == 0 && r0 >= 4;
+        for (int i = 0; ok && i < sp.nstages; ++i) {
+          const int r = sp.radix[i];
+          ok = (r & (r - 1)) == 0 && (nx / r) % r0 == 0;
+        }
+        if (ok) ps = ilog2(r0);
+      }
+      ls = nx + (ps ? nx >> ps : 0);
+      if (ls < nh2) ls = nh2;
+    };
+    pad_of(ax.sp, ax.ps, ax.ls);
+    if (ax.spw_index >= 0) pad_of(ax.spw, ax.ps_w, ax.ls_w);
     ax.smem = (size_t)ax.M * ax.ls * (f64 ? 16 : 8) * (ax.sp.has_generic ? 2 : 1);
     if (ax.smem > 227 * 1024) {
       delete p;

@@ -31,6 +31,18 @@ struct AxisPlan {
   int pipe_bps = 1;  // resident CTAs per SM of the pipelined kernel
   int pipe_e = 8;    // elements per thread of the pipelined kernel (PipeLimits)
   int pipe_nbuf = 2; // tile buffers of the pipelined kernel
+  // F64 wide pipelined kernels (16 points per thread): a second stage plan
+  // with radix-16 stages and its twiddle slice; every other kernel runs sp
+  StagePlan spw{};
+  int spw_index = -1;  // -1: none, the pipelined kernel runs sp
+  int tw_lo_w = 0, tw_cnt_w = 0;
+  int ls_w = 0, ps_w = 0;  // X axis: line-pair stride and padding of the wide tiles
+  // the pipelined kernel's stage plan index, twiddle slice and X tile layout
+  int pipe_sp() const { return spw_index >= 0 ? spw_index : sp_index; }
+  int pipe_tw_lo() const { return spw_index >= 0 ? tw_lo_w : tw_lo; }
+  int pipe_tw_cnt() const { return spw_index >= 0 ? tw_cnt_w : tw_cnt; }
+  int pipe_ls() const { return spw_index >= 0 ? ls_w : ls; }
+  int pipe_ps() const { return spw_index >= 0 ? ps_w : ps; }
 };
 
 struct TimerRec {
