@@ -1180,7 +1180,12 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     if (f64) return 8;
     return (n & (n - 1)) == 0 ? 32 : 16;
   };
-  auto wide_ok = [&](int n) { return f64 && (max_radix == 0 || max_radix >= 16) && n >= 256 && (n & (n - 1)) == 0; };
+  // the F64 wide kernels pay off on the Y pass (1024 points: 8.2 -> 7.8 ms at
+  // 1024^3); the X passes (128-thread CTAs) and the Z passes (user-format
+  // stores) ran slower with them, so only the Y axis gets a radix-16 plan
+  auto wide_ok = [&](const AxisPlan& ap, int n) {
+    return f64 && &ap == &p->ax_y && (max_radix == 0 || max_radix >= 16) && n >= 256 && (n & (n - 1)) == 0;
+  };
   auto add_axis = [&](AxisPlan& ap, int n, int lines) -> bool {
     if (!build_stages(n, f64 ? std::min(axis_pow2(n), 8) : axis_pow2(n), tw, ap.sp)) return false;
     ap.tw_lo = tw.mark;
@@ -1188,9 +1193,9 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     if (!size_tile(ap, n, lines, f64, &ap == &p->ax_x ? x_max_m : strided_max_m)) return false;
     ap.sp_index = (int)sps.size();
     sps.push_back(ap.sp);
-    // F64 power-of-two lines of at least 256 points: radix-16 stages for
-    // the wide pipelined kernels (1024 = 16 x 16 x 4 against 8 x 8 x 4 x 4)
-    if (wide_ok(n)) {
+    // F64 power-of-two Y lines of at least 256 points: radix-16 stages for
+    // the wide pipelined kernel (1024 = 16 x 16 x 4 against 8 x 8 x 4 x 4)
+    if (wide_ok(ap, n)) {
       StagePlan w;
       if (build_stages(n, 16, tw, w) && w.cnt[1] > 0) {
         ap.spw = w;
