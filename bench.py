@@ -639,6 +639,18 @@ def run_serving(torch, pg, n_requests, plain_f64_gpts, slots=3):
                             "requests waiting 8 ms first"})
     if plain_f64_gpts:
         out["capacity_vs_plain_f64_1024cubed"] = round(out["capacity_gpts_s"] / plain_f64_gpts, 3)
+    # closed-loop capacity with device-resident inputs (no host transfers): the
+    # kernels' throughput on the same request mix
+    dev_reqs = serve.make_requests(min(600, n_requests), seed=50)
+    srv.run(serve.make_requests(64, seed=51))
+    t = time.perf_counter()
+    srv.run(dev_reqs)
+    dev_wall = time.perf_counter() - t
+    out["device_resident_capacity_req_s"] = round(len(dev_reqs) / dev_wall, 1)
+    out["device_resident_capacity_gpts_s"] = round(sum(r.points for r in dev_reqs) / dev_wall / 1e9, 3)
+    if plain_f64_gpts:
+        out["device_resident_capacity_vs_plain_f64_1024cubed"] = round(
+            out["device_resident_capacity_gpts_s"] / plain_f64_gpts, 3)
     srv.close()
     return out
 
