@@ -83,6 +83,12 @@ struct SParams {
   // columns per copy.
   int xphase;
   RangeParams range;  // user-format input (Z backward) or output (Z forward) of the F64 path
+  // first launch of a four-step line (longer than one tile): the stored
+  // element of row jo, o1 is multiplied by w_N^(o1 jo) (conjugated with
+  // tw4_conj), N = tw4_n, from a table of the N roots (null: no twiddle)
+  const float4* tw4;
+  int tw4_n;
+  int tw4_conj;
 };
 
 // First column of tile xt of row (o1, o2) and the row's phase: 0, or 1 when

@@ -203,6 +203,11 @@ P3G_D void strided_tile(const SParams& prm, const StagePlan* __restrict__ sp, co
     C v;
     if (prm.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
     else v = P::from_w(sm[k * M + m]);
+    if (prm.tw4) {  // four-step twiddle w_N^(o1 jo)
+      const cdf w = load_tw(prm.tw4, (int)(((unsigned long long)o1 * (unsigned long long)jo) %
+                                           (unsigned long long)prm.tw4_n));
+      v = prm.tw4_conj ? cmul<true>(v, w) : cmul<false>(v, w);
+    }
     store_elem<P>(prm.out, prm.out_user, obase + (long long)m * prm.out_xs + (long long)jo * prm.out_axis, v, kb);
   }
 }

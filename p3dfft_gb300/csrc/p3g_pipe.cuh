@@ -293,6 +293,20 @@ P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int 
     store_elem<P>(s.out, s.out_user, obase + (long long)c * s.out_xs + (long long)jo * s.out_axis, v, kb);
   };
   const int T = blockDim.x;
+  if (s.tw4) {
+    // four-step twiddle w_N^(o1 jo) on every stored element (rows one to one)
+    const unsigned long long n4 = (unsigned long long)s.tw4_n;
+    for (int e = threadIdx.x; e < M * s.Lout; e += T) {
+      const int m = e & (M - 1), jo = e >> s.log2m;
+      if (x0 + m >= xend) continue;
+      const int c = x0 + m < s.X ? x0 + m : x0 + m - s.X;
+      C v = P::from_w(sm[jo * M + m]);
+      const cdf w = load_tw(s.tw4, (int)(((unsigned long long)o1 * (unsigned long long)jo) % n4));
+      v = s.tw4_conj ? cmul<true>(v, w) : cmul<false>(v, w);
+      store_elem<P>(s.out, s.out_user, obase + (long long)c * s.out_xs + (long long)jo * s.out_axis, v, kb);
+    }
+    return;
+  }
   if (s.out_xs == 1 && s.post == 0 && (s.smap_s0 >= s.Lout || s.smap_d == 0) && (T & (M - 1)) == 0) {
     // rows stored one to one (no pruning gap, no DST shift): each thread keeps
     // one column and walks its rows with a shared-memory address and an

@@ -326,6 +326,14 @@ int ensure_workspace(p3g_plan p, int nv) {
       return fail(P3G_E_NOMEM, "workspace allocation failed (" + std::to_string(nb) + " bytes)");
     }
   }
+  if ((p->four_y || p->four_z) && !p->wc) {
+    const size_t nc = (size_t)p->nz * std::max(p->ny, p->nyc) * p->pitch * p->esize();
+    if (cudaMalloc(&p->wc, nc) != cudaSuccess) {
+      cudaGetLastError();
+      p->wc = nullptr;
+      return fail(P3G_E_NOMEM, "workspace allocation failed (" + std::to_string(nc) + " bytes)");
+    }
+  }
   p->w_fields = nv;
   return P3G_OK;
 }
@@ -584,6 +592,82 @@ int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) 
   return P3G_OK;
 }
 
+// A Y or Z pass on lines longer than one tile, as two strided launches
+// through the scratch wc (four-step, n = n1 n2, j = j1 + n1 j2, k = k2 + n2 k1):
+// the first transforms each j1's subsequence j2 (length n2, rows n1 apart),
+// multiplies the result by w_n^(j1 k2) on its store and writes wc as
+// [field o1][k2][j1][x]; the second transforms each k2's row of j1 (length
+// n1) and stores output index k2 + n2 k1.  s is the one-launch pass (identity
+// load and store maps, no DCT/DST extension); its fields run one after another.
+template <class P>
+int run_four(p3g_plan p, const SParams& s, AxisPlan* sub, int tw4, bool fwd_sign, int nv, cudaStream_t st,
+             int max_sms = 0) {
+  const int n2 = sub[0].n, n1 = sub[1].n;
+  const long long N = (long long)n1 * n2, Pw = p->pitch;
+  const size_t es = p->esize();
+  for (int f = 0; f < nv; ++f) {
+    const char* in = static_cast<const char*>(s.in) + (size_t)f * s.in_o2 * es;
+    char* out = static_cast<char*>(s.out) + (size_t)f * s.out_o2 * es;
+    SParams a{};
+    a.in = in;
+    a.in_user = s.in_user;
+    a.in_xs = s.in_xs;
+    a.in_axis = (int)(n1 * (long long)s.in_axis);
+    a.in_o1 = s.in_axis;
+    a.in_o2 = s.in_o1;
+    a.out = p->wc;
+    a.out_xs = 1;
+    a.out_axis = (int)(n1 * Pw);
+    a.out_o1 = Pw;
+    a.out_o2 = N * Pw;
+    a.X = s.X;
+    a.O1 = n1;
+    a.L = a.N = a.Lout = n2;
+    a.lmap_a0 = a.lmap_a1 = n2;
+    a.smap_s0 = n2;
+    a.xphase = s.xphase;
+    a.range = s.range;
+    a.tw4 = p->d_tw + tw4;
+    a.tw4_n = (int)N;
+    a.tw4_conj = fwd_sign ? 0 : 1;
+    int rc = run_strided<P>(p, a, sub[0], fwd_sign, s.O1, st, max_sms);
+    if (rc) return rc;
+    SParams b{};
+    b.in = p->wc;
+    b.in_xs = 1;
+    b.in_axis = (int)Pw;
+    b.in_o1 = n1 * Pw;
+    b.in_o2 = N * Pw;
+    b.out = out;
+    b.out_user = s.out_user;
+    b.out_xs = s.out_xs;
+    b.out_axis = (int)(n2 * (long long)s.out_axis);
+    b.out_o1 = s.out_axis;
+    b.out_o2 = s.out_o1;
+    b.X = s.X;
+    b.O1 = n2;
+    b.L = b.N = b.Lout = n1;
+    b.lmap_a0 = b.lmap_a1 = n1;
+    b.smap_s0 = n1;
+    b.range = s.range;
+    rc = run_strided<P>(p, b, sub[1], fwd_sign, s.O1, st, max_sms);
+    if (rc) return rc;
+  }
+  return P3G_OK;
+}
+
+// The Y pass or the Z pass of a direction, one launch or four-step.
+template <class P>
+int run_y(p3g_plan p, SParams& y, bool fwd_sign, int nv, cudaStream_t st, int max_sms = 0) {
+  if (p->four_y) return run_four<P>(p, y, p->ly, p->tw4_y, fwd_sign, nv, st, max_sms);
+  return run_strided<P>(p, y, p->ax_y, fwd_sign, nv, st, max_sms);
+}
+template <class P>
+int run_z(p3g_plan p, SParams& z, int zi, bool fwd_sign, int nv, cudaStream_t st) {
+  if (zi == 0 && p->four_z) return run_four<P>(p, z, p->lz, p->tw4_z, fwd_sign, nv, st);
+  return run_strided<P>(p, z, p->ax_z[zi], fwd_sign, nv, st);
+}
+
 }  // namespace
 
 namespace p3g {
@@ -835,12 +919,12 @@ int do_ftran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   }
   {
     PassTimer tm(p, 6, st);
-    if ((rc = run_strided<P>(p, y, p->ax_y, true, nv, st))) return rc;
+    if ((rc = run_y<P>(p, y, true, nv, st))) return rc;
     tm.done();
   }
   {
     PassTimer tm(p, 7, st);
-    if ((rc = run_strided<P>(p, z, p->ax_z[zi], fsign, nv, st))) return rc;
+    if ((rc = run_z<P>(p, z, zi, fsign, nv, st))) return rc;
     tm.done();
   }
   return P3G_OK;
@@ -863,12 +947,12 @@ int do_btran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   if ((rc = launch_range_scan(p, in, 2LL * p->nxhpc * p->nyc * p->nzc, 2 * dim_in, nv, st))) return rc;
   {
     PassTimer tm(p, 8, st);
-    if ((rc = run_strided<P>(p, z, p->ax_z[zi], fsign, nv, st))) return rc;
+    if ((rc = run_z<P>(p, z, zi, fsign, nv, st))) return rc;
     tm.done();
   }
   {
     PassTimer tm(p, 9, st);
-    if ((rc = run_strided<P>(p, y, p->ax_y, false, nv, st))) return rc;
+    if ((rc = run_y<P>(p, y, false, nv, st))) return rc;
     tm.done();
   }
   {
@@ -986,7 +1070,7 @@ int do_ftran_to_host(p3g_plan p, const void* in, void* out_host, void* stage, co
       if (e != cudaSuccess) break;
       SParams ys = y_planes(y, slabs[k].y0, slabs[k].y1, es);
       PassTimer tm(p, 6, aux);
-      if ((rc = run_strided<P>(p, ys, p->ax_y, true, 1, aux, y_sms))) return rc;
+      if ((rc = run_y<P>(p, ys, true, 1, aux, y_sms))) return rc;
       tm.done();
     }
     if (e == cudaSuccess) e = cudaEventRecord(ev.ev[slabs.size() + 1], aux);
@@ -1000,7 +1084,7 @@ int do_ftran_to_host(p3g_plan p, const void* in, void* out_host, void* stage, co
     }
     {
       PassTimer tm(p, 6, st);
-      if ((rc = run_strided<P>(p, y, p->ax_y, true, 1, st))) return rc;
+      if ((rc = run_y<P>(p, y, true, 1, st))) return rc;
       tm.done();
     }
   }
@@ -1012,7 +1096,7 @@ int do_ftran_to_host(p3g_plan p, const void* in, void* out_host, void* stage, co
     SParams zc = z_rows(z, y0, y1, es);
     {
       PassTimer tm(p, 7, st);
-      if ((rc = run_strided<P>(p, zc, p->ax_z[zi], fsign, 1, st))) return rc;
+      if ((rc = run_z<P>(p, zc, zi, fsign, 1, st))) return rc;
       tm.done();
     }
     cudaError_t e = cudaEventRecord(evs.ev[c], st);
@@ -1069,7 +1153,7 @@ int do_btran_from_host(p3g_plan p, const void* in_host, void* stage, void* out, 
     if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("host to device copy: ") + cudaGetErrorString(e));
     SParams zc = z_rows(z, y0, y1, es);
     PassTimer tm(p, 8, st);
-    if ((rc = run_strided<P>(p, zc, p->ax_z[zi], fsign, 1, st))) return rc;
+    if ((rc = run_z<P>(p, zc, zi, fsign, 1, st))) return rc;
     tm.done();
   }
   if (!device_memory(out) && p->nz >= 2) {
@@ -1084,7 +1168,7 @@ int do_btran_from_host(p3g_plan p, const void* in_host, void* stage, void* out, 
       SParams ys = y_planes(y, slabs[k].y0, slabs[k].y1, es);
       {
         PassTimer tm(p, 9, st);
-        if ((rc = run_strided<P>(p, ys, p->ax_y, false, 1, st, y_sms))) return rc;
+        if ((rc = run_y<P>(p, ys, false, 1, st, y_sms))) return rc;
         tm.done();
       }
       e = cudaEventRecord(ev.ev[k], st);
@@ -1102,7 +1186,7 @@ int do_btran_from_host(p3g_plan p, const void* in_host, void* stage, void* out, 
   }
   {
     PassTimer tm(p, 9, st);
-    if ((rc = run_strided<P>(p, y, p->ax_y, false, 1, st))) return rc;
+    if ((rc = run_y<P>(p, y, false, 1, st))) return rc;
     tm.done();
   }
   {
@@ -1246,8 +1330,26 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
       return fail(P3G_E_UNSUPPORTED, "x length " + std::to_string(nx) + " is too long");
     }
   }
-  if (!add_axis(p->ax_y, ny, p->nxhpc)) return bad("y length " + std::to_string(ny) + " is too long");
+  // lines longer than one tile: four-step passes, n = n1 n2 with n1 the
+  // divisor nearest below sqrt(n) for which both lengths fit a tile, and the
+  // n roots of unity for the twiddle between the two launches
+  auto split_four = [&](AxisPlan* sub, int n, int& tw4) -> bool {
+    for (int n1 = (int)std::sqrt((double)n); n1 >= 2; --n1) {
+      if (n % n1) continue;
+      if (!add_axis(sub[0], n / n1, p->nxhpc) || !add_axis(sub[1], n1, p->nxhpc)) continue;
+      tw4 = (int)tw.v.size();
+      for (int t = 0; t < n; ++t) tw.push_root(t, n);
+      return true;
+    }
+    return false;
+  };
+  if (!add_axis(p->ax_y, ny, p->nxhpc)) {
+    if (nyc != ny || !split_four(p->ly, ny, p->tw4_y))
+      return bad("y length " + std::to_string(ny) + " is too long" + (nyc != ny ? " for a pruned transform" : ""));
+    p->four_y = true;
+  }
   p->z_ok[0] = add_axis(p->ax_z[0], nz, p->nxhpc);
+  if (!p->z_ok[0] && nzc == nz && split_four(p->lz, nz, p->tw4_z)) p->z_ok[0] = p->four_z = true;
   p->z_ok[1] = nz >= 2 && add_axis(p->ax_z[1], 2 * (nz - 1), p->nxhpc);
   p->z_ok[2] = add_axis(p->ax_z[2], 2 * (nz + 1), p->nxhpc);
   p->z_ok[3] = add_axis(p->ax_z[3], 1, p->nxhpc);
@@ -1269,6 +1371,10 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     p->ax_x.pipe_nbuf = c2r.pipe_nbuf;
   }
   size_pipe(p->ax_y, 0, f64);
+  for (int i = 0; i < 2; ++i) {
+    if (p->four_y) size_pipe(p->ly[i], 0, f64);
+    if (p->four_z) size_pipe(p->lz[i], 0, f64);
+  }
   for (int i = 0; i < 4; ++i)
     if (p->z_ok[i]) size_pipe(p->ax_z[i], 0, f64);
   {
@@ -1279,6 +1385,10 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     };
     bps(p->ax_x, 2);
     bps(p->ax_y, 0);
+    for (int i = 0; i < 2; ++i) {
+      if (p->four_y) bps(p->ly[i], 0);
+      if (p->four_z) bps(p->lz[i], 0);
+    }
     for (int i = 0; i < 4; ++i) bps(p->ax_z[i], 0);
   }
   {
@@ -1334,6 +1444,7 @@ int p3g_plan_destroy(p3g_plan p) {
   if (p->aux) cudaStreamDestroy(p->aux);
   if (p->wa) cudaFree(p->wa);
   if (p->wb) cudaFree(p->wb);
+  if (p->wc) cudaFree(p->wc);
   if (p->d_tw) cudaFree(p->d_tw);
   if (p->d_sp) cudaFree(p->d_sp);
   if (p->d_err) cudaFree(p->d_err);
@@ -1526,6 +1637,7 @@ long long p3g_plan_device_bytes(p3g_plan p) {
   long long b = (long long)p->tw_bytes + 6LL * sizeof(StagePlan);
   if (p->wa) b += (long long)p->nz * p->ny * p->pitch * p->w_fields * p->esize();
   if (p->wb) b += (long long)p->nz * p->nyc * p->pitch * p->w_fields * p->esize();
+  if (p->wc) b += (long long)p->nz * std::max(p->ny, p->nyc) * p->pitch * p->esize();
   return b;
 }
 

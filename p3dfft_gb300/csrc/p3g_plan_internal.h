@@ -98,6 +98,14 @@ struct p3g_plan_s {
   // check, [2] the same measured by the auto-bias reduction of the current call
   int* d_err = nullptr;
   bool use_pipe = true, use_tma = true;
+  // four-step passes for Y or Z (FFT) lines longer than one shared-memory
+  // tile: n = n1 n2, the first launch transforms length n2 (lz[0], ly[0]),
+  // the second length n1 (ly[1], lz[1]); tw4_* is the twiddle-table offset of
+  // the n roots w_n^t; wc holds one field between the two launches
+  AxisPlan ly[2], lz[2];
+  bool four_y = false, four_z = false;
+  int tw4_y = 0, tw4_z = 0;
+  void* wc = nullptr;
   int range_mode = P3G_RANGE_FIXED;  // F64 path: exponent bias fixed (ebias) or picked per call on the device
   int ebias = 0;
   int log2n = 0;  // ceil(log2(nx ny 2 (nz + 1))): bound of the transform's gain

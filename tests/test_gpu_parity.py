@@ -436,8 +436,41 @@ def test_longest_lines(torch_cuda, case):
         assert orc.relative_l2(gr, wr) <= F32_TOL
 
 
-@pytest.mark.parametrize("shape", [(8192, 4, 4), (4, 8192, 4), (4, 4, 16384)])
-def test_too_long_lines_are_rejected(torch_cuda, shape):
+# Y and Z lines longer than one tile (4096 points F64, 8192 F32) run as
+# four-step passes (two launches through a scratch field, n = n1 n2)
+@pytest.mark.parametrize("case", [((6, 16384, 4), "f64", False), ((4, 6, 12288), "f64", False),
+                                  ((8, 8192, 6), "f64", True), ((10, 6, 10000), "f64", False),
+                                  ((4, 16384, 4), "f32", False), ((6, 4, 24576), "f32", True)])
+def test_long_lines_four_step(torch_cuda, case):
+    import p3dfft_gb300 as pg
+    shape, prec, stride1 = case
+    a = _rand(shape[::-1], 44)
+    p = pg.F64 if prec == "f64" else pg.F32
+    gb, wb, gr, wr = _run_pair(torch_cuda, shape, a, "fft", "tff", p, stride1=stride1)
+    if prec == "f64":
+        assert orc.normalised_linf(gb, wb) <= F64_TOL
+        assert orc.normalised_linf(gr, wr) <= F64_TOL
+    else:
+        assert orc.relative_l2(gb, wb) <= F32_TOL
+        assert orc.relative_l2(gr, wr) <= F32_TOL
+
+
+def test_long_lines_many_fields(torch_cuda):
+    # nv fields: the four-step passes run field after field
+    import p3dfft_gb300 as pg
+    nx, ny, nz, nv = 4, 5000, 6, 3
+    plan = pg.Plan(nx, ny, nz)
+    ref = orc.OraclePlan(nx, ny, nz)
+    a = _rand((nv, nz, ny, nx), 45)
+    b = plan.ftran_r2c(torch_cuda.from_numpy(a).cuda(), nv=nv).cpu().numpy()
+    for v in range(nv):
+        assert orc.normalised_linf(b[v], ref.ftran_r2c(a[v], "fft")) <= F64_TOL
+    plan.close()
+
+
+@pytest.mark.parametrize("args", [(8192, 4, 4), (4, 8192, 4, 4, 6000, 4), (4, 4, 16384, 4, 4, 9000)])
+def test_too_long_lines_are_rejected(torch_cuda, args):
+    # x lines beyond one tile, and pruned long y or z lines, are refused
     import p3dfft_gb300 as pg
     with pytest.raises(pg.P3DFFTError, match="too long|unsupported"):
-        pg.Plan(*shape, precision=pg.F64)
+        pg.Plan(*args, precision=pg.F64)
