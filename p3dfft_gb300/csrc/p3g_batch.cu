@@ -171,7 +171,7 @@ static int build_chains(p3g_batch b, int njobs, const p3g_job* jobs, int threads
     if (jb.kind < P3G_JOB_ROUNDTRIP || jb.kind > P3G_JOB_SPECTRUM) return fail(P3G_E_ARG, who + "unknown kind");
     if (!jb.in || !jb.out || !jb.work) return fail(P3G_E_ARG, who + "NULL array");
     if (!p->z_ok[0]) return fail(P3G_E_UNSUPPORTED, who + "Z FFT unsupported for nz");
-    if (p->four_y || p->four_z) return fail(P3G_E_UNSUPPORTED, who + "lines longer than one tile (four-step)");
+    if (p->four_x || p->four_y || p->four_z) return fail(P3G_E_UNSUPPORTED, who + "lines longer than one tile (four-step)");
     const JobLayout L = job_layout(p, jb.kind);
     unsigned char* w = static_cast<unsigned char*>(jb.work);
     void* wa = w;

@@ -100,6 +100,19 @@ P3G_HD int strided_phase(const SParams& s, int o1, int o2) {
                 (unsigned long long)o2 * s.in_o2) & 1u);
 }
 
+// Long X lines (four-step, p3g_kernels_impl.cuh): pack, split, merge, unpack.
+struct XLongParams {
+  const void* in;
+  void* out;
+  long long in_line, out_line;  // element strides between lines of the real or half-spectrum arrays
+  int nlines;                   // lines per field
+  int nx;                       // line length N
+  int nkeep;                    // half-spectrum modes kept
+  int out_user;                 // split: 1 stores the user complex format (X-only transform)
+  RangeParams range;            // pack: binary64 input; unpack and user-format split: output
+};
+
+
 struct ChebyParams {
   void* data;          // user complex output of the 'ffc' transform
   long long field;     // element stride between fields
@@ -158,6 +171,9 @@ cudaError_t launch_strided(const SParams& p, const StagePlan* sp, const float4* 
                            size_t smem, int nfields, cudaStream_t st);
 template <class P>
 cudaError_t launch_cheby(const ChebyParams& p, int nfields, cudaStream_t st);
+// long X lines: kind 0 pack, 1 split, 2 merge, 3 unpack (p3g_kernels_impl.cuh)
+template <class P>
+cudaError_t launch_x_long(int kind, const XLongParams& q, int sm_count, cudaStream_t st);
 
 // pipelined kernels (p3g_pipe.cuh)
 struct SPipeParams;

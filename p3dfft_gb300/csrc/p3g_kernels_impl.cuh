@@ -1,6 +1,8 @@
 // Pass kernels, instantiated once per path by p3g_kernels_f64.cu / _f32.cu.
 #pragma once
 
+#include <algorithm>
+
 #include "p3g_pipe.cuh"
 
 namespace p3g {
@@ -260,6 +262,122 @@ __global__ void k_cheby(const ChebyParams prm) {
   d[0] = UC{v0.x * (R)0.5, v0.y * (R)0.5};
 }
 
+// ------------------------------------------------- long X lines (four-step)
+// X lines longer than one tile go through a complex buffer T of one line per
+// pair of real lines (z = x1 + i x2, N = nx points per line, pair p at p N):
+// pack before the complex four-step transform and split after it (r2c), merge
+// before it and unpack after it (c2r).  A pair whose second line is past the
+// field's last line holds zeros there.
+
+P3G_D long long grid_stride_start() { return (long long)blockIdx.x * blockDim.x + threadIdx.x; }
+P3G_D long long grid_stride() { return (long long)gridDim.x * blockDim.x; }
+
+template <class P>
+__global__ void __launch_bounds__(256) k_x_pack(const XLongParams q) {
+  using UR = typename P::UR;
+  const UR* in = static_cast<const UR*>(q.in);
+  typename P::W* T = static_cast<typename P::W*>(q.out);
+  const int kb = range_k(q.range);
+  const long long total = (long long)((q.nlines + 1) / 2) * q.nx;
+  uint32_t amax = 0;
+  for (long long e = grid_stride_start(); e < total; e += grid_stride()) {
+    const long long pr = e / q.nx, x = e - pr * q.nx;
+    const UR a = in[2 * pr * q.in_line + x];
+    const UR b = 2 * pr + 1 < q.nlines ? in[(2 * pr + 1) * q.in_line + x] : UR(0);
+    P::track(amax, a);
+    P::track(amax, b);
+    T[e] = P::to_w(P::make(P::from_ur(a, kb), P::from_ur(b, kb)));
+  }
+  range_flush(q.range, amax);
+}
+
+// X1[k] = (Z[k] + conj Z[N-k]) / 2, X2[k] = -i (Z[k] - conj Z[N-k]) / 2
+template <class P>
+__global__ void __launch_bounds__(256) k_x_split(const XLongParams q) {
+  using C = typename P::C;
+  const typename P::W* T = static_cast<const typename P::W*>(q.in);
+  const int kb = range_k(q.range);
+  const long long total = (long long)((q.nlines + 1) / 2) * q.nkeep;
+  for (long long e = grid_stride_start(); e < total; e += grid_stride()) {
+    const long long pr = e / q.nkeep;
+    const int k = (int)(e - pr * q.nkeep);
+    const C a = P::from_w(T[pr * q.nx + k]);
+    const C b = cconj(P::from_w(T[pr * q.nx + (k == 0 ? 0 : q.nx - k)]));
+    const C x1 = cscale2(a + b, 0.5f), x2 = cscale2(rot<-1>(a - b), 0.5f);
+    const long long o1 = 2 * pr * q.out_line + k, o2 = o1 + q.out_line;
+    if (q.out_user) {
+      auto* out = static_cast<typename P::UC*>(q.out);
+      out[o1] = P::to_uc(x1, kb);
+      if (2 * pr + 1 < q.nlines) out[o2] = P::to_uc(x2, kb);
+    } else {
+      auto* out = static_cast<typename P::W*>(q.out);
+      out[o1] = P::to_w(x1);
+      if (2 * pr + 1 < q.nlines) out[o2] = P::to_w(x2);
+    }
+  }
+}
+
+// Z[k] = X1[k] + i X2[k] over every k < N, X[k] = conj X[N-k] above N/2, the
+// imaginary parts of the k = 0 and k = N/2 modes dropped (as c2r does),
+// modes at or beyond nkeep zero
+template <class P>
+__global__ void __launch_bounds__(256) k_x_merge(const XLongParams q) {
+  using C = typename P::C;
+  const typename P::W* in = static_cast<const typename P::W*>(q.in);
+  typename P::W* T = static_cast<typename P::W*>(q.out);
+  const long long total = (long long)((q.nlines + 1) / 2) * q.nx;
+  for (long long e = grid_stride_start(); e < total; e += grid_stride()) {
+    const long long pr = e / q.nx;
+    const int k = (int)(e - pr * q.nx);
+    const bool mir = 2 * k > q.nx;
+    const int kk = mir ? q.nx - k : k;
+    C x1 = P::zero(), x2 = P::zero();
+    if (kk < q.nkeep) {
+      x1 = P::from_w(in[2 * pr * q.in_line + kk]);
+      if (2 * pr + 1 < q.nlines) x2 = P::from_w(in[(2 * pr + 1) * q.in_line + kk]);
+    }
+    if (kk == 0 || 2 * kk == q.nx) {
+      x1 = P::make(P::re(x1), P::re(P::zero()));
+      x2 = P::make(P::re(x2), P::re(P::zero()));
+    }
+    if (mir) {
+      x1 = cconj(x1);
+      x2 = cconj(x2);
+    }
+    T[e] = P::to_w(x1 + rot<1>(x2));
+  }
+}
+
+template <class P>
+__global__ void __launch_bounds__(256) k_x_unpack(const XLongParams q) {
+  using UR = typename P::UR;
+  const typename P::W* T = static_cast<const typename P::W*>(q.in);
+  UR* out = static_cast<UR*>(q.out);
+  const int kb = range_k(q.range);
+  const long long total = (long long)((q.nlines + 1) / 2) * q.nx;
+  for (long long e = grid_stride_start(); e < total; e += grid_stride()) {
+    const long long pr = e / q.nx, x = e - pr * q.nx;
+    const typename P::C z = P::from_w(T[e]);
+    out[2 * pr * q.out_line + x] = P::to_ur(P::re(z), kb);
+    if (2 * pr + 1 < q.nlines) out[(2 * pr + 1) * q.out_line + x] = P::to_ur(P::im(z), kb);
+  }
+}
+
+// kind: 0 pack, 1 split, 2 merge, 3 unpack
+template <class P>
+cudaError_t launch_x_long(int kind, const XLongParams& q, int sm_count, cudaStream_t st) {
+  const long long per = kind == 1 ? q.nkeep : q.nx;
+  const long long total = (long long)((q.nlines + 1) / 2) * per;
+  const int blocks = (int)std::max(1LL, std::min((total + 255) / 256, (long long)sm_count * 8));
+  switch (kind) {
+    case 0: k_x_pack<P><<<blocks, 256, 0, st>>>(q); break;
+    case 1: k_x_split<P><<<blocks, 256, 0, st>>>(q); break;
+    case 2: k_x_merge<P><<<blocks, 256, 0, st>>>(q); break;
+    default: k_x_unpack<P><<<blocks, 256, 0, st>>>(q); break;
+  }
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- launchers
 template <class P>
 cudaError_t launch_x_r2c(const XParams& p, const StagePlan* sp, const float4* tw, int threads, size_t smem,
@@ -394,6 +512,7 @@ int pipe_blocks_per_sm(int kind, int E, int threads, size_t smem) {
   template cudaError_t launch_strided<P>(const SParams&, const StagePlan*, const float4*, bool, int, size_t, int,  \
                                          cudaStream_t);                                                            \
   template cudaError_t launch_cheby<P>(const ChebyParams&, int, cudaStream_t);                                     \
+  template cudaError_t launch_x_long<P>(int, const XLongParams&, int, cudaStream_t);                               \
   template int pipe_blocks_per_sm<P>(int, int, int, size_t);                                                            \
   template cudaError_t launch_strided_pipe<P>(const CUtensorMap*, const SPipeParams&, const StagePlan*,             \
                                               const float4*, bool, int, int, size_t, int, cudaStream_t);          \

@@ -99,7 +99,7 @@ extern "C" int p3g_ftran_r2c_noalloc(p3g_plan p, const void* in, void* out, cons
     default: return fail(P3G_E_ARG, std::string("Unknown transform type: ") + op[2]);
   }
   if (!p->z_ok[zi]) return fail(P3G_E_UNSUPPORTED, std::string("Z transform '") + op[2] + "' unsupported for nz");
-  if (p->four_y || (zi == 0 && p->four_z))
+  if (p->four_x || p->four_y || (zi == 0 && p->four_z))
     return fail(P3G_E_UNSUPPORTED, "allocation-free transform: lines longer than one tile need a second workspace");
   const size_t esize = p->esize();
   const size_t wa_bytes = ((size_t)p->nz * p->ny * p->pitch * esize + 255) / 256 * 256;

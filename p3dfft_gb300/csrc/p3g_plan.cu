@@ -326,12 +326,20 @@ int ensure_workspace(p3g_plan p, int nv) {
       return fail(P3G_E_NOMEM, "workspace allocation failed (" + std::to_string(nb) + " bytes)");
     }
   }
-  if ((p->four_y || p->four_z) && !p->wc) {
-    const size_t nc = (size_t)p->nz * std::max(p->ny, p->nyc) * p->pitch * p->esize();
+  if ((p->four_y || p->four_z || p->four_x) && !p->wc) {
+    const size_t nc = p->wc_bytes();
     if (cudaMalloc(&p->wc, nc) != cudaSuccess) {
       cudaGetLastError();
       p->wc = nullptr;
       return fail(P3G_E_NOMEM, "workspace allocation failed (" + std::to_string(nc) + " bytes)");
+    }
+  }
+  if (p->four_x && !p->wd) {
+    const size_t nd = (size_t)p->xpairs() * p->nx * p->esize();
+    if (cudaMalloc(&p->wd, nd) != cudaSuccess) {
+      cudaGetLastError();
+      p->wd = nullptr;
+      return fail(P3G_E_NOMEM, "workspace allocation failed (" + std::to_string(nd) + " bytes)");
     }
   }
   p->w_fields = nv;
@@ -601,9 +609,10 @@ int run_x_c2r(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) 
 // load and store maps, no DCT/DST extension); its fields run one after another.
 template <class P>
 int run_four(p3g_plan p, const SParams& s, AxisPlan* sub, int tw4, bool fwd_sign, int nv, cudaStream_t st,
-             int max_sms = 0) {
+             int max_sms = 0, long long Pw = 0) {
   const int n2 = sub[0].n, n1 = sub[1].n;
-  const long long N = (long long)n1 * n2, Pw = p->pitch;
+  const long long N = (long long)n1 * n2;
+  if (Pw <= 0) Pw = p->pitch;  // scratch row pitch (at least s.X)
   const size_t es = p->esize();
   for (int f = 0; f < nv; ++f) {
     const char* in = static_cast<const char*>(s.in) + (size_t)f * s.in_o2 * es;
@@ -666,6 +675,80 @@ template <class P>
 int run_z(p3g_plan p, SParams& z, int zi, bool fwd_sign, int nv, cudaStream_t st) {
   if (zi == 0 && p->four_z) return run_four<P>(p, z, p->lz, p->tw4_z, fwd_sign, nv, st);
   return run_strided<P>(p, z, p->ax_z[zi], fwd_sign, nv, st);
+}
+
+// Long X lines: the pair buffer wd as a strided pass over pairs (columns,
+// nx apart) along x (rows, adjacent), transformed in place by run_four.
+SParams x_long_pass(p3g_plan p, int nlines) {
+  SParams s{};
+  s.in = s.out = p->wd;
+  s.in_xs = s.out_xs = p->nx;
+  s.in_axis = s.out_axis = 1;
+  s.X = (nlines + 1) / 2;
+  s.O1 = 1;
+  s.L = s.N = s.Lout = p->nx;
+  s.lmap_a0 = s.lmap_a1 = p->nx;
+  s.smap_s0 = p->nx;
+  return s;
+}
+int x_long(p3g_plan p, int kind, const XLongParams& q, cudaStream_t st) {
+  const cudaError_t e = p->prec == P3G_F64 ? launch_x_long<PathF64>(kind, q, p->sm_count, st)
+                                           : launch_x_long<PathF32>(kind, q, p->sm_count, st);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("long X line launch: ") + cudaGetErrorString(e));
+  p->launches++;
+  return P3G_OK;
+}
+
+// The X passes of a direction, one launch or (lines longer than one tile)
+// pack / four-step / split per field.
+template <class P>
+int run_xr2c(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) {
+  if (!p->four_x) return run_x_r2c<P>(p, x, nv, st, max_sms);
+  const size_t ur = sizeof(typename P::UR), es = p->esize();
+  for (int f = 0; f < nv; ++f) {
+    XLongParams q{};
+    q.in = static_cast<const char*>(x.in) + (size_t)f * x.in_field * ur;
+    q.out = p->wd;
+    q.in_line = x.in_line;
+    q.nlines = x.nlines;
+    q.nx = x.nx;
+    q.nkeep = x.nkeep;
+    q.range = x.range;
+    int rc = x_long(p, 0, q, st);
+    if (rc) return rc;
+    SParams s = x_long_pass(p, x.nlines);
+    if ((rc = run_four<P>(p, s, p->lx, p->tw4_x, true, 1, st, max_sms, p->xpitch()))) return rc;
+    q.in = p->wd;
+    q.out = static_cast<char*>(x.out) + (size_t)f * x.out_field * es;
+    q.out_line = x.out_line;
+    q.out_user = x.out_user;
+    if ((rc = x_long(p, 1, q, st))) return rc;
+  }
+  return P3G_OK;
+}
+template <class P>
+int run_xc2r(p3g_plan p, XParams& x, int nv, cudaStream_t st, int max_sms = 0) {
+  if (!p->four_x) return run_x_c2r<P>(p, x, nv, st, max_sms);
+  const size_t ur = sizeof(typename P::UR), es = p->esize();
+  for (int f = 0; f < nv; ++f) {
+    XLongParams q{};
+    q.in = static_cast<const char*>(x.in) + (size_t)f * x.in_field * es;
+    q.out = p->wd;
+    q.in_line = x.in_line;
+    q.nlines = x.nlines;
+    q.nx = x.nx;
+    q.nkeep = x.nkeep;
+    int rc = x_long(p, 2, q, st);
+    if (rc) return rc;
+    SParams s = x_long_pass(p, x.nlines);
+    if ((rc = run_four<P>(p, s, p->lx, p->tw4_x, false, 1, st, max_sms, p->xpitch()))) return rc;
+    q.in = p->wd;
+    q.out = static_cast<char*>(x.out) + (size_t)f * x.out_field * ur;
+    q.out_line = x.out_line;
+    q.range = x.range;
+    if ((rc = x_long(p, 3, q, st))) return rc;
+  }
+  return P3G_OK;
 }
 
 }  // namespace
@@ -914,7 +997,7 @@ int do_ftran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   if ((rc = launch_range_scan(p, in, (long long)p->nx * p->ny * p->nz, dim_in, nv, st))) return rc;
   {
     PassTimer tm(p, 4, st);
-    if ((rc = run_x_r2c<P>(p, x, nv, st))) return rc;
+    if ((rc = run_xr2c<P>(p, x, nv, st))) return rc;
     tm.done();
   }
   {
@@ -957,7 +1040,7 @@ int do_btran(p3g_plan p, const void* in, void* out, const char* op, int nv, long
   }
   {
     PassTimer tm(p, 11, st);
-    if ((rc = run_x_c2r<P>(p, x, nv, st))) return rc;
+    if ((rc = run_xc2r<P>(p, x, nv, st))) return rc;
     tm.done();
   }
   return P3G_OK;
@@ -1062,7 +1145,7 @@ int do_ftran_to_host(p3g_plan p, const void* in, void* out_host, void* stage, co
       XParams xs = x_planes(x, p->ny, slabs[k].y0, slabs[k].y1, sizeof(typename P::UR), es);
       {
         PassTimer tm(p, 4, st);
-        if ((rc = run_x_r2c<P>(p, xs, 1, st, x_sms))) return rc;
+        if ((rc = run_xr2c<P>(p, xs, 1, st, x_sms))) return rc;
         tm.done();
       }
       e = cudaEventRecord(ev.ev[k + 1], st);
@@ -1079,7 +1162,7 @@ int do_ftran_to_host(p3g_plan p, const void* in, void* out_host, void* stage, co
   } else {
     {
       PassTimer tm(p, 4, st);
-      if ((rc = run_x_r2c<P>(p, x, 1, st))) return rc;
+      if ((rc = run_xr2c<P>(p, x, 1, st))) return rc;
       tm.done();
     }
     {
@@ -1176,7 +1259,7 @@ int do_btran_from_host(p3g_plan p, const void* in_host, void* stage, void* out, 
       if (e != cudaSuccess) break;
       XParams xs = x_planes(x, p->ny, slabs[k].y0, slabs[k].y1, es, sizeof(typename P::UR));
       PassTimer tm(p, 11, aux);
-      if ((rc = run_x_c2r<P>(p, xs, 1, aux, x_sms))) return rc;
+      if ((rc = run_xc2r<P>(p, xs, 1, aux, x_sms))) return rc;
       tm.done();
     }
     if (e == cudaSuccess) e = cudaEventRecord(ev.ev[slabs.size()], aux);
@@ -1191,7 +1274,7 @@ int do_btran_from_host(p3g_plan p, const void* in_host, void* stage, void* out, 
   }
   {
     PassTimer tm(p, 11, st);
-    if ((rc = run_x_c2r<P>(p, x, 1, st))) return rc;
+    if ((rc = run_xc2r<P>(p, x, 1, st))) return rc;
     tm.done();
   }
   return P3G_OK;
@@ -1302,7 +1385,7 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
   if ((long long)p->pitch * std::max(ny, nz) >= (1LL << 31) || (long long)p->nxhpc * p->nyc >= (1LL << 31) ||
       (long long)p->nyc * p->nzc >= (1LL << 31))
     return bad("a plane of more than 2^31 elements is not supported");
-  if (!add_axis(p->ax_x, nx, (ny * nz + 1) / 2)) return bad("x length " + std::to_string(nx) + " is too long");
+  const bool x_fits = add_axis(p->ax_x, nx, (ny * nz + 1) / 2);
   {
     // line padding for the X tiles (pad_index in p3g_engine.cuh): only for
     // all-power-of-two plans whose every N/R is a multiple of the first radix
@@ -1324,6 +1407,7 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     };
     pad_of(ax.sp, ax.ps, ax.ls);
     if (ax.spw_index >= 0) pad_of(ax.spw, ax.ps_w, ax.ls_w);
+    if (!x_fits) ax.ls = 0;
     ax.smem = (size_t)ax.M * ax.ls * (f64 ? 16 : 8) * (ax.sp.has_generic ? 2 : 1);
     if (ax.smem > 227 * 1024) {
       delete p;
@@ -1333,10 +1417,10 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
   // lines longer than one tile: four-step passes, n = n1 n2 with n1 the
   // divisor nearest below sqrt(n) for which both lengths fit a tile, and the
   // n roots of unity for the twiddle between the two launches
-  auto split_four = [&](AxisPlan* sub, int n, int& tw4) -> bool {
+  auto split_four = [&](AxisPlan* sub, int n, int& tw4, int lines) -> bool {
     for (int n1 = (int)std::sqrt((double)n); n1 >= 2; --n1) {
       if (n % n1) continue;
-      if (!add_axis(sub[0], n / n1, p->nxhpc) || !add_axis(sub[1], n1, p->nxhpc)) continue;
+      if (!add_axis(sub[0], n / n1, lines) || !add_axis(sub[1], n1, lines)) continue;
       tw4 = (int)tw.v.size();
       for (int t = 0; t < n; ++t) tw.push_root(t, n);
       return true;
@@ -1344,12 +1428,17 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     return false;
   };
   if (!add_axis(p->ax_y, ny, p->nxhpc)) {
-    if (nyc != ny || !split_four(p->ly, ny, p->tw4_y))
+    if (nyc != ny || !split_four(p->ly, ny, p->tw4_y, p->nxhpc))
       return bad("y length " + std::to_string(ny) + " is too long" + (nyc != ny ? " for a pruned transform" : ""));
     p->four_y = true;
   }
   p->z_ok[0] = add_axis(p->ax_z[0], nz, p->nxhpc);
-  if (!p->z_ok[0] && nzc == nz && split_four(p->lz, nz, p->tw4_z)) p->z_ok[0] = p->four_z = true;
+  if (!p->z_ok[0] && nzc == nz && split_four(p->lz, nz, p->tw4_z, p->nxhpc)) p->z_ok[0] = p->four_z = true;
+  if (!x_fits) {
+    if (!split_four(p->lx, nx, p->tw4_x, (int)std::min<long long>(p->xpairs(), 1 << 30)))
+      return bad("x length " + std::to_string(nx) + " is too long");
+    p->four_x = true;
+  }
   p->z_ok[1] = nz >= 2 && add_axis(p->ax_z[1], 2 * (nz - 1), p->nxhpc);
   p->z_ok[2] = add_axis(p->ax_z[2], 2 * (nz + 1), p->nxhpc);
   p->z_ok[3] = add_axis(p->ax_z[3], 1, p->nxhpc);
@@ -1445,6 +1534,7 @@ int p3g_plan_destroy(p3g_plan p) {
   if (p->wa) cudaFree(p->wa);
   if (p->wb) cudaFree(p->wb);
   if (p->wc) cudaFree(p->wc);
+  if (p->wd) cudaFree(p->wd);
   if (p->d_tw) cudaFree(p->d_tw);
   if (p->d_sp) cudaFree(p->d_sp);
   if (p->d_err) cudaFree(p->d_err);
@@ -1572,7 +1662,7 @@ int p3g_ftran_r2c_1d(p3g_plan p, const void* in, void* out, void* stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   int rc = launch_range_scan(p, in, x.in_field, x.in_field, 1, st);
   if (rc) return rc;
-  return p->prec == P3G_F64 ? run_x_r2c<PathF64>(p, x, 1, st) : run_x_r2c<PathF32>(p, x, 1, st);
+  return p->prec == P3G_F64 ? run_xr2c<PathF64>(p, x, 1, st) : run_xr2c<PathF32>(p, x, 1, st);
 }
 
 int p3g_cheby(p3g_plan p, const void* in, void* out, double lz, int nv, long long dim_in, long long dim_out,
@@ -1637,7 +1727,8 @@ long long p3g_plan_device_bytes(p3g_plan p) {
   long long b = (long long)p->tw_bytes + 6LL * sizeof(StagePlan);
   if (p->wa) b += (long long)p->nz * p->ny * p->pitch * p->w_fields * p->esize();
   if (p->wb) b += (long long)p->nz * p->nyc * p->pitch * p->w_fields * p->esize();
-  if (p->wc) b += (long long)p->nz * std::max(p->ny, p->nyc) * p->pitch * p->esize();
+  if (p->wc) b += (long long)p->wc_bytes();
+  if (p->wd) b += p->xpairs() * p->nx * (long long)p->esize();
   return b;
 }
 

@@ -102,13 +102,25 @@ struct p3g_plan_s {
   // tile: n = n1 n2, the first launch transforms length n2 (lz[0], ly[0]),
   // the second length n1 (ly[1], lz[1]); tw4_* is the twiddle-table offset of
   // the n roots w_n^t; wc holds one field between the two launches
-  AxisPlan ly[2], lz[2];
-  bool four_y = false, four_z = false;
-  int tw4_y = 0, tw4_z = 0;
+  AxisPlan ly[2], lz[2], lx[2];
+  bool four_y = false, four_z = false, four_x = false;
+  int tw4_y = 0, tw4_z = 0, tw4_x = 0;
   void* wc = nullptr;
+  void* wd = nullptr;  // long X lines: one complex line per pair of real lines
+  size_t wc_bytes() const;
   int range_mode = P3G_RANGE_FIXED;  // F64 path: exponent bias fixed (ebias) or picked per call on the device
   int ebias = 0;
   int log2n = 0;  // ceil(log2(nx ny 2 (nz + 1))): bound of the transform's gain
 
   size_t esize() const { return prec == P3G_F64 ? 16 : 8; }
+  // long X lines: pairs of real lines per field, and the row pitch of the
+  // four-step scratch for them (pairs rounded up to 16 elements)
+  long long xpairs() const { return ((long long)ny * nz + 1) / 2; }
+  long long xpitch() const { return (xpairs() + 15) / 16 * 16; }
 };
+
+inline size_t p3g_plan_s::wc_bytes() const {
+  size_t n = (four_y || four_z) ? (size_t)nz * (ny > nyc ? ny : nyc) * pitch : 0;
+  if (four_x && (size_t)nx * xpitch() > n) n = (size_t)nx * xpitch();
+  return n * esize();
+}

@@ -440,7 +440,10 @@ def test_longest_lines(torch_cuda, case):
 # four-step passes (two launches through a scratch field, n = n1 n2)
 @pytest.mark.parametrize("case", [((6, 16384, 4), "f64", False), ((4, 6, 12288), "f64", False),
                                   ((8, 8192, 6), "f64", True), ((10, 6, 10000), "f64", False),
-                                  ((4, 16384, 4), "f32", False), ((6, 4, 24576), "f32", True)])
+                                  ((4, 16384, 4), "f32", False), ((6, 4, 24576), "f32", True),
+                                  ((8192, 6, 4), "f64", False), ((8192, 5, 3), "f64", True),
+                                  ((12000, 4, 6), "f64", False), ((16384, 6, 4), "f32", False),
+                                  ((10240, 3, 3), "f32", False)])
 def test_long_lines_four_step(torch_cuda, case):
     import p3dfft_gb300 as pg
     shape, prec, stride1 = case
@@ -468,9 +471,9 @@ def test_long_lines_many_fields(torch_cuda):
     plan.close()
 
 
-@pytest.mark.parametrize("args", [(8192, 4, 4), (4, 8192, 4, 4, 6000, 4), (4, 4, 16384, 4, 4, 9000)])
+@pytest.mark.parametrize("args", [(4, 8192, 4, 4, 6000, 4), (4, 4, 16384, 4, 4, 9000)])
 def test_too_long_lines_are_rejected(torch_cuda, args):
-    # x lines beyond one tile, and pruned long y or z lines, are refused
+    # pruned y or z lines beyond one tile are refused
     import p3dfft_gb300 as pg
     with pytest.raises(pg.P3DFFTError, match="too long|unsupported"):
         pg.Plan(*args, precision=pg.F64)
