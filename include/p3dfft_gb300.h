@@ -223,9 +223,17 @@ int p3g_plan_set_range(p3g_plan plan, int mode, int bias);
 int p3g_plan_check_range(p3g_plan plan, int* bias, int* emax);
 
 /* Synchronises and reports a kernel-side failure recorded on the plan's
- * device flag (a pipelined pass whose bounded wait for a tile copy expired),
- * or P3G_E_RANGE as p3g_plan_check_range (whose record it clears). */
+ * device flag (a pipelined pass whose bounded wait for a tile copy expired;
+ * reported once, then cleared), or P3G_E_RANGE as p3g_plan_check_range
+ * (whose record it clears). */
 int p3g_plan_status(p3g_plan plan);
+/* Test hook for the bounded tile waits (no counterpart in the reference):
+ * with on != 0 the pipelined passes' TMA tile barriers expect 16 bytes more
+ * than their copies deliver, so every wait runs out (about half a second),
+ * the pass records the time-out and ends early, and the next p3g_plan_status
+ * reports it (then clears it); on = 0 restores.  Nothing faults and the
+ * context stays usable. */
+int p3g_plan_block_tiles(p3g_plan plan, int on);
 /* Kernel selection: use_pipe = persistent double-buffered passes (default 1),
  * use_tma = TMA tensor-tile copies where the layout allows (default 1).  With
  * both 0 every pass runs the single-tile kernels. */

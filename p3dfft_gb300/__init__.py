@@ -210,6 +210,10 @@ class Plan:
         transform's input was outside the exponent window (p3g_plan_status)."""
         _check(_core().p3g_plan_status(self._h))
 
+    def block_tiles(self, on=True):
+        """Test hook: the pipelined passes' tile waits run out (p3g_plan_block_tiles)."""
+        _check(_core().p3g_plan_block_tiles(self._h, int(on)))
+
     def set_range(self, mode=RANGE_FIXED, bias=0):
         """Exponent bias of the F64 path (p3g_plan_set_range): RANGE_FIXED
         with inputs scaled by 2^-bias, or RANGE_AUTO (picked per call on the

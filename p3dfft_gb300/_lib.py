@@ -38,6 +38,7 @@ CORE_SIGNATURES = {
                                              ctypes.c_void_p]),
     "p3g_plan_status": (ctypes.c_int, [ctypes.c_void_p]),
     "p3g_plan_set_range": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "p3g_plan_block_tiles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "p3g_plan_check_range": (ctypes.c_int, [ctypes.c_void_p, _c_int_p, _c_int_p]),
     "p3g_plan_create_tuned": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
                                              ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,

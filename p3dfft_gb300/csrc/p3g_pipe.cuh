@@ -33,6 +33,7 @@ struct SPipeParams {
   int use_tma;              // 1: TMA tensor tiles, 0: cp.async
   int brows, nbox;          // TMA: rows per box, boxes per tile
   int box_bytes;
+  int tx_extra;             // test hook: bytes the barrier expects beyond the boxes (0)
   int chunk;                // cp.async bytes per element copy (16 or 8)
 };
 
@@ -233,7 +234,7 @@ P3G_D void strided_issue(const SPipeParams& q, const CUtensorMap* tin, int tile,
     if (threadIdx.x == 0) {
       constexpr int kWords = sizeof(W) / 4;
       fence_proxy_async_smem();
-      mbar_arrive_expect_tx(&sm.mbar[b], (uint32_t)(q.nbox * q.box_bytes));
+      mbar_arrive_expect_tx(&sm.mbar[b], (uint32_t)(q.nbox * q.box_bytes + q.tx_extra));
       for (int i = 0; i < q.nbox; ++i)
         tma_load_4d(dst + i * q.brows * q.s.M, tin, &sm.mbar[b], xt * q.s.M * kWords, i * q.brows, o1, o2);
     }

@@ -501,6 +501,7 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
         pp.brows = brows;
         pp.nbox = (s.L + brows - 1) / brows;
         pp.box_bytes = brows * s.M * esize;
+        pp.tx_extra = p->tx_extra;
       }
     }
     const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
@@ -1770,8 +1771,19 @@ int p3g_plan_status(p3g_plan p) {
   int flag = 0;
   if (cudaMemcpy(&flag, p->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
     return fail(P3G_E_CUDA, std::string("status read: ") + cudaGetErrorString(cudaGetLastError()));
-  if (flag) return fail(P3G_E_CUDA, "a pipelined pass timed out waiting for its tile copy (results invalid)");
+  if (flag) {
+    // reported once: the record is cleared for the calls that follow
+    if (cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess) cudaGetLastError();
+    return fail(P3G_E_CUDA, "a pipelined pass timed out waiting for its tile copy (results invalid)");
+  }
   return p3g_plan_check_range(p, nullptr, nullptr);
+}
+
+int p3g_plan_block_tiles(p3g_plan p, int on) {
+  if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  std::lock_guard<std::mutex> lk(p->mu);
+  p->tx_extra = on ? 16 : 0;
+  return P3G_OK;
 }
 
 int p3g_plan_set_options(p3g_plan p, int use_pipe, int use_tma) {

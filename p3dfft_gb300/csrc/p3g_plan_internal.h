@@ -98,6 +98,7 @@ struct p3g_plan_s {
   // check, [2] the same measured by the auto-bias reduction of the current call
   int* d_err = nullptr;
   bool use_pipe = true, use_tma = true;
+  int tx_extra = 0;  // test hook (p3g_plan_block_tiles)
   // four-step passes for Y or Z (FFT) lines longer than one shared-memory
   // tile: n = n1 n2, the first launch transforms length n2 (lz[0], ly[0]),
   // the second length n1 (ly[1], lz[1]); tw4_* is the twiddle-table offset of

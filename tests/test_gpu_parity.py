@@ -477,3 +477,28 @@ def test_too_long_lines_are_rejected(torch_cuda, args):
     import p3dfft_gb300 as pg
     with pytest.raises(pg.P3DFFTError, match="too long|unsupported"):
         pg.Plan(*args, precision=pg.F64)
+
+
+def test_tile_wait_times_out_and_context_survives(torch_cuda):
+    # the TMA tile barriers of the pipelined passes expect more bytes than
+    # their copies deliver (a host-side test hook; nothing faults): every wait
+    # runs out, the pass ends early, the status reports the time-out once, and
+    # the next transform on the same plan and context is correct
+    import time
+
+    import p3dfft_gb300 as pg
+    nx, ny, nz = 64, 48, 40
+    plan = pg.Plan(nx, ny, nz)
+    a = _rand((nz, ny, nx), 46)
+    x = torch_cuda.from_numpy(a).cuda()
+    plan.block_tiles(True)
+    t = time.perf_counter()
+    plan.ftran_r2c(x)
+    with pytest.raises(pg.P3DFFTError, match="timed out"):
+        plan.check()
+    assert time.perf_counter() - t < 60
+    plan.block_tiles(False)
+    b = plan.ftran_r2c(x)
+    plan.check()
+    assert orc.normalised_linf(b.cpu().numpy(), orc.OraclePlan(nx, ny, nz).ftran_r2c(a, "fft")) <= F64_TOL
+    plan.close()
