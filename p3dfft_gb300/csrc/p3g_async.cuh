@@ -1,9 +1,9 @@
 // Asynchronous global -> shared copies for the pipelined passes:
 //   * TMA tensor tile loads (cp.async.bulk.tensor) completing on an mbarrier,
 //   * per-thread cp.async (LDGSTS) with zero fill, tracked by commit groups.
-// Every wait on an mbarrier is bounded: after kMbarSpinLimit polls the waiting
-// thread records an error in the plan's device flag and gives up, so a
-// mis-sized transaction can never hang the GPU.
+// Every wait on an mbarrier is bounded: after a second (kMbarWaitNs) the
+// waiting thread records an error in the plan's device flag and gives up, so
+// a mis-sized transaction can never hang the GPU.
 #pragma once
 
 #include <cuda.h>
@@ -14,8 +14,18 @@
 
 namespace p3g {
 
-constexpr uint32_t kMbarSpinLimit = 1u << 22;  // x >= 32 ns backoff: well under a second
+// A wait gives up after kMbarWaitNs of the global timer (try_wait suspends
+// the thread for a hardware-chosen time on each poll, so a poll count alone
+// is a poor clock), or after kMbarSpinLimit polls at the latest.
+constexpr uint64_t kMbarWaitNs = 1000000000ull;  // 1 s
+constexpr uint32_t kMbarSpinLimit = 1u << 24;
 constexpr int kErrMbarTimeout = 1;
+
+P3G_D uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 P3G_D uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -60,8 +70,11 @@ P3G_D bool mbar_try_wait(uint64_t* b, uint32_t parity) {
 // Bounded wait for phase `parity` of the barrier; false (and the error flag
 // set) if it did not complete within the limit.
 P3G_D bool mbar_wait_bounded(uint64_t* b, uint32_t parity, int* err) {
+  if (mbar_try_wait(b, parity)) return true;
+  const uint64_t t0 = global_ns();
   for (uint32_t i = 0; i < kMbarSpinLimit; ++i) {
     if (mbar_try_wait(b, parity)) return true;
+    if ((i & 15) == 15 && global_ns() - t0 > kMbarWaitNs) break;
     if (i > 16) __nanosleep(32);
   }
   if (err) atomicExch(err, kErrMbarTimeout);
