@@ -185,9 +185,9 @@ long long p3g_plan_launches(p3g_plan plan);
  * frameworks that route every allocation through their own pool, loops that
  * cannot afford cudaMalloc's device synchronisation): the workspace is a
  * fixed 32 MiB device array inside the library, not a cudaMalloc.  Grids
- * whose workspace ((ny + nyc)*nz*pitch*16 bytes for F64, *8 for F32, pitch =
- * nxc/2+1 rounded up to 8 resp. 16; about 120^3 F64 or 150^3 F32 at most)
- * exceeds it are rejected with P3G_E_UNSUPPORTED.  The plan must exist
+ * whose workspace (nz*ny*pitch*16 bytes for F64, *8 for F32, pitch =
+ * nxc/2+1 rounded up to 8 resp. 16, plus nz*nyc*pitch*16 resp. 8 when
+ * nyc < ny) exceeds it are rejected with P3G_E_UNSUPPORTED.  The plan must exist
  * already (p3g_plan_create allocates).  The first call on each device looks
  * up the array's device address, so make it before any stream capture.
  * All calls share the array: calls that overlap on the GPU race. */

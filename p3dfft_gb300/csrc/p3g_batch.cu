@@ -101,7 +101,7 @@ cudaError_t batch_launch(const BatchPass* d_pass, int npass, int nitems, int* ct
 
 size_t round256(size_t b) { return (b + 255) / 256 * 256; }
 
-// Workspace of one job inside its work buffer: wa | wb (the forward Y output) | complex
+// Workspace of one job inside its work buffer: wa | wb (Y pruning) | complex
 // field (round trip and spectrum jobs).
 struct JobLayout {
   size_t wa, wb, cplx, total;
@@ -110,7 +110,7 @@ JobLayout job_layout(p3g_plan p, int kind) {
   JobLayout l{};
   const size_t es = p->esize();
   l.wa = round256((size_t)p->nz * p->ny * p->pitch * es);
-  l.wb = round256((size_t)p->nz * p->nyc * p->pitch * es);
+  l.wb = p->nyc < p->ny ? round256((size_t)p->nz * p->nyc * p->pitch * es) : 0;
   l.cplx = (kind == P3G_JOB_ROUNDTRIP || kind == P3G_JOB_SPECTRUM)
                ? round256((size_t)p->nxhpc * p->nyc * p->nzc * es)
                : 0;
@@ -250,7 +250,7 @@ static int build_chains(p3g_batch b, int njobs, const p3g_job* jobs, int threads
       XParams x;
       SParams y, z;
       void* fout = jb.kind == P3G_JOB_FORWARD ? jb.out : cplx;
-      make_forward_params(p, jb.in, fout, wa, wb, 0, rsize, csize, x, y, z);
+      make_forward_params(p, jb.in, fout, wa, wb, 0, rsize, csize, x, y, z, true);
       x.range = range_params(p, true, false);
       z.range = range_params(p, false, false);
       x_pass(kBXr2c, x);

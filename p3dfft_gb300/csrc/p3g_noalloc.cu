@@ -64,7 +64,8 @@ int forward_passes(p3g_plan p, const void* in, void* out, int zi, bool fsign, vo
   XParams x;
   SParams y, z;
   const long long rsize = (long long)p->nx * p->ny * p->nz;
-  make_forward_params(p, in, out, wa, wb, zi, rsize, (long long)p->nxhpc * p->nyc * p->nzc, x, y, z);
+  // the Y output in place in wa (no second buffer unless y is pruned)
+  make_forward_params(p, in, out, wa, wb, zi, rsize, (long long)p->nxhpc * p->nyc * p->nzc, x, y, z, true);
   x.range = range_params(p, true, true);
   z.range = range_params(p, false, true);
   const int rc = launch_range_scan(p, in, rsize, rsize, 1, st);  // P3G_RANGE_AUTO only
@@ -103,7 +104,7 @@ extern "C" int p3g_ftran_r2c_noalloc(p3g_plan p, const void* in, void* out, cons
     return fail(P3G_E_UNSUPPORTED, "allocation-free transform: lines longer than one tile need a second workspace");
   const size_t esize = p->esize();
   const size_t wa_bytes = ((size_t)p->nz * p->ny * p->pitch * esize + 255) / 256 * 256;
-  const size_t wb_bytes = (size_t)p->nz * p->nyc * p->pitch * esize;
+  const size_t wb_bytes = p->nyc < p->ny ? (size_t)p->nz * p->nyc * p->pitch * esize : 0;
   if (wa_bytes + wb_bytes > kNoAllocScratchBytes)
     return fail(P3G_E_UNSUPPORTED, "allocation-free transform: the grid needs " + std::to_string(wa_bytes + wb_bytes) +
                                        " bytes of workspace, more than its fixed " +

@@ -808,12 +808,14 @@ int launch_range_scan(p3g_plan p, const void* in, long long n, long long field, 
 // nyc-nycph (seg_copy_y, ftran.F90:736-738), Z ybuf -> user complex with the
 // Z op and z pruning (seg_copy_z, ftran.F90:705-706).
 void make_forward_params(p3g_plan p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
-                         long long dim_out, XParams& x, SParams& y, SParams& z) {
+                         long long dim_out, XParams& x, SParams& y, SParams& z, bool y_zyx) {
   const long long P_ = p->pitch;
   const long long wa_field = (long long)p->nz * p->ny * P_;
   const long long wb_field = (long long)p->nz * p->nyc * P_;
-  void* ybuf = wb;
-  const long long y_field = wb_field;
+  // the Y output: wb as [y][z][x], or (y_zyx) [z][y][x] in wa itself unless
+  // y is pruned
+  void* ybuf = y_zyx && p->nyc == p->ny ? wa : wb;
+  const long long y_field = y_zyx && p->nyc == p->ny ? wa_field : wb_field;
   x = XParams{};
   x.in = in;
   x.out = wa;
@@ -840,8 +842,8 @@ void make_forward_params(p3g_plan p, const void* in, void* out, void* wa, void* 
   // the Y output (Z input) is stored [y][z][x]: the Z pass then reads its
   // lines at a stride of one row (pitch) instead of a whole plane, and the
   // scattered accesses move to the Y pass's stores
-  y.out_axis = (int)(p->nz * P_);
-  y.out_o1 = P_;
+  y.out_axis = (int)(y_zyx ? P_ : p->nz * P_);
+  y.out_o1 = y_zyx ? (long long)p->nyc * P_ : P_;
   y.out_o2 = y_field;
   y.X = p->nxhpc;
   y.O1 = p->nz;
@@ -862,8 +864,8 @@ void make_forward_params(p3g_plan p, const void* in, void* out, void* wa, void* 
   z.in = ybuf;
   z.out = out;
   z.out_user = 1;
-  z.in_axis = (int)P_;
-  z.in_o1 = (long long)p->nz * P_;
+  z.in_axis = (int)(y_zyx ? p->nyc * P_ : P_);
+  z.in_o1 = y_zyx ? P_ : (long long)p->nz * P_;
   z.in_o2 = y_field;
   if (p->layout == P3G_LAYOUT_STRIDE1) {  // (nzc, nyc, nxhpc), z fastest (module.F90:245-254)
     z.out_axis = 1;

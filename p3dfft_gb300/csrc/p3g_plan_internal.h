@@ -58,8 +58,11 @@ namespace p3g {
 // Pass parameters of one field's forward (X, Y, Z) and backward (Z, Y, X)
 // transform with workspaces wa/wb; zi = Z op index (0 fft, 1 dct, 2 dst,
 // 3 none).  Defined in p3g_plan.cu.
+// y_zyx keeps the Y output in [z][y][x] order (in place in wa when y is not
+// pruned) as the batch kernel's small grids prefer; by default it goes to wb
+// as [y][z][x], so that the Z pass reads rows one pitch apart.
 void make_forward_params(p3g_plan_s* p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
-                         long long dim_out, XParams& x, SParams& y, SParams& z);
+                         long long dim_out, XParams& x, SParams& y, SParams& z, bool y_zyx = false);
 void make_backward_params(p3g_plan_s* p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
                           long long dim_out, SParams& z, SParams& y, XParams& x);
 // Exponent-window parameters of a pass converting the plan's binary64 user
