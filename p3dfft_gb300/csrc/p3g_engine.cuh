@@ -346,10 +346,10 @@ __device__ __forceinline__ void run_family(const Tile<P>& t, const float4* __res
 }
 
 // Runs all stages of the plan on the tile (sm must be filled and
-// synchronised).  MAXR is the largest power-of-two radix compiled in: 32 on
-// the F32 path; 8 on F64, 16 in the F64 wide pipelined kernels (a
-// double-float radix-16 codelet needs ~200 registers, so only kernels that
-// may use them carry it; their plans' stages never exceed MAXR).  The plan orders its stages by radix family (16, 8, 4, 2, 3,
+// synchronised).  MAXR is the largest power-of-two radix compiled in: 16 on
+// the F32 path and 8 on F64, 32 and 16 in the wide pipelined kernels (the
+// large codelets need many registers, so only kernels that may use them
+// carry them; the plans they run never exceed MAXR).  The plan orders its stages by radix family (16, 8, 4, 2, 3,
 // 5, then generic primes) and each family runs in its own loop: a single loop
 // with a switch over the radix makes the register allocator keep the live
 // ranges of every codelet at once and spill.  Radix 16 is compiled only for
@@ -362,7 +362,7 @@ __device__ __forceinline__ void run_family(const Tile<P>& t, const float4* __res
 // tile still holds the raw line pairs of an X r2c or c2r tile (kRawR2C,
 // kRawC2R; plans without generic stages only), read by the first stage.
 template <class P, int DIR, int E = kElemsPerThread, int LAY = kAnyLayout, int RAW = kRawNone,
-          int MAXR = P::kF64 ? 8 : 32>
+          int MAXR = P::kF64 ? 8 : 16>
 __device__ __forceinline__ void cta_fft(const Tile<P>& t, const StagePlan* __restrict__ sp,
                                         const float4* __restrict__ tw, int tw_base = 0) {
   const int N = __ldg(&sp->n);

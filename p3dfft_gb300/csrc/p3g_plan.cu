@@ -229,14 +229,14 @@ static void pipe_shape(bool xk, int& max_threads, int& regs) {
 
 // Pipelined kernels: two tile buffers (1 KB aligned), the axis's twiddles
 // and two mbarriers in shared memory.  kind: 0 strided, 1 r2c, 2 c2r.  The
-// elements per thread follow the axis's stages: 8 on the F64 path; on F32, 32
-// when a radix-32 stage is present, else 16.
+// elements per thread follow the axis's stage plans: 16 on F64 and 32 on F32
+// when the axis has a wide plan, else 8 and 16.
 static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   ap.pipe_ok = false;
   if (ap.sp.nstages < 1 || ap.sp.has_generic || ap.n < 2) return;
   const size_t esize = f64 ? 16 : 8;
   const bool xk = kind != 0;  // X kernels have their own launch shape (XPipeLimits)
-  const int E = f64 ? (ap.spw_index >= 0 ? 16 : 8) : (ap.sp.cnt[0] > 0 ? 32 : 16);
+  const int E = f64 ? (ap.spw_index >= 0 ? 16 : 8) : (ap.spw_index >= 0 ? 32 : 16);
   ap.pipe_e = E;
   int max_threads = 0, regs_max = 0;
   if (f64) {
@@ -1350,24 +1350,29 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     if (f64) return 8;
     return (n & (n - 1)) == 0 ? 32 : 16;
   };
-  // the F64 wide kernels pay off on the Y pass (1024 points: 8.2 -> 7.8 ms at
-  // 1024^3); the X passes (128-thread CTAs) and the Z passes (user-format
-  // stores) ran slower with them, so only the Y axis gets a radix-16 plan
+  // Every axis has a stage plan of radices up to 8 (F64) or 16 (F32) for the
+  // kernels that run 8 or 16 points per thread (and the single-tile and batch
+  // kernels); power-of-two lines add a wide plan for the wide pipelined
+  // kernels: radix 32 on F32 (every axis), radix 16 on F64, where it pays off
+  // on the Y pass only (1024 points: 8.2 -> 7.8 ms at 1024^3; the X passes'
+  // 128-thread CTAs and the Z passes' user-format stores ran slower with it)
   auto wide_ok = [&](const AxisPlan& ap, int n) {
-    return f64 && &ap == &p->ax_y && (max_radix == 0 || max_radix >= 16) && n >= 256 && (n & (n - 1)) == 0;
+    if ((n & (n - 1)) != 0) return false;
+    if (f64) return &ap == &p->ax_y && (max_radix == 0 || max_radix >= 16) && n >= 256;
+    return max_radix == 0 || max_radix >= 32;
   };
   auto add_axis = [&](AxisPlan& ap, int n, int lines) -> bool {
-    if (!build_stages(n, f64 ? std::min(axis_pow2(n), 8) : axis_pow2(n), tw, ap.sp)) return false;
+    if (!build_stages(n, std::min(axis_pow2(n), f64 ? 8 : 16), tw, ap.sp)) return false;
     ap.tw_lo = tw.mark;
     ap.tw_cnt = (int)tw.v.size() - tw.mark;
     if (!size_tile(ap, n, lines, f64, &ap == &p->ax_x ? x_max_m : strided_max_m)) return false;
     ap.sp_index = (int)sps.size();
     sps.push_back(ap.sp);
-    // F64 power-of-two Y lines of at least 256 points: radix-16 stages for
-    // the wide pipelined kernel (1024 = 16 x 16 x 4 against 8 x 8 x 4 x 4)
+    // the wide plan (1024 = 16 x 16 x 4 against 8 x 8 x 4 x 4 on F64, 32 x 32
+    // against 16 x 16 x 4 on F32), kept when it has a wide stage
     if (wide_ok(ap, n)) {
       StagePlan w;
-      if (build_stages(n, 16, tw, w) && w.cnt[1] > 0) {
+      if (build_stages(n, f64 ? 16 : 32, tw, w) && w.cnt[f64 ? 1 : 0] > 0) {
         ap.spw = w;
         ap.tw_lo_w = tw.mark;
         ap.tw_cnt_w = (int)tw.v.size() - tw.mark;
