@@ -330,6 +330,12 @@ def accuracy(torch, grid, ops, kind, x, plan64, plan32, stream, lz=None, seed=No
     return out
 
 
+def pass_times(timers, steps):
+    """Per-pass milliseconds per round trip from a plan's timer slots."""
+    slots = {"x_r2c": 4, "y_fwd": 6, "z_fwd": 7, "z_bwd": 8, "y_bwd": 9, "x_c2r": 11}
+    return {k: round(timers[i] * 1e3 / steps, 4) for k, i in slots.items()}
+
+
 def measure_config(torch, pg, name, args, dev, stream, seed, with_accuracy=True, clock=None):
     """One workload: FP64 and FP32 round trips timed with CUDA events on the
     plan's stream (the plan timers give the per-pass times; `clock`, a
@@ -347,7 +353,7 @@ def measure_config(torch, pg, name, args, dev, stream, seed, with_accuracy=True,
     plan.set_options(*MODES[args.mode])
     b = torch.empty(plan.complex_shape, dtype=torch.complex128, device=dev)
     r = torch.empty_like(x)
-    plan32 = pg.Plan(nx, ny, nz, precision=pg.F32)
+    plan32 = pg.Plan(nx, ny, nz, precision=pg.F32, timers=True)
     plan32.set_options(*MODES[args.mode])
     x32 = x.float()
     b32 = torch.empty(plan32.complex_shape, dtype=torch.complex64, device=dev)
@@ -356,6 +362,7 @@ def measure_config(torch, pg, name, args, dev, stream, seed, with_accuracy=True,
         ms64, launches = time_device(torch, plan, x, b, r, ops, args.steps, args.warmup, stream)
         ms32, _ = time_device(torch, plan32, x32, b32, r32, ops, args.steps, args.warmup, stream)
     timers = plan.timers()
+    t32 = plan32.timers()
     del b, r, x32, b32, r32
     peak, _ = load_peaks()
     bm64, bm32 = bytes_model(grid, 8), bytes_model(grid, 4)
@@ -364,7 +371,7 @@ def measure_config(torch, pg, name, args, dev, stream, seed, with_accuracy=True,
                 "step_frac_of_measured_hbm": round(bm64["rt"] / (ms64 * 1e-3) / 1e9 / peak, 4)},
         "f32": {"value": round(npts / (ms32 * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_step": round(ms32, 4),
                 "step_frac_of_measured_hbm": round(bm32["rt"] / (ms32 * 1e-3) / 1e9 / peak, 4),
-                "speedup_vs_f64": round(ms64 / ms32, 3)},
+                "speedup_vs_f64": round(ms64 / ms32, 3), "passes_ms": pass_times(t32, args.steps)},
     })
     if with_accuracy:
         res["error"] = accuracy(torch, grid, ops, cfg["input"], x, plan, plan32, stream,
@@ -472,7 +479,8 @@ def run_ours(args):
         "error": error,
         "f32": {"value": round(aggregate_gpts(world, npts, ms32), 3), "unit": UNIT, "ms_per_step": round(ms32, 4),
                 "speedup_vs_f64": round(ms64 / ms32, 3),
-                "step_frac": round(bytes_model(grid, 4)["rt"] / (ms32 * 1e-3) / 1e9 / peak, 4)},
+                "step_frac": round(bytes_model(grid, 4)["rt"] / (ms32 * 1e-3) / 1e9 / peak, 4),
+                "passes_ms": head["f32"]["passes_ms"]},
         "passes_ms": {k: round(v, 4) for k, v in pass_ms.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "launches_per_step": nl,
                      "algorithmic_bytes_per_launch": int(dom_bytes),

@@ -261,7 +261,7 @@ static int build_chains(p3g_batch b, int njobs, const p3g_job* jobs, int threads
       SParams z, y;
       XParams x;
       const void* bin = jb.kind == P3G_JOB_BACKWARD ? jb.in : cplx;
-      make_backward_params(p, bin, jb.out, wa, wb, 0, csize, rsize, z, y, x);
+      make_backward_params(p, bin, jb.out, wa, wb, 0, csize, rsize, z, y, x, true);
       if (jb.kind == P3G_JOB_BACKWARD) z.range = range_params(p, true, false);  // user input
       x.range = range_params(p, false, false);
       s_pass(kBBwd, z, p->ax_z[0]);

@@ -82,6 +82,10 @@ struct SParams {
   // column 0), so that full tiles start on a 16-byte boundary and load two
   // columns per copy.
   int xphase;
+  // > 0: the pass's columns are the positions of a plane of rows holding
+  // xrow columns each, contiguous in the input (one row set, O1 = 1); the
+  // output of position c goes to row c / xrow, column c % xrow
+  int xrow;
   RangeParams range;  // user-format input (Z backward) or output (Z forward) of the F64 path
   // first launch of a four-step line (longer than one tile): the stored
   // element of row jo, o1 is multiplied by w_N^(o1 jo) (conjugated with
@@ -98,6 +102,14 @@ P3G_HD int strided_phase(const SParams& s, int o1, int o2) {
   if (!s.xphase) return 0;
   return (int)(((unsigned long long)reinterpret_cast<uintptr_t>(s.in) / 8u + (unsigned long long)o1 * s.in_o1 +
                 (unsigned long long)o2 * s.in_o2) & 1u);
+}
+
+// Output offset of tile column c: c * out_xs, or with xrow > 0 the offset of
+// its row (out_o1 apart) and column.
+P3G_HD long long strided_col_out(const SParams& s, int c) {
+  if (s.xrow <= 0) return (long long)c * s.out_xs;
+  const int r = c / s.xrow;
+  return (long long)r * s.out_o1 + (long long)(c - r * s.xrow) * s.out_xs;
 }
 
 // Long X lines (four-step, p3g_kernels_impl.cuh): pack, split, merge, unpack.

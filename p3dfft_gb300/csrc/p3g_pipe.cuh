@@ -291,7 +291,7 @@ P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int 
     C v;
     if (s.post == 1) v = rot<1>(P::from_w(sm[(k + 1) * M + m]));
     else v = P::from_w(sm[k * M + m]);
-    store_elem<P>(s.out, s.out_user, obase + (long long)c * s.out_xs + (long long)jo * s.out_axis, v, kb);
+    store_elem<P>(s.out, s.out_user, obase + strided_col_out(s, c) + (long long)jo * s.out_axis, v, kb);
   };
   const int T = blockDim.x;
   if (s.tw4) {
@@ -304,7 +304,7 @@ P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int 
       C v = P::from_w(sm[jo * M + m]);
       const cdf w = load_tw(s.tw4, (int)(((unsigned long long)o1 * (unsigned long long)jo) % n4));
       v = s.tw4_conj ? cmul<true>(v, w) : cmul<false>(v, w);
-      store_elem<P>(s.out, s.out_user, obase + (long long)c * s.out_xs + (long long)jo * s.out_axis, v, kb);
+      store_elem<P>(s.out, s.out_user, obase + strided_col_out(s, c) + (long long)jo * s.out_axis, v, kb);
     }
     return;
   }
@@ -319,7 +319,7 @@ P3G_D void strided_store(const SParams& s, const typename P::W* sm, int xt, int 
     using W = typename P::W;
     uint32_t a = (uint32_t)__cvta_generic_to_shared(sm) + (uint32_t)((j0 * M + m) * (int)sizeof(W));
     const uint32_t astep = (uint32_t)(T * (int)sizeof(W));
-    const long long o = obase + c + (long long)j0 * s.out_axis;
+    const long long o = obase + strided_col_out(s, c) + (long long)j0 * s.out_axis;
     const long long ostep = (long long)js * s.out_axis;
     if (s.out_user) {
       typename P::UC* d = static_cast<typename P::UC*>(s.out) + o;

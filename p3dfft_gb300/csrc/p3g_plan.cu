@@ -478,7 +478,27 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
     s.xtiles = (s.X + s.M - 1) / s.M;
     SPipeParams pp{};
     pp.s = s;
-    pp.c.tiles_per_field = s.xtiles * s.O1;
+    // TMA boxes copy rows one to one: the load map must be the identity
+    // (no zero band and no shift; the backward passes of an unpruned grid
+    // have a0 == a1 and d == 0)
+    const bool identity_rows = (s.lmap_a0 >= s.L && s.lmap_a1 >= s.L) || (s.lmap_d == 0 && s.lmap_a0 >= s.lmap_a1);
+    // binary32 user rows of an odd length (the Z backward input, nx/2+1
+    // modes) start at odd 8-byte elements, which neither TMA nor 16-byte
+    // copies address.  When the rows of a plane are contiguous the pass takes
+    // the plane's positions as its columns instead: every tile then starts
+    // on a 16-byte boundary and loads by TMA boxes, and the store splits each
+    // position into its row and column
+    if (!P::kF64 && s.xphase && p->use_tma && s.in_xs == 1 && s.in_o1 == s.X && s.O1 > 1 && !s.tw4 &&
+        s.pre <= 1 && identity_rows && aligned_to(s.in, 16) && s.in_axis % 2 == 0 &&
+        (nv == 1 || s.in_o2 % 2 == 0) && (long long)s.X * s.O1 < (1ll << 30) && device_memory(s.in)) {
+      pp.s.xrow = s.X;
+      pp.s.X = s.X * s.O1;
+      pp.s.O1 = 1;
+      pp.s.in_o1 = (long long)s.in_axis * s.L;
+      pp.s.xphase = 0;
+      pp.s.xtiles = (pp.s.X + s.M - 1) / s.M;
+    }
+    pp.c.tiles_per_field = pp.s.xtiles * pp.s.O1;
     pp.c.ntiles = pp.c.tiles_per_field * nv;
     pp.c.tw_base = ap.pipe_tw_lo();
     pp.c.tw_count = ap.pipe_tw_cnt();
@@ -488,14 +508,11 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
     pp.chunk = esize;
     CUtensorMap map;
     std::memset(&map, 0, sizeof(map));
-    // TMA boxes copy rows one to one: the load map must be the identity
-    // (no zero band and no shift; the backward passes of an unpruned grid
-    // have a0 == a1 and d == 0)
-    const bool identity_rows = (s.lmap_a0 >= s.L && s.lmap_a1 >= s.L) || (s.lmap_d == 0 && s.lmap_a0 >= s.lmap_a1);
-    if (p->use_tma && s.in_xs == 1 && s.pre <= 1 && identity_rows && !s.xphase &&
-        (!s.in_user || device_memory(s.in))) {
-      const int brows = pick_box_rows(s.L, ap.n, s.M, esize);
-      if (brows > 0 && encode_strided_map(&map, s.in, esize, s.X, s.L, s.O1, nv, s.in_axis, s.in_o1, s.in_o2, s.M,
+    const SParams& q = pp.s;
+    if (p->use_tma && q.in_xs == 1 && q.pre <= 1 && identity_rows && !q.xphase &&
+        (!q.in_user || device_memory(q.in))) {
+      const int brows = pick_box_rows(q.L, ap.n, q.M, esize);
+      if (brows > 0 && encode_strided_map(&map, q.in, esize, q.X, q.L, q.O1, nv, q.in_axis, q.in_o1, q.in_o2, q.M,
                                           brows)) {
         pp.use_tma = 1;
         pp.brows = brows;
@@ -892,18 +909,19 @@ void make_forward_params(p3g_plan p, const void* in, void* out, void* wa, void* 
   z.xtiles = (z.X + z.M - 1) / z.M;
 }
 
-// Pass parameters of a backward transform: Z user complex -> zbuf with the
-// z zero fill (seg_copy_z + seg_zero_z, btran.F90:553-555), Y zbuf -> wa with
-// the y zero fill (seg_copy_y + seg_zero_y, btran.F90:585-588), X c2r wa ->
-// user real with x modes beyond nxhpc read as zero (seg_zero_x,
-// btran.F90:662-663).
+// Pass parameters of a backward transform: Z user complex -> zbuf ([y][z][x]
+// in wb; y_zyx: [z][y][x], in wa unless y is pruned) with the z zero fill
+// (seg_copy_z + seg_zero_z, btran.F90:553-555), Y zbuf -> wa with the y zero
+// fill (seg_copy_y + seg_zero_y, btran.F90:585-588), X c2r wa -> user real
+// with x modes beyond nxhpc read as zero (seg_zero_x, btran.F90:662-663).
 void make_backward_params(p3g_plan p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
-                          long long dim_out, SParams& z, SParams& y, XParams& x) {
+                          long long dim_out, SParams& z, SParams& y, XParams& x, bool y_zyx) {
   const long long P_ = p->pitch;
   const long long wa_field = (long long)p->nz * p->ny * P_;
   const long long wb_field = (long long)p->nz * p->nyc * P_;
-  void* zbuf = p->nyc < p->ny ? wb : wa;
-  const long long z_field = p->nyc < p->ny ? wb_field : wa_field;
+  const bool in_wa = y_zyx && p->nyc == p->ny;
+  void* zbuf = in_wa ? wa : wb;
+  const long long z_field = in_wa ? wa_field : wb_field;
   const AxisPlan& az = p->ax_z[zi];
   z = SParams{};
   z.in_xs = z.out_xs = 1;
@@ -921,8 +939,10 @@ void make_backward_params(p3g_plan p, const void* in, void* out, void* wa, void*
   z.in_o2 = dim_in;
   // binary32 complex rows of nxhpc modes start at odd elements for odd nxhpc
   z.xphase = p->prec == P3G_F32 && z.in_xs == 1;
-  z.out_axis = (int)(p->nyc * P_);
-  z.out_o1 = P_;
+  // the Z output (Y input) as [y][z][x]: the Z pass stores each line one
+  // pitch apart, so only its user-format reads are a plane apart
+  z.out_axis = (int)(y_zyx ? p->nyc * P_ : P_);
+  z.out_o1 = y_zyx ? P_ : (long long)p->nz * P_;
   z.out_o2 = z_field;
   z.X = p->nxhpc;
   z.O1 = p->nyc;
@@ -943,8 +963,8 @@ void make_backward_params(p3g_plan p, const void* in, void* out, void* wa, void*
   y.in_xs = y.out_xs = 1;
   y.in = zbuf;
   y.out = wa;
-  y.in_axis = (int)P_;
-  y.in_o1 = (long long)p->nyc * P_;
+  y.in_axis = (int)(y_zyx ? P_ : p->nz * P_);
+  y.in_o1 = y_zyx ? (long long)p->nyc * P_ : P_;
   y.in_o2 = z_field;
   y.out_axis = (int)P_;
   y.out_o1 = (long long)p->ny * P_;

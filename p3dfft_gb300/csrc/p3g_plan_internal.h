@@ -58,13 +58,15 @@ namespace p3g {
 // Pass parameters of one field's forward (X, Y, Z) and backward (Z, Y, X)
 // transform with workspaces wa/wb; zi = Z op index (0 fft, 1 dct, 2 dst,
 // 3 none).  Defined in p3g_plan.cu.
-// y_zyx keeps the Y output in [z][y][x] order (in place in wa when y is not
-// pruned) as the batch kernel's small grids prefer; by default it goes to wb
-// as [y][z][x], so that the Z pass reads rows one pitch apart.
+// y_zyx keeps the array between the Y and Z passes in [z][y][x] order (the
+// forward Y output in place in wa when y is not pruned) as the batch kernel's
+// small grids prefer; by default it is wb as [y][z][x], so that the Z pass
+// (forward reads, backward writes) walks its lines one pitch apart and each
+// pass has at most one side whose lines are a plane apart.
 void make_forward_params(p3g_plan_s* p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
                          long long dim_out, XParams& x, SParams& y, SParams& z, bool y_zyx = false);
 void make_backward_params(p3g_plan_s* p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
-                          long long dim_out, SParams& z, SParams& y, XParams& x);
+                          long long dim_out, SParams& z, SParams& y, XParams& x, bool y_zyx = false);
 // Exponent-window parameters of a pass converting the plan's binary64 user
 // data in (input = true: tracked) or out; allow_auto = false ignores the
 // auto mode (callers that run no reduction first).  Zero on the F32 path.

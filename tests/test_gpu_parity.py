@@ -132,6 +132,64 @@ def test_f32_parity(torch_cuda, shape):
     assert orc.relative_l2(gr, wr) <= F32_TOL
 
 
+# binary32 complex rows of nx/2+1 modes start at odd 8-byte elements when
+# nx/2+1 is odd: the backward Z pass then reads each plane's positions as its
+# columns (TMA) when it can, and phase-shifted tiles otherwise (pruned z, DST,
+# unaligned fields, no TMA); every form must match the oracle
+@pytest.mark.parametrize("mode", ["pipe_tma", "pipe_cpasync"])
+@pytest.mark.parametrize("case", [((64, 48, 40), "fft", "tff"), ((64, 48, 40, 64, 30, 40), "fft", "tff"),
+                                  ((64, 48, 40, 64, 48, 30), "fft", "tff"), ((40, 36, 33), "ffc", "cff"),
+                                  ((40, 36, 30), "ffs", "sff"), ((96, 20, 64), "fft", "tff")])
+def test_f32_odd_row_backward(torch_cuda, mode, case):
+    import p3dfft_gb300 as pg
+    args, opf, opb = case
+    a = _rand(args[:3][::-1], 23)
+    gb, wb, gr, wr = _run_pair(torch_cuda, args, a, opf, opb, pg.F32, mode=mode)
+    assert orc.relative_l2(gb, wb) <= F32_TOL
+    assert orc.relative_l2(gr, wr) <= F32_TOL
+
+
+@pytest.mark.parametrize("spacing", [0, 1, 2])
+def test_f32_odd_row_backward_many_fields(torch_cuda, spacing):
+    # field spacings that keep every field 16-byte aligned (0, 2) or not (1)
+    import p3dfft_gb300 as pg
+    torch = torch_cuda
+    nx, ny, nz, nv = 64, 24, 40, 3
+    plan = pg.Plan(nx, ny, nz, precision=pg.F32)
+    ref = orc.OraclePlan(nx, ny, nz)
+    csize, rsize = (nx // 2 + 1) * ny * nz, nx * ny * nz
+    dim_c, dim_r = csize + spacing, rsize + 2
+    c = _spectrum((nv, dim_c), 24)
+    r = torch.zeros((nv, dim_r), dtype=torch.float32, device="cuda")
+    plan.btran_c2r(torch.from_numpy(c).to("cuda", torch.complex64), r, op="tff", nv=nv, dim_in=dim_c,
+                   dim_out=dim_r)
+    plan.check()
+    got = r.cpu().numpy().astype(np.float64)
+    for v in range(nv):
+        cv = c[v, :csize].astype(np.complex64).astype(np.complex128).reshape(nz, ny, nx // 2 + 1)
+        want = ref.btran_c2r(cv, "tff")
+        assert orc.relative_l2(got[v, :rsize].reshape(nz, ny, nx), want) <= F32_TOL
+    plan.close()
+
+
+@pytest.mark.parametrize("chunks", [1, 3, 8])
+def test_f32_host_row_blocks_bit_identical(torch_cuda, chunks):
+    # row blocks of odd-length binary32 rows start at 16-byte boundaries or
+    # not; both load forms give the plain call's bits
+    import p3dfft_gb300 as pg
+    torch = torch_cuda
+    nx, ny, nz = 64, 21, 18
+    plan = pg.Plan(nx, ny, nz, precision=pg.F32)
+    c = torch.from_numpy(_spectrum(plan.complex_shape, 25)).to("cuda", torch.complex64)
+    want = plan.btran_c2r(c)
+    hc = c.cpu().pin_memory()
+    r = torch.zeros((nz, ny, nx), dtype=torch.float32, device="cuda")
+    plan.btran_c2r_from_host(hc, r, chunks=chunks)
+    assert torch.equal(r, want)
+    plan.check()
+    plan.close()
+
+
 def test_f64_roundtrip_sample_rule(torch_cuda):
     # driver_rand.F90: ftran 'fft', multiply by 1/N, btran 'tff', max |diff| <= 1e-14 N/4
     import p3dfft_gb300 as pg
