@@ -94,6 +94,24 @@ P3G_D void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0,
       : "memory");
 }
 
+// 4-D tiled tensor store from shared memory (bulk async group).  The
+// threads that wrote the tile fence it to the async proxy and synchronise
+// before one thread issues the store.
+P3G_D void tma_store_4d(const CUtensorMap* map, const void* src, int c0, int c1, int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4}], [%5];\n" ::"l"(map),
+      "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(src))
+      : "memory");
+}
+P3G_D void bulk_commit_group() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+// Waits until at most N of this thread's bulk groups still read shared memory.
+template <int N>
+P3G_D void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read %0;\n" ::"n"(N) : "memory");
+}
+// Waits until every bulk group of this thread has completed.
+P3G_D void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+
 // 1-D bulk copy of `bytes` (a multiple of 16, both addresses 16-byte
 // aligned) from global into shared memory, completing on `bar`.
 P3G_D void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {

@@ -191,8 +191,9 @@ cudaError_t launch_x_long(int kind, const XLongParams& q, int sm_count, cudaStre
 struct SPipeParams;
 struct XPipeParams;
 template <class P>
-cudaError_t launch_strided_pipe(const CUtensorMap* map, const SPipeParams& p, const StagePlan* sp, const float4* tw,
-                                bool forward_sign, int E, int threads, size_t smem, int grid, cudaStream_t st);
+cudaError_t launch_strided_pipe(const CUtensorMap* map, const CUtensorMap* omap, const SPipeParams& p,
+                                const StagePlan* sp, const float4* tw, bool forward_sign, int E, int threads,
+                                size_t smem, int grid, cudaStream_t st);
 template <class P>
 cudaError_t launch_xr2c_pipe(const XPipeParams& p, const StagePlan* sp, const float4* tw, int E, int threads,
                              size_t smem, int grid, cudaStream_t st);

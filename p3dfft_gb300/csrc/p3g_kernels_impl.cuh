@@ -416,25 +416,26 @@ cudaError_t launch_cheby(const ChebyParams& p, int nfields, cudaStream_t st) {
 
 // Pipelined launchers: E (elements per thread) selects the instantiation.
 template <class P, int E>
-cudaError_t launch_strided_pipe_e(const CUtensorMap* map, const SPipeParams& p, const StagePlan* sp,
-                                  const float4* tw, bool forward_sign, int threads, size_t smem, int grid,
-                                  cudaStream_t st) {
+cudaError_t launch_strided_pipe_e(const CUtensorMap* map, const CUtensorMap* omap, const SPipeParams& p,
+                                  const StagePlan* sp, const float4* tw, bool forward_sign, int threads, size_t smem,
+                                  int grid, cudaStream_t st) {
   cudaError_t ea = opt_in_smem((const void*)k_strided_pipe<P, -1, E>, 227 * 1024);
   if (ea == cudaSuccess) ea = opt_in_smem((const void*)k_strided_pipe<P, 1, E>, 227 * 1024);
   if (ea != cudaSuccess) return ea;
-  if (forward_sign) k_strided_pipe<P, -1, E><<<grid, threads, smem, st>>>(*map, p, sp, tw);
-  else k_strided_pipe<P, 1, E><<<grid, threads, smem, st>>>(*map, p, sp, tw);
+  if (forward_sign) k_strided_pipe<P, -1, E><<<grid, threads, smem, st>>>(*map, *omap, p, sp, tw);
+  else k_strided_pipe<P, 1, E><<<grid, threads, smem, st>>>(*map, *omap, p, sp, tw);
   return cudaGetLastError();
 }
 template <class P>
-cudaError_t launch_strided_pipe(const CUtensorMap* map, const SPipeParams& p, const StagePlan* sp, const float4* tw,
-                                bool forward_sign, int E, int threads, size_t smem, int grid, cudaStream_t st) {
+cudaError_t launch_strided_pipe(const CUtensorMap* map, const CUtensorMap* omap, const SPipeParams& p,
+                                const StagePlan* sp, const float4* tw, bool forward_sign, int E, int threads,
+                                size_t smem, int grid, cudaStream_t st) {
   if constexpr (P::kF64) {
-    if (E == 8) return launch_strided_pipe_e<P, 8>(map, p, sp, tw, forward_sign, threads, smem, grid, st);
-    if (E == 16) return launch_strided_pipe_e<P, 16>(map, p, sp, tw, forward_sign, threads, smem, grid, st);
+    if (E == 8) return launch_strided_pipe_e<P, 8>(map, omap, p, sp, tw, forward_sign, threads, smem, grid, st);
+    if (E == 16) return launch_strided_pipe_e<P, 16>(map, omap, p, sp, tw, forward_sign, threads, smem, grid, st);
   } else {
-    if (E == 16) return launch_strided_pipe_e<P, 16>(map, p, sp, tw, forward_sign, threads, smem, grid, st);
-    if (E == 32) return launch_strided_pipe_e<P, 32>(map, p, sp, tw, forward_sign, threads, smem, grid, st);
+    if (E == 16) return launch_strided_pipe_e<P, 16>(map, omap, p, sp, tw, forward_sign, threads, smem, grid, st);
+    if (E == 32) return launch_strided_pipe_e<P, 32>(map, omap, p, sp, tw, forward_sign, threads, smem, grid, st);
   }
   return cudaErrorInvalidValue;
 }
@@ -514,8 +515,9 @@ int pipe_blocks_per_sm(int kind, int E, int threads, size_t smem) {
   template cudaError_t launch_cheby<P>(const ChebyParams&, int, cudaStream_t);                                     \
   template cudaError_t launch_x_long<P>(int, const XLongParams&, int, cudaStream_t);                               \
   template int pipe_blocks_per_sm<P>(int, int, int, size_t);                                                            \
-  template cudaError_t launch_strided_pipe<P>(const CUtensorMap*, const SPipeParams&, const StagePlan*,             \
-                                              const float4*, bool, int, int, size_t, int, cudaStream_t);          \
+  template cudaError_t launch_strided_pipe<P>(const CUtensorMap*, const CUtensorMap*, const SPipeParams&,         \
+                                              const StagePlan*, const float4*, bool, int, int, size_t, int,       \
+                                              cudaStream_t);                                                      \
   template cudaError_t launch_xr2c_pipe<P>(const XPipeParams&, const StagePlan*, const float4*, int, int, size_t,  \
                                            int, cudaStream_t);                                                     \
   template cudaError_t launch_xc2r_pipe<P>(const XPipeParams&, const StagePlan*, const float4*, int, int, size_t,  \

@@ -35,6 +35,12 @@ struct SPipeParams {
   int box_bytes;
   int tx_extra;             // test hook: bytes the barrier expects beyond the boxes (0)
   int chunk;                // cp.async bytes per element copy (16 or 8)
+  // 1: the transformed tile leaves by TMA stores (one thread, asynchronous)
+  // in onbox boxes of obrows rows; the kernel then keeps nbuf = 3 buffers
+  // and loads one tile ahead, so a buffer is reloaded two iterations after
+  // its store was issued
+  int tma_store;
+  int obrows, onbox;
 };
 
 struct XPipeParams {
@@ -359,9 +365,11 @@ P3G_D void cp_async_wait_ahead(int nbuf) {
 
 template <class P, int DIR, int E>
 __global__ void __launch_bounds__(PipeLimits<P, E>::kMaxThreads, PipeLimits<P, E>::kMinBlocks)
-    k_strided_pipe(const __grid_constant__ CUtensorMap tin, const __grid_constant__ SPipeParams pp,
-                   const StagePlan* __restrict__ sp, const float4* __restrict__ tw_g) {
+    k_strided_pipe(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
+                   const __grid_constant__ SPipeParams pp, const StagePlan* __restrict__ sp,
+                   const float4* __restrict__ tw_g) {
   const int nb = pp.c.nbuf;
+  const int la = nb - 1 - pp.tma_store;  // tiles loaded ahead of the current one
   {
     const StridedSmem<P> sm = strided_smem<P>(pp.c);
     for (int i = threadIdx.x; i < pp.c.tw_count; i += blockDim.x) sm.tw[i] = __ldg(tw_g + pp.c.tw_base + i);
@@ -375,8 +383,8 @@ __global__ void __launch_bounds__(PipeLimits<P, E>::kMaxThreads, PipeLimits<P, E
   uint32_t amax = 0;
   int it = 0;
   int tile = blockIdx.x;
-  // tiles of the first nb - 1 iterations in flight before the loop
-  for (int j = 0; j < nb - 1; ++j) {
+  // tiles of the first la iterations in flight before the loop
+  for (int j = 0; j < la; ++j) {
     const int t = tile + j * (int)gridDim.x;
     if (t < pp.c.ntiles) strided_issue<P>(pp, &tin, t, j);
     else if (!pp.use_tma) cp_async_commit();
@@ -387,9 +395,16 @@ __global__ void __launch_bounds__(PipeLimits<P, E>::kMaxThreads, PipeLimits<P, E
     bool ok = true;
     {
       const SPipeParams& q = pp;
-      const int ahead = tile + (nb - 1) * (int)gridDim.x;  // into the buffer the last iteration released
-      if (ahead < q.c.ntiles) strided_issue<P>(q, &tin, ahead, b == 0 ? nb - 1 : b - 1);
-      else if (!q.use_tma) cp_async_commit();  // one group per iteration
+      // into the buffer of iteration it + la - nb (with TMA stores: the
+      // store issued two iterations ago, which must have read its tile)
+      const int ahead = tile + la * (int)gridDim.x;
+      const int bl = b + la >= nb ? b + la - nb : b + la;
+      if (ahead < q.c.ntiles) {
+        if (q.tma_store && threadIdx.x == 0) bulk_wait_read<1>();
+        strided_issue<P>(q, &tin, ahead, bl);
+      } else if (!q.use_tma) {
+        cp_async_commit();  // one group per iteration
+      }
       if (q.use_tma) ok = mbar_wait_bounded(&strided_smem<P>(q.c).mbar[b], ph, q.c.err);
       else cp_async_wait_ahead(nb);
     }
@@ -404,7 +419,19 @@ __global__ void __launch_bounds__(PipeLimits<P, E>::kMaxThreads, PipeLimits<P, E
     {
       int xt, o1, o2;
       strided_decode(pp, tile, xt, o1, o2);
-      strided_store<P>(pp.s, strided_smem<P>(pp.c).buf0 + b * pp.c.buf_elems, xt, o1, o2, k);
+      const typename P::W* tb = strided_smem<P>(pp.c).buf0 + b * pp.c.buf_elems;
+      if (pp.tma_store) {
+        fence_proxy_async_smem();  // this thread's tile writes, before the async-proxy reads
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          constexpr int kWords = sizeof(typename P::W) / 4;
+          for (int i = 0; i < pp.onbox; ++i)
+            tma_store_4d(&tout, tb + i * pp.obrows * pp.s.M, xt * pp.s.M * kWords, i * pp.obrows, o1, o2);
+          bulk_commit_group();
+        }
+      } else {
+        strided_store<P>(pp.s, tb, xt, o1, o2, k);
+      }
     }
     __syncthreads();
     if (++b == nb) {
@@ -417,13 +444,17 @@ __global__ void __launch_bounds__(PipeLimits<P, E>::kMaxThreads, PipeLimits<P, E
   if (pp.use_tma) {
     if (threadIdx.x == 0) {
       const StridedSmem<P> sm = strided_smem<P>(pp.c);
-      for (int j = 0; j < nb; ++j)
-        if (tile + j * (int)gridDim.x < pp.c.ntiles)
-          mbar_wait_bounded(&sm.mbar[(it + j) % nb], ((it + j) / nb) & 1, nullptr);
+      for (int j = 0; j <= la; ++j)
+        if (tile + j * (int)gridDim.x < pp.c.ntiles) {
+          const int i = it + j;
+          mbar_wait_bounded(&sm.mbar[i % nb], (i / nb) & 1, nullptr);
+        }
     }
   } else {
     cp_async_wait<0>();
   }
+  // the tile stores must have completed before the CTA's shared memory goes
+  if (pp.tma_store && threadIdx.x == 0) bulk_wait_all();
   range_flush(pp.s.range, amax);
 }
 

@@ -293,6 +293,10 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   ap.pipe_smem = smem_for(M, buf_bytes, ap.pipe_nbuf);
   ap.buf_elems = (int)(buf_bytes / esize);
   ap.pipe_ok = ap.pipe_smem <= 227 * 1024;
+  // the strided kernels' TMA-store form: a third buffer drains the stores
+  ap.pipe_smem3 = 0;
+  if (!xk && smem_for(M, buf_bytes, 3) <= 227 * 1024 && warps_for(M, 3) >= warps_for(M, 2))
+    ap.pipe_smem3 = smem_for(M, buf_bytes, 3);
 }
 
 
@@ -506,8 +510,9 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
     pp.c.nbuf = ap.pipe_nbuf;
     pp.c.err = p->d_err;
     pp.chunk = esize;
-    CUtensorMap map;
+    CUtensorMap map, omap;
     std::memset(&map, 0, sizeof(map));
+    std::memset(&omap, 0, sizeof(omap));
     const SParams& q = pp.s;
     if (p->use_tma && q.in_xs == 1 && q.pre <= 1 && identity_rows && !q.xphase &&
         (!q.in_user || device_memory(q.in))) {
@@ -521,10 +526,27 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
         pp.tx_extra = p->tx_extra;
       }
     }
+    // TMA tile stores: workspace-format output rows stored one to one (no
+    // pruning gap, no DST shift, no four-step twiddle), in device memory,
+    // when the axis has room for a third buffer
+    size_t smem = ap.pipe_smem;
+    const bool identity_store = q.smap_s0 >= q.Lout || q.smap_d == 0;
+    if (pp.use_tma && ap.pipe_smem3 && !q.out_user && q.out_xs == 1 && q.post == 0 && identity_store && !q.tw4 &&
+        q.xrow == 0 && aligned_to(q.out, 16) && device_memory(q.out)) {
+      const int obrows = pick_box_rows(q.Lout, ap.n, q.M, esize);
+      if (obrows > 0 && encode_strided_map(&omap, q.out, esize, q.X, q.Lout, q.O1, nv, q.out_axis, q.out_o1,
+                                           q.out_o2, q.M, obrows)) {
+        pp.tma_store = 1;
+        pp.obrows = obrows;
+        pp.onbox = (q.Lout + obrows - 1) / obrows;
+        pp.c.nbuf = 3;
+        smem = ap.pipe_smem3;
+      }
+    }
     const int slots = (max_sms > 0 && max_sms < p->sm_count ? max_sms : p->sm_count) * ap.pipe_bps;
     const int grid = pp.c.ntiles < slots ? pp.c.ntiles : slots;
-    cudaError_t e = launch_strided_pipe<P>(&map, pp, p->d_sp + ap.pipe_sp(), p->d_tw, fwd_sign, ap.pipe_e,
-                                           ap.pipe_threads, ap.pipe_smem, grid, st);
+    cudaError_t e = launch_strided_pipe<P>(&map, &omap, pp, p->d_sp + ap.pipe_sp(), p->d_tw, fwd_sign, ap.pipe_e,
+                                           ap.pipe_threads, smem, grid, st);
     if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("strided pass launch: ") + cudaGetErrorString(e));
     p->launches++;
     return P3G_OK;
@@ -1496,9 +1518,13 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     if (p->z_ok[i]) size_pipe(p->ax_z[i], 0, f64);
   {
     auto bps = [&](AxisPlan& ap, int kind) {
-      if (ap.pipe_ok)
-        ap.pipe_bps = f64 ? pipe_blocks_per_sm<PathF64>(kind, ap.pipe_e, ap.pipe_threads, ap.pipe_smem)
-                          : pipe_blocks_per_sm<PathF32>(kind, ap.pipe_e, ap.pipe_threads, ap.pipe_smem);
+      if (!ap.pipe_ok) return;
+      auto occ = [&](size_t sm) {
+        return f64 ? pipe_blocks_per_sm<PathF64>(kind, ap.pipe_e, ap.pipe_threads, sm)
+                   : pipe_blocks_per_sm<PathF32>(kind, ap.pipe_e, ap.pipe_threads, sm);
+      };
+      ap.pipe_bps = occ(ap.pipe_smem);
+      if (ap.pipe_smem3 && occ(ap.pipe_smem3) < ap.pipe_bps) ap.pipe_smem3 = 0;
     };
     bps(p->ax_x, 2);
     bps(p->ax_y, 0);

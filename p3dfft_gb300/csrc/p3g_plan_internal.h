@@ -31,6 +31,9 @@ struct AxisPlan {
   int pipe_bps = 1;  // resident CTAs per SM of the pipelined kernel
   int pipe_e = 8;    // elements per thread of the pipelined kernel (PipeLimits)
   int pipe_nbuf = 2; // tile buffers of the pipelined kernel
+  // strided passes that store tiles by TMA: three buffers (0: they do not
+  // fit without fewer resident CTAs)
+  size_t pipe_smem3 = 0;
   // F64 wide pipelined kernels (16 points per thread): a second stage plan
   // with radix-16 stages and its twiddle slice; every other kernel runs sp
   StagePlan spw{};
