@@ -526,12 +526,14 @@ int run_strided(p3g_plan p, SParams& s, const AxisPlan& ap, bool fwd_sign, int n
         pp.tx_extra = p->tx_extra;
       }
     }
-    // TMA tile stores: workspace-format output rows stored one to one (no
-    // pruning gap, no DST shift, no four-step twiddle), in device memory,
-    // when the axis has room for a third buffer
+    // TMA tile stores: output rows stored one to one (no pruning gap, no DST
+    // shift, no four-step twiddle) in device memory, when the axis has room
+    // for a third buffer.  Binary64 user output is converted in shared memory
+    // first; binary32 user rows of an odd length (not 16-byte aligned) fail
+    // the tensor map's stride check and keep the thread stores
     size_t smem = ap.pipe_smem;
     const bool identity_store = q.smap_s0 >= q.Lout || q.smap_d == 0;
-    if (pp.use_tma && ap.pipe_smem3 && !q.out_user && q.out_xs == 1 && q.post == 0 && identity_store && !q.tw4 &&
+    if (pp.use_tma && ap.pipe_smem3 && q.out_xs == 1 && q.post == 0 && identity_store && !q.tw4 &&
         q.xrow == 0 && aligned_to(q.out, 16) && device_memory(q.out)) {
       const int obrows = pick_box_rows(q.Lout, ap.n, q.M, esize);
       if (obrows > 0 && encode_strided_map(&omap, q.out, esize, q.X, q.Lout, q.O1, nv, q.out_axis, q.out_o1,
