@@ -87,6 +87,7 @@ struct p3g_plan_s {
   int nxh, nxhp, nxhc, nxhpc, nycph, nzcph;
   long long pitch;
   AxisPlan ax_x, ax_y, ax_z[4];  // z: 0 fft, 1 dct (2(nz-1)), 2 dst (2(nz+1)), 3 none
+  AxisPlan ax_xc;                 // the X c2r pass's pipelined kernel (ax_x for the rest)
   bool z_ok[4];
   float4* d_tw = nullptr;
   StagePlan* d_sp = nullptr;
