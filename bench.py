@@ -46,12 +46,16 @@ CONFIGS = {
 
 MODES = {"pipe_tma": (True, True), "pipe_cpasync": (True, False), "single_tile": (False, False)}
 
-# DRAM bytes (read + write) per algorithmic byte of one launch, from an ncu
-# capture of the strided Y pass on a 1024x1024x32 grid (272.84 MB read +
-# 217.36 MB written for 538.97 MB of 2C model traffic).  The
-# full-size launch moves the same bytes per line, so traffic scales with the
-# model.
-TRAFFIC_PER_ALGO_BYTE = {"k_strided_pipe": (272.841216e6 + 217.356544e6) / 538968064.0}
+# DRAM bytes (read + write) per algorithmic byte of one launch of the
+# dominant kernel, from ncu captures of its Y pass on a 1024x1024x32 grid
+# (273.69 MB read + 225.91 MB written) and its Z passes on a 1024x32x1024
+# grid (273.93 + 222.29 and 270.01 + 224.63 MB), each for 538.97 MB of 2C
+# model traffic; the four launches of a round trip (Y, Z, Z, Y) averaged.
+# The full-size launches move the same bytes per line, so traffic scales
+# with the model.
+TRAFFIC_PER_ALGO_BYTE = {
+    "k_strided_pipe": (2 * (273.687040e6 + 225.914880e6) + (273.926656e6 + 222.291712e6) +
+                       (270.008320e6 + 224.634880e6)) / (4 * 538968064.0)}
 
 
 def load_peaks():
@@ -488,8 +492,8 @@ def run_ours(args):
                      "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                      "peak_kind": peak_kind, "traffic": traffic,
-                     "traffic_source": "ncu DRAM read+write of the 1024x1024x32 Y-pass launch, 0.909 per "
-                                       "algorithmic byte, scaled to this launch",
+                     "traffic_source": "ncu DRAM read+write of the Y pass (1024x1024x32) and Z passes "
+                                       "(1024x32x1024), 0.923 per algorithmic byte, scaled to this launch",
                      "step_bytes_model": bm["rt"],
                      "step_frac": round(bm["rt"] / (ms64 * 1e-3) / 1e9 / peak, 4)},
         "gpu_launches": launches,

@@ -606,7 +606,18 @@ def summarize(reqs, wall_s: float) -> dict:
     import numpy as np
     lat = np.array([r.latency for r in reqs]) * 1e3
     pts = sum(r.points for r in reqs)
-    return {"requests": len(reqs), "p50_ms": round(float(np.percentile(lat, 50)), 3),
-            "p99_ms": round(float(np.percentile(lat, 99)), 3), "mean_ms": round(float(lat.mean()), 3),
-            "throughput_req_s": round(len(reqs) / wall_s, 1), "gpts_per_s": round(pts / wall_s / 1e9, 3),
-            "wall_s": round(wall_s, 3), "f64_requests": sum(1 for r in reqs if r.precision == F64)}
+    out = {"requests": len(reqs), "p50_ms": round(float(np.percentile(lat, 50)), 3),
+           "p99_ms": round(float(np.percentile(lat, 99)), 3), "mean_ms": round(float(lat.mean()), 3),
+           "throughput_req_s": round(len(reqs) / wall_s, 1), "gpts_per_s": round(pts / wall_s / 1e9, 3),
+           "wall_s": round(wall_s, 3), "f64_requests": sum(1 for r in reqs if r.precision == F64)}
+    # the slowest 1 %: time queued (arrival to admission) against time in
+    # flight (admission to completion), and what they were
+    tail = [r for r, l in zip(reqs, lat) if l >= np.percentile(lat, 99)]
+    if tail:
+        out["p99_tail"] = {
+            "requests": len(tail),
+            "queued_ms": round(float(np.mean([r.t_admit - r.arrival for r in tail])) * 1e3, 3),
+            "in_flight_ms": round(float(np.mean([r.t_done - r.t_admit for r in tail])) * 1e3, 3),
+            "mean_points": int(np.mean([r.points for r in tail])),
+            "f64_share": round(sum(1 for r in tail if r.precision == F64) / len(tail), 3)}
+    return out
