@@ -609,60 +609,60 @@ def run_serving(torch, pg, n_requests, plain_f64_gpts, slots=3):
     """Serving form: requests (forward : backward : spectrum = 4:4:2, cubic or
     box grids with sides log-uniform over the 2^a 3^b 5^c values in [32,512],
     10 % asking for FP64 accuracy) through the continuous-batching server with
-    a 150 GB device-memory budget.  Capacity is measured first with a closed
-    loop (all requests queued at once); the timed stream then arrives as a
-    Poisson process at 70 % of that capacity."""
+    a 150 GB device-memory budget, in two runs: every request with its own
+    host input and result (H2D and D2H inside its latency), and every request
+    with its own device input (a view of a device arena; no host transfer).
+    Each run measures its capacity first with a closed loop (600 requests
+    queued at once); its timed stream then arrives as a Poisson process at
+    70 % of that capacity."""
     from p3dfft_gb300 import serve
-    # every request brings its own host input and takes its result back to
-    # the host (views rotating through two 2 GiB page-locked arenas)
-    cap_reqs = serve.make_requests(min(600, n_requests), seed=50)
-    reqs = serve.poisson_arrivals(serve.make_requests(n_requests, seed=5), rate=1.0)  # rate set below
-    serve.attach_host_data(cap_reqs + reqs, arena_bytes=2 << 30)
     srv = serve.Server(budget_bytes=150e9, slots=slots, max_jobs=64, window=4, keep_outputs=False,
                        launch_work=40e6, age_limit=0.008)
-    t = time.time()
-    for r in cap_reqs + reqs:  # plans (tables) resident before the clock starts
-        srv.plan(r.shape, pg.F64 if r.tol < serve.F32_TOL else pg.F32)
-    plan_s = time.time() - t
-    srv.run(serve.make_requests(64, seed=51))  # warm-up
-    t = time.perf_counter()
-    srv.run(cap_reqs)
-    cap_wall = time.perf_counter() - t
-    capacity = len(cap_reqs) / cap_wall
-    rate = 0.7 * capacity
-    serve.poisson_arrivals(reqs, rate=rate, seed=6)
-    launches0 = srv.launches
-    t = time.perf_counter()
-    srv.run(reqs)
-    wall = time.perf_counter() - t
-    out = serve.summarize(reqs, wall)
-    out.update({"arrival_rate_req_s": round(rate, 1), "capacity_req_s": round(capacity, 1),
-                "capacity_gpts_s": round(sum(r.points for r in cap_reqs) / cap_wall / 1e9, 3),
-                "budget_gb": 150, "peak_in_flight_gb": round(srv.peak_in_flight / 1e9, 2),
-                "launches": srv.launches - launches0,
-                "mean_jobs_per_launch": round(float(np.mean(srv.batch_sizes[-(srv.launches - launches0):]
-                                                            or [0])), 2),
-                "slots": len(srv.slots), "plans_resident": len(srv.plans), "plan_setup_s": round(plan_s, 1),
-                "mix": "forward:backward:spectrum 4:4:2, 10% FP64",
+
+    def one(attach, seed_cap, seed_run):
+        cap_reqs = serve.make_requests(min(600, n_requests), seed=seed_cap)
+        reqs = serve.poisson_arrivals(serve.make_requests(n_requests, seed=seed_run), rate=1.0)
+        attach(cap_reqs + reqs)
+        t = time.time()
+        for r in cap_reqs + reqs:  # plans (tables) resident before the clock starts
+            srv.plan(r.shape, pg.F64 if r.tol < serve.F32_TOL else pg.F32)
+        plan_s = time.time() - t
+        srv.run(serve.make_requests(64, seed=51))  # warm-up
+        t = time.perf_counter()
+        srv.run(cap_reqs)
+        cap_wall = time.perf_counter() - t
+        capacity = len(cap_reqs) / cap_wall
+        rate = 0.7 * capacity
+        serve.poisson_arrivals(reqs, rate=rate, seed=6)
+        launches0 = srv.launches
+        t = time.perf_counter()
+        srv.run(reqs)
+        wall = time.perf_counter() - t
+        out = serve.summarize(reqs, wall)
+        out.update({"arrival_rate_req_s": round(rate, 1), "capacity_req_s": round(capacity, 1),
+                    "capacity_gpts_s": round(sum(r.points for r in cap_reqs) / cap_wall / 1e9, 3),
+                    "launches": srv.launches - launches0,
+                    "mean_jobs_per_launch": round(float(np.mean(srv.batch_sizes[-(srv.launches - launches0):]
+                                                                or [0])), 2),
+                    "fallbacks": sum(1 for r in reqs if r.fallback), "plan_setup_s": round(plan_s, 1)})
+        if plain_f64_gpts:
+            out["capacity_vs_plain_f64_1024cubed"] = round(out["capacity_gpts_s"] / plain_f64_gpts, 3)
+        return out
+
+    # every request brings its own host input and takes its result back to the
+    # host (views rotating through two 2 GiB page-locked arenas)
+    out = one(lambda rs: serve.attach_host_data(rs, arena_bytes=2 << 30), 50, 5)
+    out.update({"budget_gb": 150, "peak_in_flight_gb": round(srv.peak_in_flight / 1e9, 2), "slots": len(srv.slots),
+                "plans_resident": len(srv.plans), "mix": "forward:backward:spectrum 4:4:2, 10% FP64",
                 "data": "per request: H2D of its own input and D2H of its result on its launch's stream, "
                         "inside the latency",
-                "fallbacks": sum(1 for r in reqs if r.fallback),
                 "schedule": "least estimated work first, launches bounded at 40M point-equivalents, "
                             "requests waiting 8 ms first"})
-    if plain_f64_gpts:
-        out["capacity_vs_plain_f64_1024cubed"] = round(out["capacity_gpts_s"] / plain_f64_gpts, 3)
-    # closed-loop capacity with device-resident inputs (no host transfers): the
-    # kernels' throughput on the same request mix
-    dev_reqs = serve.make_requests(min(600, n_requests), seed=50)
-    srv.run(serve.make_requests(64, seed=51))
-    t = time.perf_counter()
-    srv.run(dev_reqs)
-    dev_wall = time.perf_counter() - t
-    out["device_resident_capacity_req_s"] = round(len(dev_reqs) / dev_wall, 1)
-    out["device_resident_capacity_gpts_s"] = round(sum(r.points for r in dev_reqs) / dev_wall / 1e9, 3)
-    if plain_f64_gpts:
-        out["device_resident_capacity_vs_plain_f64_1024cubed"] = round(
-            out["device_resident_capacity_gpts_s"] / plain_f64_gpts, 3)
+    # every request transforms its own device buffer (views rotating through
+    # an 8 GiB device arena): the kernels' and the scheduler's share
+    dev = one(lambda rs: serve.attach_device_data(rs, arena_bytes=8 << 30), 52, 7)
+    dev["data"] = "per request: its own input buffer in device memory (no host transfer)"
+    out["device_data"] = dev
     srv.close()
     return out
 

@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <cstddef>
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -132,11 +133,28 @@ struct p3g_batch_s {
   size_t pass_cap = 0;
   int* d_ctl = nullptr;
   size_t ctl_cap = 0;
+  // page-locked staging of the pass table, copied on the launch stream by
+  // the next launch (dirty); `staged` marks the end of that copy, so the
+  // next set_jobs overwrites the staging only after it.  No call waits on
+  // the copy engines' queues, which other streams' bulk copies may fill.
+  BatchPass* h_pass = nullptr;
+  size_t h_cap = 0;
+  bool dirty = false;
+  cudaEvent_t staged = nullptr;
+  bool staged_pending = false;
+  // the launch's error word, copied to page-locked memory after the kernel
+  // on the launch stream; `done` marks the copy
+  int* h_err = nullptr;
+  cudaEvent_t done = nullptr;
+  bool done_pending = false;
+  // the F64 jobs' plans' range words (d_err[0..2] each), copied after the
+  // kernel on the launch stream (and the range record cleared there)
+  int* h_range = nullptr;
+  size_t h_range_cap = 0;  // plans
   int npass = 0, nitems = 0;
   size_t smem = 0;
   int buf_elems = 0;
   int threads = 0, grid = 0;
-  cudaStream_t upload = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   long long launches = 0;
@@ -303,8 +321,13 @@ int p3g_batch_create(p3g_batch* out, int precision) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->upload, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&b->h_err), sizeof(int), cudaHostAllocDefault);
+  if (e == cudaSuccess) *b->h_err = 0;
   if (e != cudaSuccess) {
+    if (b->staged) cudaEventDestroy(b->staged);
+    if (b->done) cudaEventDestroy(b->done);
     delete b;
     return fail(P3G_E_CUDA, std::string("batch create: ") + cudaGetErrorString(e));
   }
@@ -317,7 +340,11 @@ int p3g_batch_destroy(p3g_batch b) {
   b->drop_graph();
   if (b->d_pass) cudaFree(b->d_pass);
   if (b->d_ctl) cudaFree(b->d_ctl);
-  if (b->upload) cudaStreamDestroy(b->upload);
+  if (b->h_pass) cudaFreeHost(b->h_pass);
+  if (b->h_err) cudaFreeHost(b->h_err);
+  if (b->h_range) cudaFreeHost(b->h_range);
+  if (b->staged) cudaEventDestroy(b->staged);
+  if (b->done) cudaEventDestroy(b->done);
   delete b;
   return P3G_OK;
 }
@@ -380,34 +407,66 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
   const size_t pass_bytes = table.size() * sizeof(BatchPass);
   const size_t ctl_bytes = (2 + table.size()) * sizeof(int);
   b->drop_graph();
+  // the table (device and staging) and the counters grow by at least 2x, so
+  // that a server's batches stop reallocating (cudaFree waits for the whole
+  // device) after a few launches
+  auto grow = [](size_t need, size_t cap) { return std::max(need, std::max<size_t>(2 * cap, 16384)); };
+  if (b->staged_pending) {  // the last upload has read the staging
+    e = cudaEventSynchronize(b->staged);
+    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch table upload: ") + cudaGetErrorString(e));
+    b->staged_pending = false;
+  }
   if (pass_bytes > b->pass_cap) {
+    const size_t cap = grow(pass_bytes, b->pass_cap);
     if (b->d_pass) cudaFree(b->d_pass);
     b->d_pass = nullptr;
     b->pass_cap = 0;
-    if (cudaMalloc(&b->d_pass, pass_bytes) != cudaSuccess) {
+    if (cudaMalloc(&b->d_pass, cap) != cudaSuccess) {
       cudaGetLastError();
       return fail(P3G_E_NOMEM, "batch table allocation failed");
     }
-    b->pass_cap = pass_bytes;
+    b->pass_cap = cap;
+  }
+  if (pass_bytes > b->h_cap) {
+    const size_t cap = grow(pass_bytes, b->h_cap);
+    if (b->h_pass) cudaFreeHost(b->h_pass);
+    b->h_pass = nullptr;
+    b->h_cap = 0;
+    if (cudaHostAlloc(reinterpret_cast<void**>(&b->h_pass), cap, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(P3G_E_NOMEM, "batch table staging allocation failed");
+    }
+    b->h_cap = cap;
   }
   if (ctl_bytes > b->ctl_cap) {
+    const size_t cap = grow(ctl_bytes, b->ctl_cap);
     if (b->d_ctl) cudaFree(b->d_ctl);
     b->d_ctl = nullptr;
     b->ctl_cap = 0;
-    if (cudaMalloc(&b->d_ctl, ctl_bytes) != cudaSuccess) {
+    if (cudaMalloc(&b->d_ctl, cap) != cudaSuccess) {
       cudaGetLastError();
       return fail(P3G_E_NOMEM, "batch counter allocation failed");
     }
-    b->ctl_cap = ctl_bytes;
+    b->ctl_cap = cap;
   }
-  e = cudaMemcpyAsync(b->d_pass, table.data(), pass_bytes, cudaMemcpyHostToDevice, b->upload);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_ctl, 0, ctl_bytes, b->upload);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(b->upload);
-  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch table upload: ") + cudaGetErrorString(e));
+  std::memcpy(b->h_pass, table.data(), pass_bytes);
+  b->dirty = true;
   b->host = std::move(table);
   b->plans.clear();
   for (int j = 0; j < njobs; ++j)
     if (std::find(b->plans.begin(), b->plans.end(), jobs[j].plan) == b->plans.end()) b->plans.push_back(jobs[j].plan);
+  if (f64 && b->plans.size() > b->h_range_cap) {
+    const size_t cap = std::max<size_t>(b->plans.size(), 2 * b->h_range_cap);
+    if (b->h_range) cudaFreeHost(b->h_range);
+    b->h_range = nullptr;
+    b->h_range_cap = 0;
+    if (cudaHostAlloc(reinterpret_cast<void**>(&b->h_range), cap * 3 * sizeof(int), cudaHostAllocDefault) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      return fail(P3G_E_NOMEM, "batch range staging allocation failed");
+    }
+    b->h_range_cap = cap;
+  }
   b->npass = (int)b->host.size();
   b->nitems = (int)items;
   b->smem = smem;
@@ -415,6 +474,22 @@ int p3g_batch_set_jobs(p3g_batch b, int njobs, const p3g_job* jobs, int window) 
   b->threads = threads;
   const long long slots = (long long)b->sm_count * per_sm;
   b->grid = (int)std::max(1LL, std::min(slots, items));
+  return P3G_OK;
+}
+
+// The pass table's copy from its staging (when set_jobs changed it), the
+// counter clear, the kernel and the copy of its error word, all on st.
+static int batch_upload(p3g_batch b, cudaStream_t st) {
+  if (!b->dirty) return P3G_OK;
+  // after the previous launch (which reads the table), on whichever stream
+  cudaError_t e = b->done_pending ? cudaStreamWaitEvent(st, b->done, 0) : cudaSuccess;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_pass, b->h_pass, (size_t)b->npass * sizeof(BatchPass), cudaMemcpyHostToDevice,
+                                  st);
+  if (e == cudaSuccess) e = cudaEventRecord(b->staged, st);
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch table upload: ") + cudaGetErrorString(e));
+  b->staged_pending = true;
+  b->dirty = false;
   return P3G_OK;
 }
 
@@ -428,14 +503,28 @@ static int batch_enqueue(p3g_batch b, cudaStream_t st) {
           : batch_launch<PathF32>(b->d_pass, b->npass, b->nitems, b->d_ctl, b->buf_elems, b->grid, b->threads,
                                   b->smem, st);
   if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+  e = cudaMemcpyAsync(b->h_err, b->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (b->prec == P3G_F64)
+    for (size_t i = 0; i < b->plans.size() && e == cudaSuccess; ++i) {
+      e = cudaMemcpyAsync(b->h_range + 3 * i, b->plans[i]->d_err, 3 * sizeof(int), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaMemsetAsync(b->plans[i]->d_err + 1, 0, sizeof(int), st);
+    }
+  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch status copy: ") + cudaGetErrorString(e));
   return P3G_OK;
 }
 
 int p3g_batch_launch(p3g_batch b, void* stream) {
   if (!b || b->nitems == 0) return fail(P3G_E_STATE, "batch has no jobs");
   std::lock_guard<std::mutex> lk(b->mu);
-  int rc = batch_enqueue(b, static_cast<cudaStream_t>(stream));
-  if (rc == P3G_OK) b->launches++;
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int rc = batch_upload(b, st);
+  if (rc == P3G_OK) rc = batch_enqueue(b, st);
+  if (rc == P3G_OK) {
+    if (cudaEventRecord(b->done, st) != cudaSuccess)
+      return fail(P3G_E_CUDA, std::string("batch launch: ") + cudaGetErrorString(cudaGetLastError()));
+    b->done_pending = true;
+    b->launches++;
+  }
   return rc;
 }
 
@@ -446,6 +535,15 @@ int p3g_batch_capture(p3g_batch b) {
   cudaStream_t cs = nullptr;
   cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("capture stream: ") + cudaGetErrorString(e));
+  // the table goes to the device before the capture: replays reuse it
+  int urc = batch_upload(b, cs);
+  if (urc == P3G_OK && cudaStreamSynchronize(cs) != cudaSuccess)
+    urc = fail(P3G_E_CUDA, std::string("batch table upload: ") + cudaGetErrorString(cudaGetLastError()));
+  if (urc != P3G_OK) {
+    cudaStreamDestroy(cs);
+    return urc;
+  }
+  b->staged_pending = false;
   e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   int rc = P3G_OK;
   if (e == cudaSuccess) {
@@ -472,7 +570,9 @@ int p3g_batch_replay(p3g_batch b, void* stream) {
   if (!b || !b->exec) return fail(P3G_E_STATE, "batch has no captured graph");
   std::lock_guard<std::mutex> lk(b->mu);
   cudaError_t e = cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream));
+  if (e == cudaSuccess) e = cudaEventRecord(b->done, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+  b->done_pending = true;
   b->launches++;
   return P3G_OK;
 }
@@ -480,17 +580,20 @@ int p3g_batch_replay(p3g_batch b, void* stream) {
 int p3g_batch_status(p3g_batch b, void* stream) {
   if (!b) return fail(P3G_E_STATE, "batch is NULL");
   cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+  if (e == cudaSuccess && b->done_pending) e = cudaEventSynchronize(b->done);
   if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch: ") + cudaGetErrorString(e));
-  if (!b->d_ctl) return P3G_OK;
-  int err = 0;
-  e = cudaMemcpy(&err, b->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("batch status: ") + cudaGetErrorString(e));
+  if (!b->done_pending) return P3G_OK;
+  const int err = *static_cast<volatile int*>(b->h_err);
   if (err) return fail(P3G_E_CUDA, "batch kernel: a dependency wait timed out");
-  // the F64 jobs' binary64 inputs against the exponent window at their plans' biases
-  for (p3g_plan p : b->plans) {
-    const int rc = p3g_plan_check_range(p, nullptr, nullptr);
-    if (rc) return rc;
-  }
+  // the F64 jobs' binary64 inputs against the exponent window at their plans'
+  // biases, from the words copied after the kernel
+  if (b->prec == P3G_F64)
+    for (size_t i = 0; i < b->plans.size(); ++i) {
+      int w[3];
+      for (int k = 0; k < 3; ++k) w[k] = static_cast<volatile int*>(b->h_range)[3 * i + k];
+      const int rc = plan_range_result(b->plans[i], w, nullptr, nullptr);
+      if (rc) return rc;
+    }
   return P3G_OK;
 }
 
@@ -500,10 +603,15 @@ int p3g_batch_block_pass(p3g_batch b, int pass) {
   std::lock_guard<std::mutex> lk(b->mu);
   // waiters compare the pass's done-counter with this device copy of its tile
   // count; one more than the pass has makes every dependent wait run out
-  const int blocked = b->host[pass].tiles + 1;
-  cudaError_t e = cudaMemcpy(reinterpret_cast<unsigned char*>(b->d_pass + pass) + offsetof(BatchPass, tiles), &blocked,
-                             sizeof(int), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("block pass: ") + cudaGetErrorString(e));
+  // (in the staging, uploaded by the next launch)
+  if (b->staged_pending) {
+    cudaError_t e = cudaEventSynchronize(b->staged);
+    if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("block pass: ") + cudaGetErrorString(e));
+    b->staged_pending = false;
+  }
+  b->h_pass[pass].tiles = b->host[pass].tiles + 1;
+  b->dirty = true;
+  b->drop_graph();
   return P3G_OK;
 }
 

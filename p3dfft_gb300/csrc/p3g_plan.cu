@@ -1331,6 +1331,25 @@ bool valid_op(const char* op) { return op && op[0] && op[1] && op[2]; }
 
 }  // namespace
 
+namespace p3g {
+// p3g_plan_check_range on words w copied from the plan's d_err.
+int plan_range_result(p3g_plan p, const int w[3], int* bias, int* emax) {
+  const uint32_t amax = (uint32_t)w[1];
+  const int ebits = (int)(amax >> 20);
+  if (emax) *emax = ebits == 0 ? -1075 : ebits - 1023;
+  const int need = range_bias(amax, p->log2n);
+  if (bias) *bias = need;
+  if (p->prec != P3G_F64 || p->range_mode == P3G_RANGE_AUTO || ebits == 0 || ebits == 2047) return P3G_OK;
+  // inside the window at the plan's bias?
+  const int E = ebits - 1023 - p->ebias;
+  if (E >= kRangeLo && E <= kRangeTop - p->log2n) return P3G_OK;
+  return fail(P3G_E_RANGE, "F64 transform input of largest magnitude 2^" + std::to_string(ebits - 1023) +
+                               " is outside the exponent window at bias " + std::to_string(p->ebias) +
+                               " (results invalid): call again after p3g_plan_set_range(plan, P3G_RANGE_FIXED, " +
+                               std::to_string(need) + ") or with P3G_RANGE_AUTO");
+}
+}  // namespace p3g
+
 extern "C" {
 
 int p3g_version(void) { return 100; }
@@ -1811,24 +1830,18 @@ int p3g_plan_set_range(p3g_plan p, int mode, int bias) {
 
 int p3g_plan_check_range(p3g_plan p, int* bias, int* emax) {
   if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");
+  if (p->prec != P3G_F64) {  // binary32 inputs are not tracked: nothing to read
+    if (bias) *bias = 0;
+    if (emax) *emax = -1075;
+    return P3G_OK;
+  }
   int w[3] = {0, 0, 0};
   cudaError_t e = cudaMemcpy(w, p->d_err, sizeof(w), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemset(p->d_err + 1, 0, sizeof(int));
   if (e != cudaSuccess) return fail(P3G_E_CUDA, std::string("range read: ") + cudaGetErrorString(e));
-  const uint32_t amax = (uint32_t)w[1];
-  const int ebits = (int)(amax >> 20);
-  if (emax) *emax = ebits == 0 ? -1075 : ebits - 1023;
-  const int need = range_bias(amax, p->log2n);
-  if (bias) *bias = need;
-  if (p->prec != P3G_F64 || p->range_mode == P3G_RANGE_AUTO || ebits == 0 || ebits == 2047) return P3G_OK;
-  // inside the window at the plan's bias?
-  const int E = ebits - 1023 - p->ebias;
-  if (E >= kRangeLo && E <= kRangeTop - p->log2n) return P3G_OK;
-  return fail(P3G_E_RANGE, "F64 transform input of largest magnitude 2^" + std::to_string(ebits - 1023) +
-                               " is outside the exponent window at bias " + std::to_string(p->ebias) +
-                               " (results invalid): call again after p3g_plan_set_range(plan, P3G_RANGE_FIXED, " +
-                               std::to_string(need) + ") or with P3G_RANGE_AUTO");
+  return plan_range_result(p, w, bias, emax);
 }
+
 
 int p3g_plan_status(p3g_plan p) {
   if (!p) return fail(P3G_E_STATE, "P3DFFT error: call setup before other routines");

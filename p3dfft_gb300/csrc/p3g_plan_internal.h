@@ -70,6 +70,9 @@ void make_forward_params(p3g_plan_s* p, const void* in, void* out, void* wa, voi
                          long long dim_out, XParams& x, SParams& y, SParams& z, bool y_zyx = false);
 void make_backward_params(p3g_plan_s* p, const void* in, void* out, void* wa, void* wb, int zi, long long dim_in,
                           long long dim_out, SParams& z, SParams& y, XParams& x, bool y_zyx = false);
+// The range check of p3g_plan_check_range on a copy of the plan's device
+// words w (d_err[0..2]), for callers that copied them asynchronously.
+int plan_range_result(p3g_plan_s* p, const int w[3], int* bias, int* emax);
 // Exponent-window parameters of a pass converting the plan's binary64 user
 // data in (input = true: tracked) or out; allow_auto = false ignores the
 // auto mode (callers that run no reduction first).  Zero on the F32 path.

@@ -114,6 +114,10 @@ class _Slot:
     reqs: list = field(default_factory=list)
     busy: bool = False
     finite: object = None  # per FP32 request of the launch: result finite
+    # page-locked copy of `finite`, written on the slot's stream before its
+    # event: read at retire without a synchronous copy (which would queue
+    # behind other slots' bulk copies on the copy engines)
+    finite_host: object = None
 
 
 class Server:
@@ -371,6 +375,10 @@ class Server:
             # the copies back to the host
             f32 = [r for r in live if r.precision == F32]
             slot.finite = t.stack([t.isfinite(r.out).all() for r in f32]) if f32 else None
+            if f32:
+                if slot.finite_host is None or slot.finite_host.numel() < len(f32):
+                    slot.finite_host = t.empty(max(len(f32), self.max_jobs), dtype=t.bool).pin_memory()
+                slot.finite_host[:len(f32)].copy_(slot.finite, non_blocking=True)
             for r in live:
                 if r.host_out is not None:
                     r.host_out.copy_(r.out, non_blocking=True)
@@ -421,7 +429,7 @@ class Server:
                             r.fallback = True
                             self._rerun(r, F64)
             b._keep = []  # release the work buffers
-        finite = slot.finite.cpu().tolist() if slot.finite is not None else []
+        finite = slot.finite_host[:slot.finite.numel()].tolist() if slot.finite is not None else []
         i32 = 0
         for r in slot.reqs:
             ok = True
@@ -600,6 +608,38 @@ def poisson_arrivals(reqs, rate: float, seed: int = 6):
         t += rng.exponential(1.0 / rate)
         r.arrival = t
     return reqs
+
+
+def attach_device_data(reqs, seed: int = 8, arena_bytes: int = 8 << 30):
+    """Gives every request an input of its own in device memory: a view of a
+    device arena of uniform values in [-1, 1) (binary32 for FP32 requests,
+    binary64, a quarter of the bytes, for FP64 ones; real fields, or complex
+    spectra for backward requests), views rotating through the arena, so
+    each request transforms its own buffer with no host transfer."""
+    import numpy as np
+    import torch
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    n64 = arena_bytes // 4 // 8
+    n32 = (arena_bytes - n64 * 8) // 4
+    arenas = {False: torch.empty(n32, dtype=torch.float32, device="cuda").uniform_(-1, 1, generator=g),
+              True: torch.empty(n64, dtype=torch.float64, device="cuda").uniform_(-1, 1, generator=g)}
+    offs = {False: 0, True: 0}
+    for r in reqs:
+        nx, ny, nz = r.shape
+        f64 = r.tol < F32_TOL
+        a = arenas[f64]
+        if r.kind == "backward":
+            shape_in, dt_in = (nz, ny, nx // 2 + 1), torch.complex128 if f64 else torch.complex64
+        else:
+            shape_in, dt_in = (nz, ny, nx), torch.float64 if f64 else torch.float32
+        n = int(np.prod(shape_in)) * (2 if dt_in.is_complex else 1)
+        if n > a.numel():
+            raise ValueError(f"request {r.rid} needs {n} elements, more than the device arena holds")
+        if offs[f64] + n > a.numel():
+            offs[f64] = 0
+        r.inp = a[offs[f64]:offs[f64] + n].view(dt_in).view(shape_in)
+        offs[f64] = (offs[f64] + n + 63) // 64 * 64
 
 
 def summarize(reqs, wall_s: float) -> dict:
