@@ -640,6 +640,7 @@ def attach_device_data(reqs, seed: int = 8, arena_bytes: int = 8 << 30):
             offs[f64] = 0
         r.inp = a[offs[f64]:offs[f64] + n].view(dt_in).view(shape_in)
         offs[f64] = (offs[f64] + n + 63) // 64 * 64
+    return reqs
 
 
 def summarize(reqs, wall_s: float) -> dict:

@@ -227,6 +227,35 @@ def test_batch_long_lines_use_large_ctas(torch_cuda, prec):
     b.close()
 
 
+def test_batch_new_jobs_launched_on_another_stream(torch_cuda):
+    # set_jobs right after a launch, and the next launch on another stream:
+    # the new table reaches the device only after the running launch, whose
+    # results stay those of its own jobs
+    import p3dfft_gb300 as pg
+    torch = torch_cuda
+    a = _make_jobs(torch, SHAPES[:3], [pg.JOB_ROUNDTRIP] * 3, pg.F32, seed=11)
+    c = _make_jobs(torch, SHAPES[3:6], [pg.JOB_FORWARD] * 3, pg.F32, seed=12)
+    for j in a + c:  # work buffers that outlive every launch
+        j["work"] = torch.empty(j["plan"].work_bytes(j["kind"]), dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    s1.wait_stream(torch.cuda.current_stream())
+    s2.wait_stream(torch.cuda.current_stream())
+    b = pg.Batch(pg.F32).set_jobs(a)
+    for _ in range(3):
+        b.set_jobs(a)
+        b.launch(s1)
+        b.set_jobs(c)
+        b.launch(s2)
+        b.check(s2)
+        b.check(s1)
+    torch.cuda.synchronize()
+    for j in a + c:
+        want = _alone(torch, j["plan"], j["kind"], j["in"])
+        torch.cuda.synchronize()
+        assert torch.equal(j["out"], want)
+    b.close()
+
+
 def test_batch_rejects_mixed_precision(torch_cuda):
     import p3dfft_gb300 as pg
     torch = torch_cuda

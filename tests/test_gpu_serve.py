@@ -123,6 +123,21 @@ def test_serve_requests_with_their_own_host_data(torch_cuda):
     srv.close()
 
 
+def test_serve_requests_with_their_own_device_data(torch_cuda):
+    # each request transforms its own view of a device arena (the bench's
+    # device-data run): the results match the oracle
+    from p3dfft_gb300 import serve
+    reqs = serve.attach_device_data(_small_requests(16, seed=15), seed=4, arena_bytes=64 << 20)
+    inputs = [r.inp.clone() for r in reqs]
+    srv = serve.Server(budget_bytes=8e9, slots=2, max_jobs=6)
+    srv.run(reqs)
+    for r, x in zip(reqs, inputs):
+        assert r.status == "done"
+        r.inp = x
+        _oracle_check(r)
+    srv.close()
+
+
 def test_serve_allocation_failure_fails_only_its_request(torch_cuda):
     # failure injected on the host: the work buffer of every fourth request
     # fails to allocate; the others complete and the budget is freed
