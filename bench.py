@@ -617,7 +617,7 @@ def run_serving(torch, pg, n_requests, plain_f64_gpts, slots=3):
     70 % of that capacity."""
     from p3dfft_gb300 import serve
     srv = serve.Server(budget_bytes=150e9, slots=slots, max_jobs=64, window=4, keep_outputs=False,
-                       launch_work=40e6, age_limit=0.008)
+                       launch_work=20e6, age_limit=0.008)
 
     def one(attach, seed_cap, seed_run):
         cap_reqs = serve.make_requests(min(600, n_requests), seed=seed_cap)
@@ -656,7 +656,7 @@ def run_serving(torch, pg, n_requests, plain_f64_gpts, slots=3):
                 "plans_resident": len(srv.plans), "mix": "forward:backward:spectrum 4:4:2, 10% FP64",
                 "data": "per request: H2D of its own input and D2H of its result on its launch's stream, "
                         "inside the latency",
-                "schedule": "least estimated work first, launches bounded at 40M point-equivalents, "
+                "schedule": "least estimated work first, launches bounded at 20M point-equivalents, "
                             "requests waiting 8 ms first"})
     # every request transforms its own device buffer (views rotating through
     # an 8 GiB device arena): the kernels' and the scheduler's share

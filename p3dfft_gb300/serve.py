@@ -19,9 +19,10 @@ seconds goes first.  Every result of a launch is known only when the whole
 launch ends, so bounded launches keep a small request from waiting for a
 large batch; the size order keeps bursts of small requests from queueing
 behind large ones, and the age limit keeps large requests from starving.
-Measured at 70 % load (10,000 requests of sides 32..512): p99 22 ms FIFO
-against 16 ms with a 40M-point bound, mean 3.4 ms against 2.6 ms, for ~5 %
-less closed-loop capacity.
+Measured at 70 % load (10,000 requests of sides 32..512, each with its own
+device input): p99 10.5 ms with a 20M-point bound against 12.1 ms with 40M
+(8 % more closed-loop capacity) and ~77 ms with 40M and a 4 ms age limit;
+FIFO admission had given p99 22 ms against 16 ms with a 40M bound.
 
 Admission: a request holds its input, output and work buffer while in
 flight, and the sum over in-flight requests stays within the device-memory
@@ -124,7 +125,7 @@ class Server:
     """Continuous-batching transform server on the current CUDA device."""
 
     def __init__(self, budget_bytes: float = 150e9, slots: int = 3, max_jobs: int = 64, window: int = 4,
-                 tuned: bool = False, keep_outputs: bool = True, launch_work: float = 40e6,
+                 tuned: bool = False, keep_outputs: bool = True, launch_work: float = 20e6,
                  age_limit: float = 0.008):
         import torch
         self.torch = torch
