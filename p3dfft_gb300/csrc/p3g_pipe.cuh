@@ -76,16 +76,18 @@ struct PipeLimits {
   static constexpr int kMinBlocks = kWide ? 1 : 65536 / 128 / kMaxThreads;
 };
 
-// X passes: 256-thread CTAs, three per SM (85 registers; 128-thread CTAs
-// with up to 170 registers for the F32 radix-32 stages), with the twiddles
+// X passes: 256-thread CTAs, three per SM (85 registers; for the F32
+// radix-32 stages 64-thread CTAs, six per SM, with up to 170 registers: 1024
+// points X r2c 2.57 -> 2.49 ms at 1024^3 against three 128-thread CTAs; the
+// F64 radix-16 kernel keeps 128-thread CTAs), with the twiddles
 // read from the global table through L1 instead of a shared-memory copy,
 // which leaves room for three double-buffered tiles per SM.  The X passes
 // gain from the extra resident CTAs; the strided passes, whose tiles must
 // stay wide for their long-stride DRAM rows, keep PipeLimits.
 template <class P, int E>
 struct XPipeLimits {
-  static constexpr int kMaxThreads = PipeLimits<P, E>::kWide ? 128 : 256;
-  static constexpr int kMinBlocks = 3;
+  static constexpr int kMaxThreads = PipeLimits<P, E>::kWide ? (P::kF64 ? 128 : 64) : 256;
+  static constexpr int kMinBlocks = PipeLimits<P, E>::kWide && !P::kF64 ? 6 : 3;
 };
 
 // Largest radix compiled into a pipelined kernel (cta_fft's MAXR).

@@ -1520,8 +1520,16 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     if (!size_tile(p->ax_z[3], nz, p->nxhpc, f64, strided_max_m)) p->z_ok[3] = false;
   }
   if (!p->z_ok[0] && !p->z_ok[1] && !p->z_ok[3]) return bad("z length " + std::to_string(nz) + " is too long");
-  size_pipe(p->ax_x, 1, f64);  // r2c and c2r share the tile; c2r needs the larger buffer
-  {
+  // the wide kernels take fewer points per tile line set (fewer threads per
+  // CTA); an axis whose wide tile does not fit runs the narrow kernels
+  auto narrow_if_unfit = [&](AxisPlan& ap, int kind) {
+    if (!ap.pipe_ok && ap.spw_index >= 0) {
+      ap.spw_index = -1;
+      size_pipe(ap, kind, f64);
+    }
+  };
+  auto size_x = [&] {  // r2c and c2r share the tile; c2r needs the larger buffer
+    size_pipe(p->ax_x, 1, f64);
     AxisPlan c2r = p->ax_x;
     size_pipe(c2r, 2, f64);
     if (!c2r.pipe_ok || c2r.pipe_threads != p->ax_x.pipe_threads || c2r.pipe_m != p->ax_x.pipe_m)
@@ -1529,6 +1537,11 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     p->ax_x.buf_elems = c2r.buf_elems;
     p->ax_x.pipe_smem = c2r.pipe_smem;
     p->ax_x.pipe_nbuf = c2r.pipe_nbuf;
+  };
+  size_x();
+  if (!p->ax_x.pipe_ok && p->ax_x.spw_index >= 0) {
+    p->ax_x.spw_index = -1;
+    size_x();
   }
   // the X c2r pass: the same kernel shape, except on the F32 path, whose
   // c2r pass runs the 16-point kernel (1024^3: 3.01 -> 2.80 ms; the r2c pass
@@ -1539,12 +1552,22 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
     size_pipe(p->ax_xc, 2, f64);
   }
   size_pipe(p->ax_y, 0, f64);
+  narrow_if_unfit(p->ax_y, 0);
   for (int i = 0; i < 2; ++i) {
-    if (p->four_y) size_pipe(p->ly[i], 0, f64);
-    if (p->four_z) size_pipe(p->lz[i], 0, f64);
+    if (p->four_y) {
+      size_pipe(p->ly[i], 0, f64);
+      narrow_if_unfit(p->ly[i], 0);
+    }
+    if (p->four_z) {
+      size_pipe(p->lz[i], 0, f64);
+      narrow_if_unfit(p->lz[i], 0);
+    }
   }
   for (int i = 0; i < 4; ++i)
-    if (p->z_ok[i]) size_pipe(p->ax_z[i], 0, f64);
+    if (p->z_ok[i]) {
+      size_pipe(p->ax_z[i], 0, f64);
+      narrow_if_unfit(p->ax_z[i], 0);
+    }
   {
     auto bps = [&](AxisPlan& ap, int kind) {
       if (!ap.pipe_ok) return;
