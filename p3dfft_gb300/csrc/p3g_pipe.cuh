@@ -425,10 +425,10 @@ __global__ void __launch_bounds__(PipeLimits<P, E>::kMaxThreads, PipeLimits<P, E
       if (pp.tma_store) {
         if constexpr (P::kF64) {
           if (pp.s.out_user) {  // binary64 user format, converted in place (16 bytes each)
-            typename P::W* tw = strided_smem<P>(pp.c).buf0 + b * pp.c.buf_elems;
+            typename P::W* tm = strided_smem<P>(pp.c).buf0 + b * pp.c.buf_elems;
             const int ne = pp.s.Lout * pp.s.M;
             for (int e = threadIdx.x; e < ne; e += blockDim.x)
-              reinterpret_cast<typename P::UC*>(tw)[e] = P::to_uc(P::from_w(tw[e]), k);
+              reinterpret_cast<typename P::UC*>(tm)[e] = P::to_uc(P::from_w(tm[e]), k);
           }
         }
         fence_proxy_async_smem();  // this thread's tile writes, before the async-proxy reads
