@@ -131,10 +131,14 @@ int p3g_spectrum(p3g_plan plan, const void* in, double* E, int kmax, double scal
  *                      out double[kmax+1] shell spectrum (p3g_spectrum with
  *                      kmax, scale, flags)
  * p3g_batch_set_jobs builds the work queue (jobs in windows of `window`,
- * pass-major inside a window; <= 0 = one window) and uploads it;
- * p3g_batch_launch enqueues one launch on a stream; p3g_batch_capture
- * records the launch as a CUDA graph that p3g_batch_replay launches.  The job
- * arrays are bound at set_jobs time.  One precision per batch. */
+ * pass-major inside a window; <= 0 = one window) in page-locked staging,
+ * without waiting for the device; p3g_batch_launch enqueues on a stream the
+ * queue's upload (after the previous launch of the batch, on whichever
+ * stream), the launch and the copy of its status words; p3g_batch_capture
+ * uploads the queue and records the launch as a CUDA graph that
+ * p3g_batch_replay launches.  The job arrays are bound at set_jobs time;
+ * the caller keeps them alive and unchanged until the launches that use them
+ * have finished.  One precision per batch. */
 enum { P3G_JOB_ROUNDTRIP = 0, P3G_JOB_FORWARD = 1, P3G_JOB_BACKWARD = 2, P3G_JOB_SPECTRUM = 3 };
 typedef struct {
   p3g_plan plan;
@@ -154,7 +158,9 @@ int p3g_batch_set_jobs(p3g_batch batch, int njobs, const p3g_job* jobs, int wind
 int p3g_batch_launch(p3g_batch batch, void* stream);
 int p3g_batch_capture(p3g_batch batch);
 int p3g_batch_replay(p3g_batch batch, void* stream);
-/* Synchronises the stream and reports a timed-out dependency wait. */
+/* Synchronises the stream and the batch's last launch, then reports a
+ * timed-out dependency wait, or P3G_E_RANGE for F64 jobs whose binary64
+ * inputs left their plans' exponent window. */
 int p3g_batch_status(p3g_batch batch, void* stream);
 /* info = {passes, work items, persistent CTAs, launches so far, threads per
  * CTA (128, or 256 when a line is longer than 2048 points)} */
