@@ -285,8 +285,9 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
   ap.pipe_m = M;
   ap.pipe_log2m = ilog2(M);
   // a third tile buffer (loads two tiles ahead) for the X kernels where it
-  // fits without costing resident warps; the strided kernels keep two (with
-  // three in flight per SM their scattered rows ran 3-15 % slower)
+  // fits without costing resident warps; the strided kernels load one tile
+  // ahead (two loads in flight per CTA ran their scattered rows 3-15 %
+  // slower) and take a third buffer only to drain TMA stores (pipe_smem3)
   size_t buf_bytes = 0;
   ap.pipe_nbuf = 2;
   if (xk && smem_for(M, buf_bytes, 3) <= 227 * 1024 && warps_for(M, 3) >= warps_for(M, 2)) ap.pipe_nbuf = 3;

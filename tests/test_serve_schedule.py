@@ -89,3 +89,21 @@ def test_cancel_pending_request_on_the_host():
     assert srv.cancel(7) is False
     took = srv._select(0)
     assert [r.rid for r in took] == [0, 2]
+
+
+def test_summary_reports_the_slowest_requests():
+    # summarize: percentiles over every request, and for the slowest 1 % the
+    # mean time queued (arrival to admission) against in flight
+    reqs = []
+    for i in range(200):
+        r = _req(i, 32, arrival=0.0)
+        r.t_admit = 0.001
+        r.t_done = 0.002 if i < 198 else 0.101  # two slow requests
+        reqs.append(r)
+    out = serve.summarize(reqs, wall_s=1.0)
+    assert out["requests"] == 200 and out["throughput_req_s"] == 200.0
+    assert out["p50_ms"] == pytest.approx(2.0)
+    tail = out["p99_tail"]
+    assert tail["requests"] == 2
+    assert tail["queued_ms"] == pytest.approx(1.0)
+    assert tail["in_flight_ms"] == pytest.approx(100.0)
