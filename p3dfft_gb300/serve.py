@@ -41,10 +41,13 @@ API with the exponent bias picked on the device; ``Request.fallback``
 records it.
 
 Request data: a request either names a device tensor (``inp``), or brings
-host memory (``host_in``, page-locked for asynchronous copies) that is copied
-to a device buffer of its own on the slot's stream just before its launch;
-with ``host_out`` the result is copied back on the same stream, so the
-request's latency includes its own data movement.  Without either the
+host memory (``host_in``, page-locked): a real input (forward, spectrum) is
+read by the batch kernel's X pass over the host link directly
+(``host_direct``), a complex one (backward, whose Z pass reads strided runs
+that cross the link slowly) is copied to a device buffer of its own on the
+slot's stream just before its launch; with ``host_out`` the result is copied
+back on the same stream, so the request's latency includes its own data
+movement.  Without either the
 request uses the shape's resident input grid.
 
 Failures stay per request: a device buffer that cannot be allocated fails
@@ -126,13 +129,14 @@ class Server:
 
     def __init__(self, budget_bytes: float = 150e9, slots: int = 3, max_jobs: int = 64, window: int = 4,
                  tuned: bool = False, keep_outputs: bool = True, launch_work: float = 20e6,
-                 age_limit: float = 0.008):
+                 age_limit: float = 0.008, host_direct: bool = True):
         import torch
         self.torch = torch
         self.budget = int(budget_bytes)
         self.max_jobs = max_jobs
         self.launch_work = launch_work
         self.age_limit = age_limit
+        self.host_direct = host_direct
         self.window = window
         self.tuned = tuned
         self.keep_outputs = keep_outputs
@@ -345,9 +349,15 @@ class Server:
         live, copies = [], []
         for r in reqs:
             try:
-                if r.host_in is not None:
+                rdt, cdt = self._dtypes(r.precision)
+                if (r.host_in is not None and self.host_direct and r.kind != "backward" and
+                        r.host_in.dtype == rdt and r.host_in.is_contiguous() and r.host_in.is_pinned()):
+                    # a real input in page-locked memory: the X pass reads its
+                    # lines over the host link itself, with no copy queued on
+                    # the copy engines behind other launches' bulk copies
+                    r.inp = r.host_in
+                elif r.host_in is not None:
                     # the request's own data: a device buffer filled on the slot's stream
-                    rdt, cdt = self._dtypes(r.precision)
                     r.inp = self.alloc(tuple(r.host_in.shape), cdt if r.kind == "backward" else rdt)
                     copies.append((r.inp, r.host_in))
                 elif r.inp is None:

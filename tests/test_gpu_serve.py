@@ -108,12 +108,15 @@ def test_serve_poisson_stream_reports_latency(torch_cuda):
     srv.close()
 
 
-def test_serve_requests_with_their_own_host_data(torch_cuda):
-    # each request's input is copied from host memory of its own and its
-    # result copied back: the host results match the oracle
+@pytest.mark.parametrize("host_direct", [True, False])
+def test_serve_requests_with_their_own_host_data(torch_cuda, host_direct):
+    # each request's input comes from host memory of its own (real inputs
+    # read by the kernel over the host link, or every input copied to the
+    # device first) and its result is copied back: the host results match
+    # the oracle
     from p3dfft_gb300 import serve
     reqs = serve.attach_host_data(_small_requests(16, seed=14), seed=3, arena_bytes=64 << 20)
-    srv = serve.Server(budget_bytes=8e9, slots=2, max_jobs=6)
+    srv = serve.Server(budget_bytes=8e9, slots=2, max_jobs=6, host_direct=host_direct)
     srv.run(reqs)
     for r in reqs:
         assert r.status == "done"
