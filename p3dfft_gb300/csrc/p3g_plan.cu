@@ -231,7 +231,7 @@ static void pipe_shape(bool xk, int& max_threads, int& regs) {
 // and two mbarriers in shared memory.  kind: 0 strided, 1 r2c, 2 c2r.  The
 // elements per thread follow the axis's stage plans: 16 on F64 and 32 on F32
 // when the axis has a wide plan, else 8 and 16.
-static void size_pipe(AxisPlan& ap, int kind, bool f64) {
+static void size_pipe(AxisPlan& ap, int kind, bool f64, int thread_cap = 0) {
   ap.pipe_ok = false;
   if (ap.sp.nstages < 1 || ap.sp.has_generic || ap.n < 2) return;
   const size_t esize = f64 ? 16 : 8;
@@ -244,6 +244,7 @@ static void size_pipe(AxisPlan& ap, int kind, bool f64) {
     else pipe_shape<PathF64, 8>(xk, max_threads, regs_max);
   } else if (E == 32) pipe_shape<PathF32, 32>(xk, max_threads, regs_max);
   else pipe_shape<PathF32, 16>(xk, max_threads, regs_max);
+  if (thread_cap > 0 && thread_cap < max_threads) max_threads = thread_cap;
   const bool tw_shared = !xk;  // the X kernels read the global table
   const int n = ap.n;
   const int nh = n / 2 + 1;
@@ -1549,8 +1550,12 @@ int p3g_plan_create_tuned(p3g_plan* out, int nx, int ny, int nz, int nxc, int ny
   // is faster with the radix-32 one, 2.56 against 2.72 ms)
   p->ax_xc = p->ax_x;
   if (!f64 && p->ax_xc.spw_index >= 0) {
+    // and in CTAs of at most 128 threads, six per SM, for power-of-two lines
+    // of 512 points or more (1024: 2.80 -> 2.69 ms; on 768-point lines the
+    // smaller CTAs were slower, 1.82 -> 1.88 ms)
     p->ax_xc.spw_index = -1;
-    size_pipe(p->ax_xc, 2, f64);
+    size_pipe(p->ax_xc, 2, f64, nx >= 512 && (nx & (nx - 1)) == 0 ? 128 : 0);
+    if (!p->ax_xc.pipe_ok) size_pipe(p->ax_xc, 2, f64);
   }
   size_pipe(p->ax_y, 0, f64);
   narrow_if_unfit(p->ax_y, 0);
