@@ -60,8 +60,9 @@ cudaError_t opt_in_smem(const void* func, int bytes) {
 // ------------------------------------------------------------ factorisation
 // Stage radices for length n, ordered by family (32, 16, 8, 4, 2, 3, 5,
 // other primes) as cta_fft expects.  Powers of two use the largest radix
-// allowed (max_pow2: 32 or 16 only on the F32 path, 8 by default on F64, 4 or
-// 2 when a tuner asks) with a smaller remainder; with 32 the 2^a factor is
+// allowed (max_pow2: 16, or 32 for the wide plans, on the F32 path; 8, or 16
+// for the wide plans, on F64; 4 or 2 when a tuner asks) with a smaller
+// remainder; with 32 the 2^a factor is
 // split into the fewest stages of at most 32, as evenly as possible
 // (1024 = 32 x 32, 512 = 32 x 16, 256 = 16 x 16, 128 = 16 x 8).
 static bool factor(int n, int max_pow2, std::vector<int>& radices) {
