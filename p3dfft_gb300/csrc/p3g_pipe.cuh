@@ -1,13 +1,16 @@
-// Pipelined (persistent, double-buffered) pass kernels.
+// Pipelined (persistent, multi-buffered) pass kernels.
 //
-// Each CTA walks a strided list of tiles (grid = SMs x resident CTAs).  While it transforms tile i
-// in shared buffer b, the copy of tile i+1 into buffer b^1 is already in
-// flight (TMA tensor tiles or cp.async), so HBM traffic overlaps the
-// double-float butterflies.  Each tile goes through: a fix-up step in shared
-// memory (format conversion of user data, DCT-I/DST-I extension), the Stockham
-// stages of p3g_engine.cuh with the pass's twiddles held in shared memory for
-// the life of the CTA, and a store step with the pruning map and output
-// format conversion fused in.
+// Each CTA walks a strided list of tiles (grid = SMs x resident CTAs).  While
+// it transforms tile i in one shared buffer, the copy of the next tile (two
+// tiles ahead in the X kernels with three buffers) is already in flight (TMA
+// tensor tiles, bulk copies or cp.async), so HBM traffic overlaps the
+// butterflies.  Each strided tile goes through: a fix-up step in shared
+// memory (format conversion of user data, DCT-I/DST-I extension), the
+// Stockham stages of p3g_engine.cuh with the pass's twiddles held in shared
+// memory for the life of the CTA, and a store step with the pruning map and
+// output format conversion fused in, or, for rows stored one to one, TMA
+// tensor stores issued by one thread (with a third buffer, so a buffer is
+// reloaded only after its store has read it).
 #pragma once
 
 #include <type_traits>
@@ -23,7 +26,7 @@ struct PipeCommon {
   int tiles_per_field;
   int tw_base, tw_count;    // this pass's slice of the twiddle table (float4)
   int buf_elems;            // elements (W) per buffer
-  int nbuf;                 // tile buffers (2 or 3): loads run nbuf - 1 tiles ahead
+  int nbuf;                 // tile buffers (2 or 3): loads run nbuf - 1 tiles ahead (nbuf - 2 with TMA stores)
   int* err;                 // device error flag
 };
 
